@@ -1,0 +1,196 @@
+/*
+ * cycasgpu.h -- C ABI of the GB300 SIMPLE solve (libcycasgpu.so).
+ *
+ * Drop-in boundary for the reference's per-rank solver seams:
+ *   NavierStokesSolver  (NS/navier.h:30-226)   -- CalculateVelocity / CalculatePressure /
+ *                                                UpdateTurKEpsilon / NSSolve
+ *   DataPartition::solve* (NS/MPIStructure.h:224-228, MPIStructure.cpp:234-531)
+ *
+ * Plain C types only: pointers + sizes, no C++ or torch types.  Every call returns an
+ * int status (CYCAS_OK = 0) and never throws; the text of the last error of the calling
+ * thread is available from cycas_last_error().  A context owns all device state of one
+ * case and one CUDA stream; its calls must come from one host thread at a time.
+ */
+#ifndef CYCASGPU_H
+#define CYCASGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+enum {
+  CYCAS_OK = 0,
+  CYCAS_NOT_CONVERGED = 1,  /* a Krylov solve ended with a negative KSP reason; the reference
+                               throws ConvergeError{iter,residual,varname} here
+                               (BasicType.h:62-68, MPIStructure.cpp:279-282) */
+  CYCAS_NAN_DETECTED = 2,   /* NaN/Inf residual norm (KSP_DIVERGED_NANORINF) */
+  CYCAS_ERR_INVALID = 3,    /* bad argument / unknown name / size mismatch */
+  CYCAS_ERR_CUDA = 4,       /* CUDA runtime error */
+  CYCAS_ERR_ALLOC = 5,      /* device or host allocation failed */
+  CYCAS_ERR_IO = 6,         /* param or mesh file unreadable */
+  CYCAS_ERR_TIMEOUT = 7,    /* a bounded device-side wait ran out (kernel returned early) */
+  CYCAS_ERR_MESH = 8,       /* mesh rejected by the reference's own checks */
+  CYCAS_ERR_UNSUPPORTED = 9 /* option outside the steady, constant-density path */
+};
+
+/* KSP converged reasons reported in cycas_solve_stats.reason (PETSc enum values) */
+enum {
+  CYCAS_KSP_CONVERGED_RTOL = 2,
+  CYCAS_KSP_CONVERGED_ATOL = 3,
+  CYCAS_KSP_DIVERGED_ITS = -3,
+  CYCAS_KSP_DIVERGED_DTOL = -4,
+  CYCAS_KSP_DIVERGED_BREAKDOWN = -5,
+  CYCAS_KSP_DIVERGED_NANORINF = -9
+};
+
+/* preconditioners */
+enum {
+  CYCAS_PC_NONE = 0,
+  CYCAS_PC_JACOBI = 1,   /* PCJACOBI: z = r / diag(A) */
+  CYCAS_PC_ILU0 = 2      /* ILU(0) in the natural (reference) cell order -- PETSc's
+                            one-rank default PC; triangular solves level-scheduled */
+};
+
+/* systems, in the order of the reference's three solve wrappers */
+enum { CYCAS_SYS_VELOCITY = 0, CYCAS_SYS_PRESSURE = 1, CYCAS_SYS_SCALAR = 2 };
+
+/* ---- host-side case (param.in + gmsh v2 ASCII mesh) ------------------------------- */
+typedef struct cycas_case cycas_case;
+
+/* Reads a param.in (NS/readparamfile.cpp:10-344) and the gmsh mesh it names
+ * (RootProcess::read, NS/RootStructure.cpp:428-487), numbers elements as the reference
+ * does at one rank (RootStructure.cpp:797-816), builds the face list in the reference's
+ * discovery order (CreateFaces/FindFace, NS/geometry.cpp:222-358) and the initial fields
+ * (InitFlowField, NS/navier.cpp:588-697).  A relative gridfile is resolved against the
+ * directory of param_path. */
+int cycas_case_load(const char* param_path, cycas_case** out);
+void cycas_case_free(cycas_case* c);
+/* dims: [0] Ncel [1] Nfac [2] Nbnd [3] Nvrt [4] TurModel [5] MaxStep [6] cellPressureRef [7] nnz */
+int cycas_case_dims(const cycas_case* c, int64_t dims[8]);
+/* residual stop value and relaxation factors of the case (dbOptions, NS/navier.cpp:777-791) */
+int cycas_case_params(const cycas_case* c, double* residual_steady, double urf[8], double gravity[3]);
+/* integer topology arrays by name (face_cell1, face_cell2, face_bnd, face_vertices, cell_nface,
+ * cell_face, cell_cell, cell_vertices, cell_rid, bnd_face, bnd_rid, bnd_type, bnd_vertices) */
+int cycas_case_get_int(const cycas_case* c, const char* name, int32_t* dst, int64_t n);
+
+/* ---- mesh view for callers that already hold the reference's Face/Cell/Bnd arrays --- */
+typedef struct {
+  int32_t ncel, nfac, nbnd, nvrt;
+  /* topology, reference order (FaceData/CellData/BoundaryData, NS/BasicType.h:151-243) */
+  const int32_t* face_cell1;    /* [nfac] */
+  const int32_t* face_cell2;    /* [nfac]  < 0 on boundary faces */
+  const int32_t* face_bnd;      /* [nfac]  boundary index, < 0 on interior faces */
+  const int32_t* face_vertices; /* [4*nfac] (needed only when geometry is computed here) */
+  const int32_t* cell_nface;    /* [ncel] */
+  const int32_t* cell_face;     /* [6*ncel] row-major, cell_face[6*i+j] = Cell[i].face[j] */
+  const int32_t* cell_cell;     /* [6*ncel] row-major, neighbour or < 0 */
+  const int32_t* cell_vertices; /* [8*ncel] hex-form vertex list (needed only for geometry) */
+  const int32_t* bnd_face;      /* [nbnd] */
+  const int32_t* bnd_type;      /* [nbnd] regionMap[Bnd[i].rid].type1: 1 wall 2 inlet 3 outlet 4 sym */
+  const double* vert;           /* [3*nvrt] (needed only for geometry) */
+  /* geometry (CellFaceInfo, NS/geometry.cpp:391-752).  If face_x is NULL, all geometry is
+   * computed on the device from vert/face_vertices/cell_vertices, bit-identical to the
+   * reference's formulas evaluated without contraction. */
+  const double* face_x;         /* [3*nfac] */
+  const double* face_n;         /* [3*nfac] */
+  const double* face_area;      /* [nfac] */
+  const double* face_lambda;    /* [nfac] */
+  const double* face_rlencos;   /* [nfac] */
+  const double* face_xpac;      /* [3*nfac] */
+  const double* face_xnac;      /* [3*nfac] */
+  const double* cell_vol;       /* [ncel] */
+  const double* cell_x;         /* [3*ncel] */
+  const double* bnd_distance;   /* [nbnd] */
+} cycas_mesh_view;
+
+typedef struct {
+  int32_t turb_model;        /* TurModel: 0 laminar, 1 k-epsilon */
+  int32_t density_model;     /* must be 0 (constant density) */
+  int32_t cell_pressure_ref; /* cellPressureRef */
+  double urf[8];             /* URF[0..7] */
+  double gravity[3];
+} cycas_params;
+
+typedef struct {
+  int32_t restart;   /* GMRES(m), default 30 */
+  int32_t pc;        /* CYCAS_PC_* */
+  double rtol;       /* <= 0: the reference's per-call value (1e-8 velocity/scalar, 1e-6 pressure) */
+  int32_t maxit;     /* <= 0: the reference's per-call value (1000 velocity/pressure, 500 scalar) */
+  int32_t reserved;
+} cycas_ksp_options;
+
+typedef struct {
+  cycas_ksp_options ksp[3]; /* indexed by CYCAS_SYS_* */
+  int32_t device;           /* CUDA device ordinal */
+  int32_t reserved[7];
+} cycas_options;
+
+/* fills defaults: GMRES(30), Jacobi, reference tolerances, device 0 */
+void cycas_options_default(cycas_options* o);
+
+/* ---- device context ------------------------------------------------------------------ */
+typedef struct cycas_ctx cycas_ctx;
+
+/* Copies the mesh (and computes geometry if not given) into device memory. */
+int cycas_create(const cycas_mesh_view* mesh, const cycas_params* params, const cycas_options* opt,
+                 cycas_ctx** out);
+/* Same from a loaded case; fields start at the case's InitFlowField state. */
+int cycas_create_from_case(const cycas_case* c, const cycas_options* opt, cycas_ctx** out);
+void cycas_destroy(cycas_ctx* ctx);
+
+/* Named device arrays: cell fields U V W P R T TE ED deltaP VisLam VisTur Apr; face field RUFace;
+ * boundary arrays BRo BU BV BW BPre BTE BED; gradients dUdX dVdX dWdX dPdX dPhidX ([3*Ncel]);
+ * geometry face_x face_n face_area face_lambda face_rlencos face_xpac face_xnac cell_vol cell_x
+ * bnd_distance; matrix values A_val (+ b0 b1 b2 right-hand sides) of the last assembled system.
+ * Host buffers; the call synchronises the context's stream. */
+int cycas_get_field(cycas_ctx* ctx, const char* name, double* dst, int64_t n);
+int cycas_set_field(cycas_ctx* ctx, const char* name, const double* src, int64_t n);
+int cycas_get_int(cycas_ctx* ctx, const char* name, int32_t* dst, int64_t n); /* A_rowptr, A_col */
+
+typedef struct {
+  int32_t its[8];      /* Krylov iterations of each solve of the iteration, in call order */
+  int32_t reason[8];   /* KSP converged reason of each solve */
+  double rnorm[8];     /* final preconditioned residual norm of each solve */
+  int32_t nsolves;
+  int32_t failed_solve;/* index of the first solve with reason < 0, or -1 */
+} cycas_iter_stats;
+
+/* One steady SIMPLE-C iteration (NS/navier.cpp:60-111): CalculateVelocity, CalculatePressure,
+ * UpdateTurKEpsilon when TurModel==1.  residual[10] receives the reduced localRes, *resmax
+ * vec_max(residual).  Returns CYCAS_NOT_CONVERGED if any solve reported reason < 0. */
+int cycas_simple_iteration(cycas_ctx* ctx, double residual[10], double* resmax, cycas_iter_stats* stats);
+
+/* Runs n iterations back to back on the device and reads the residual history once at the
+ * end (no host synchronisation between iterations). res_hist: [n*10], resmax: [n], its: [n*8]. */
+int cycas_simple_iterations(cycas_ctx* ctx, int32_t n, double* res_hist, double* resmax, int32_t* its,
+                            int32_t* reasons);
+
+/* Individual stages for parity tests: bc_velocity bc_pressure bc_deltap grad_uvwp grad_deltap
+ * build_velocity ruface2 build_pressure correct_cells correct_ruface calculate_velocity
+ * calculate_pressure keps clear_residual. */
+int cycas_run_stage(cycas_ctx* ctx, const char* stage);
+
+/* DataPartition::solveVelocity_GMRES / solvePressureCorrection / solveScarlar_GMRES
+ * (MPIStructure.cpp:234-531) on the system last assembled for `sys`; x is solved in place
+ * (device-resident fields are used when x is NULL: U/V/W, deltaP, or the scalar being
+ * transported).  tol/maxit as the reference passes them. */
+typedef struct {
+  int32_t its;
+  int32_t reason;
+  double rnorm;
+} cycas_solve_stats;
+
+/* Standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
+ * col[nnz], double val[nnz]); b and x are host arrays, x holds the initial guess unless
+ * guess_zero.  Same GMRES/PC as the SIMPLE path. */
+int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
+                    double* x, const cycas_ksp_options* ksp, double rtol, int32_t maxit, int32_t guess_zero,
+                    cycas_solve_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CYCASGPU_H */

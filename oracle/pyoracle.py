@@ -1,0 +1,159 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Used by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU arm as the
+checker; the product never imports it.  Parity is unpinned at the PETSc
+boundary (see oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle_cycas.so")
+
+PC_NONE, PC_JACOBI, PC_ILU0 = 0, 1, 2
+VELOCITY, PRESSURE, SCALAR = 0, 1, 2
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_load.restype = C.c_void_p
+        L.orc_load.argtypes = [C.c_char_p]
+        L.orc_free.argtypes = [C.c_void_p]
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_dims.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+        L.orc_get_params.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        for f in (L.orc_get, L.orc_set):
+            f.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_long]
+        L.orc_geti.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_long]
+        L.orc_set_ksp.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.orc_set_ksp_perm.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_long]
+        L.orc_stage.argtypes = [C.c_void_p, C.c_char_p]
+        L.orc_iterate.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_csr_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class OracleCase:
+    """One loaded case (param.in + gmsh mesh) in the CPU restatement."""
+
+    def __init__(self, param_path: str):
+        L = lib()
+        h = L.orc_load(param_path.encode())
+        if not h:
+            raise RuntimeError("oracle load failed: " + L.orc_last_error().decode())
+        self.h = C.c_void_p(h)
+        d = (C.c_int * 8)()
+        L.orc_dims(self.h, d)
+        self.ncel, self.nfac, self.nbnd, self.nvrt, self.turb, self.nnz, self.max_step, self.cell_pref = list(d)
+
+    def close(self):
+        if self.h:
+            lib().orc_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    _SIZES = None
+
+    def _size(self, name):
+        n, f, b = self.ncel, self.nfac, self.nbnd
+        table = {
+            "face_x": 3 * f, "face_n": 3 * f, "face_xpac": 3 * f, "face_xnac": 3 * f,
+            "face_area": f, "face_lambda": f, "face_rlencos": f, "RUFace": f,
+            "cell_vol": n, "cell_x": 3 * n, "bnd_distance": b, "bnd_shear": 3 * b,
+            "dUdX": 3 * n, "dVdX": 3 * n, "dWdX": 3 * n, "dPdX": 3 * n, "dPhidX": 3 * n,
+            "BRo": b, "BU": b, "BV": b, "BW": b, "BPre": b, "BTE": b, "BED": b,
+            "Au_val": self.nnz, "Ap_val": self.nnz, "As_val": self.nnz, "residual": 10,
+            "vert": 3 * self.nvrt,
+            "face_cell1": f, "face_cell2": f, "face_bnd": f, "face_vertices": 4 * f,
+            "cell_nface": n, "cell_rid": n, "cell_face": 6 * n, "cell_cell": 6 * n, "cell_vertices": 8 * n,
+            "bnd_face": b, "bnd_rid": b, "bnd_type": b, "bnd_vertices": 4 * b,
+            "A_rowptr": n + 1, "A_col": self.nnz,
+        }
+        return table.get(name, n)
+
+    def get(self, name):
+        out = np.empty(self._size(name), dtype=np.float64)
+        rc = lib().orc_get(self.h, name.encode(), _ptr(out), out.size)
+        if rc != 0:
+            raise KeyError(f"{name}: rc={rc} {lib().orc_last_error().decode()}")
+        return out
+
+    def geti(self, name):
+        out = np.empty(self._size(name), dtype=np.int32)
+        rc = lib().orc_geti(self.h, name.encode(), _ptr(out), out.size)
+        if rc != 0:
+            raise KeyError(f"{name}: rc={rc} {lib().orc_last_error().decode()}")
+        return out
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        rc = lib().orc_set(self.h, name.encode(), _ptr(a), a.size)
+        if rc != 0:
+            raise KeyError(f"{name}: rc={rc} {lib().orc_last_error().decode()}")
+
+    def params(self):
+        urf = np.empty(8); g = np.empty(3)
+        lib().orc_get_params(self.h, _ptr(urf), _ptr(g))
+        return urf, g
+
+    def set_ksp(self, which, pc=PC_ILU0, restart=30, rtol=-1.0, maxit=-1, perm=None):
+        lib().orc_set_ksp(self.h, which, pc, restart, rtol, maxit)
+        if perm is not None:
+            p = np.ascontiguousarray(perm, dtype=np.int32)
+            lib().orc_set_ksp_perm(self.h, which, _ptr(p), p.size)
+
+    def stage(self, name):
+        rc = lib().orc_stage(self.h, name.encode())
+        if rc != 0:
+            raise RuntimeError(f"stage {name}: {lib().orc_last_error().decode()}")
+
+    def iterate(self, nsteps):
+        res = np.zeros((nsteps, 10)); rm = np.zeros(nsteps)
+        its = np.zeros((nsteps, 8), dtype=np.int32); rs = np.zeros((nsteps, 8), dtype=np.int32)
+        rc = lib().orc_iterate(self.h, nsteps, _ptr(res), _ptr(rm), _ptr(its), _ptr(rs))
+        if rc != nsteps:
+            raise RuntimeError(f"oracle iteration {-rc} failed: {lib().orc_last_error().decode()}")
+        return {"residual": res, "resmax": rm, "ksp_its": its, "ksp_reason": rs}
+
+
+def csr_solve(rowptr, col, val, b, x0=None, pc=PC_JACOBI, restart=30, rtol=1e-8, maxit=1000, guess_zero=True):
+    n = len(rowptr) - 1
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    vl = np.ascontiguousarray(val, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    its = C.c_int(); reason = C.c_int(); rn = C.c_double()
+    rc = lib().orc_csr_solve(n, _ptr(rp), _ptr(cl), _ptr(vl), _ptr(bb), _ptr(x), pc, restart, rtol, maxit,
+                             1 if guess_zero else 0, C.byref(its), C.byref(reason), C.byref(rn))
+    if rc != 0:
+        raise RuntimeError(lib().orc_last_error().decode())
+    return x, its.value, reason.value, rn.value

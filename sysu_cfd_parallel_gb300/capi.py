@@ -1,0 +1,142 @@
+"""ctypes binding of libcycasgpu.so (declarations in include/cycasgpu.h).
+
+The shared library is the product; this module only marshals numpy arrays across the C
+ABI.  Loading fails loudly when the library is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+CYCAS_OK = 0
+CYCAS_NOT_CONVERGED = 1
+CYCAS_NAN_DETECTED = 2
+CYCAS_ERR_INVALID = 3
+CYCAS_ERR_CUDA = 4
+CYCAS_ERR_ALLOC = 5
+CYCAS_ERR_IO = 6
+CYCAS_ERR_TIMEOUT = 7
+CYCAS_ERR_MESH = 8
+CYCAS_ERR_UNSUPPORTED = 9
+
+PC_NONE, PC_JACOBI, PC_ILU0 = 0, 1, 2
+SYS_VELOCITY, SYS_PRESSURE, SYS_SCALAR = 0, 1, 2
+
+_P = C.c_void_p
+_I32P = C.POINTER(C.c_int32)
+_F64P = C.POINTER(C.c_double)
+
+
+class MeshView(C.Structure):
+    _fields_ = [("ncel", C.c_int32), ("nfac", C.c_int32), ("nbnd", C.c_int32), ("nvrt", C.c_int32)] + [
+        (name, _P) for name in (
+            "face_cell1", "face_cell2", "face_bnd", "face_vertices", "cell_nface", "cell_face", "cell_cell",
+            "cell_vertices", "bnd_face", "bnd_type", "vert", "face_x", "face_n", "face_area", "face_lambda",
+            "face_rlencos", "face_xpac", "face_xnac", "cell_vol", "cell_x", "bnd_distance")]
+
+
+class Params(C.Structure):
+    _fields_ = [("turb_model", C.c_int32), ("density_model", C.c_int32), ("cell_pressure_ref", C.c_int32),
+                ("urf", C.c_double * 8), ("gravity", C.c_double * 3)]
+
+
+class KspOptions(C.Structure):
+    _fields_ = [("restart", C.c_int32), ("pc", C.c_int32), ("rtol", C.c_double), ("maxit", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class Options(C.Structure):
+    _fields_ = [("ksp", KspOptions * 3), ("device", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class IterStats(C.Structure):
+    _fields_ = [("its", C.c_int32 * 8), ("reason", C.c_int32 * 8), ("rnorm", C.c_double * 8),
+                ("nsolves", C.c_int32), ("failed_solve", C.c_int32)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("its", C.c_int32), ("reason", C.c_int32), ("rnorm", C.c_double)]
+
+
+# every exported symbol declared in include/cycasgpu.h
+EXPORTS = (
+    "cycas_last_error", "cycas_options_default", "cycas_case_load", "cycas_case_free", "cycas_case_dims",
+    "cycas_case_params", "cycas_case_get_int", "cycas_create", "cycas_create_from_case", "cycas_destroy",
+    "cycas_get_field", "cycas_set_field", "cycas_get_int", "cycas_simple_iteration", "cycas_simple_iterations",
+    "cycas_run_stage", "cycas_csr_solve",
+)
+
+_lib = None
+
+
+class CycasError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"cycas error {code}: {msg}")
+        self.code = code
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libcycasgpu.so (building it first when missing and allowed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError(f"libcycasgpu.so not built at {path}")
+        _build.build()
+    L = C.CDLL(path)
+    L.cycas_last_error.restype = C.c_char_p
+    L.cycas_options_default.argtypes = [C.POINTER(Options)]
+    L.cycas_options_default.restype = None
+    L.cycas_case_load.argtypes = [C.c_char_p, C.POINTER(_P)]
+    L.cycas_case_free.argtypes = [_P]
+    L.cycas_case_free.restype = None
+    L.cycas_case_dims.argtypes = [_P, C.POINTER(C.c_int64)]
+    L.cycas_case_params.argtypes = [_P, _F64P, _F64P, _F64P]
+    L.cycas_case_get_int.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.cycas_create.argtypes = [C.POINTER(MeshView), C.POINTER(Params), C.POINTER(Options), C.POINTER(_P)]
+    L.cycas_create_from_case.argtypes = [_P, C.POINTER(Options), C.POINTER(_P)]
+    L.cycas_destroy.argtypes = [_P]
+    L.cycas_destroy.restype = None
+    L.cycas_get_field.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.cycas_set_field.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.cycas_get_int.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.cycas_simple_iteration.argtypes = [_P, _F64P, _F64P, C.POINTER(IterStats)]
+    L.cycas_simple_iterations.argtypes = [_P, C.c_int32, _P, _P, _P, _P]
+    L.cycas_run_stage.argtypes = [_P, C.c_char_p]
+    L.cycas_csr_solve.argtypes = [C.c_int32, _P, _P, _P, _P, _P, C.POINTER(KspOptions), C.c_double, C.c_int32,
+                                  C.c_int32, C.POINTER(SolveStats)]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().cycas_last_error().decode(errors="replace")
+
+
+def check(rc: int):
+    if rc != CYCAS_OK:
+        raise CycasError(rc, last_error())
+
+
+def ptr(a: np.ndarray):
+    return a.ctypes.data_as(_P)
+
+
+def default_options(pc=PC_JACOBI, restart=30, device=0) -> Options:
+    o = Options()
+    load().cycas_options_default(C.byref(o))
+    for s in range(3):
+        o.ksp[s].pc = pc
+        o.ksp[s].restart = restart
+    o.device = device
+    return o

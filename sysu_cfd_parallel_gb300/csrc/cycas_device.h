@@ -1,0 +1,151 @@
+// Device-resident state of one case and the kernel entry points of libcycasgpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace cycas {
+
+constexpr int kMaxRestart = 32;  // largest GMRES restart length supported
+
+// ---- mesh (structure of arrays; per-cell slot arrays are slot-major [6][ncel]) --------
+struct DevMesh {
+  int ncel = 0, nfac = 0, nbnd = 0, nnz = 0, nvrt = 0;
+  // faces
+  int* f_c1 = nullptr;
+  int* f_c2 = nullptr;
+  int* f_bnd = nullptr;
+  int* f_vert = nullptr;   // [4*nfac]
+  double* f_x = nullptr;   // [3*nfac]
+  double* f_n = nullptr;   // [3*nfac]
+  double* f_area = nullptr;
+  double* f_lambda = nullptr;
+  double* f_rlencos = nullptr;
+  double* f_xpac = nullptr;  // [3*nfac]
+  double* f_xnac = nullptr;  // [3*nfac]
+  // cells
+  int* c_nface = nullptr;
+  int* c_face = nullptr;   // [6][ncel]  Cell[i].face[j] at j*ncel+i (assembly order)
+  int* c_gface = nullptr;  // [6][ncel]  same faces sorted by face index (gradient order)
+  int* c_slot = nullptr;   // [6][ncel]  CSR position of the off-diagonal of face slot j, -1 on boundary
+  int* c_diag = nullptr;   // [ncel]     CSR position of the diagonal
+  int* c_vert = nullptr;   // [8*ncel]
+  double* c_vol = nullptr;
+  double* c_x = nullptr;   // [3*ncel]
+  double* vert = nullptr;  // [3*nvrt]
+  // boundary
+  int* b_face = nullptr;
+  int* b_type = nullptr;
+  double* b_dist = nullptr;
+  // boundary index lists (reference loop order)
+  int n_inlet = 0, n_outlet = 0, n_sym = 0, n_wallcell = 0;
+  int* inlet_list = nullptr;
+  int* outlet_list = nullptr;
+  int* sym_list = nullptr;
+  int* wc_cell = nullptr;   // cells that own at least one wall face
+  int* wc_start = nullptr;  // [n_wallcell+1] into wc_bnd
+  int* wc_bnd = nullptr;    // wall boundary indices of each wall cell, ascending
+  // CSR pattern of every system (diagonal + face neighbours, columns ascending)
+  int* rowptr = nullptr;
+  int* col = nullptr;
+};
+
+struct DevFields {
+  double *U, *V, *W, *P, *R, *T, *TE, *ED, *dp, *VisLam, *VisTur, *Apr, *RUFace;
+  double *BRo, *BU, *BV, *BW, *BPre, *BTE, *BED, *BTem;
+  double *dUdX, *dVdX, *dWdX, *dPdX, *dPhidX;  // [3*ncel]
+  double* shear;                                // [3*nbnd] wall shear (Bnd[].shear)
+  double* old;                                  // [3*ncel] U,V,W before the velocity solve
+  double *Prod, *TES, *EDS, *ApTE, *ApED, *VisTE, *VisED;
+  double *Au, *Ap, *As;                         // values on the shared pattern
+  double *bu, *bv, *bw, *bp, *bs;
+  double *dinv_u, *dinv_p, *dinv_s;             // Jacobi: reciprocal of the diagonal
+};
+
+// per-solve report written by the Krylov kernel
+struct KspOut {
+  int its;
+  int reason;
+  double rnorm;
+};
+
+// one status block per context, read back once per iteration
+struct DevStatus {
+  double localRes[10];
+  KspOut ksp[8];
+  int nsolve;
+  int err;          // bit 0 barrier timeout, bit 1 mesh check failed, bit 2 reverse inlet flow (scalar)
+  int warn_inlet;   // reverse-flow-at-inlet warnings (momentum)
+  int pad;
+};
+
+struct KrylovWork {
+  double* V = nullptr;       // (m+1) vectors of length ldv
+  long ldv = 0;
+  double* part = nullptr;    // block partial sums
+  unsigned* bar = nullptr;   // grid barrier [count, generation]
+  double* red = nullptr;     // residual reduction partials
+  int nblocks = 0;           // persistent grid size
+  int threads = 0;
+  int m = 0;
+};
+
+struct KspConf {
+  int restart;
+  int pc;
+  double rtol;
+  int maxit;
+};
+
+// ---------------------------------------------------------------- launches
+// geometry (CellFaceInfo, NS/geometry.cpp:391-752)
+void launch_geometry(const DevMesh& m, int* d_err, cudaStream_t s);
+
+// boundary conditions, gradients, assembly, corrections (NS/navier_*.cpp)
+void launch_bc_velocity(const DevMesh& m, const DevFields& f, int density_model, bool set_pressure,
+                        cudaStream_t s);
+void launch_bc_deltap(const DevMesh& m, const DevFields& f, cudaStream_t s);
+void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
+                     double* const* grad, cudaStream_t s);
+void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, const double* gravity,
+                     DevStatus* st, cudaStream_t s);
+void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s);
+void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s);
+void launch_correct_cells(const DevMesh& m, const DevFields& f, int cell_pref, double urf_p, double* red,
+                          cudaStream_t s);
+void launch_correct_ruface(const DevMesh& m, const DevFields& f, double urf_p, cudaStream_t s);
+void launch_keps_sources(const DevMesh& m, const DevFields& f, cudaStream_t s);
+void launch_keps_wall(const DevMesh& m, const DevFields& f, cudaStream_t s);
+void launch_scalar(const DevMesh& m, const DevFields& f, const double* phi, const double* bphi,
+                   const double* diff, const double* src, const double* app, double urf_s, DevStatus* st,
+                   cudaStream_t s);
+void launch_clip_te(const DevMesh& m, const DevFields& f, cudaStream_t s);
+void launch_eps_wall_rows(const DevMesh& m, const DevFields& f, cudaStream_t s);
+void launch_finish_keps(const DevMesh& m, const DevFields& f, cudaStream_t s);
+
+// reductions (krylov.cu)
+void launch_residual_uvw(const DevMesh& m, const DevFields& f, double* red, DevStatus* st, cudaStream_t s);
+void launch_finalize_residual(const double* red, int nparts, int slot, DevStatus* st, cudaStream_t s);
+int residual_blocks(int n);
+
+// Krylov
+struct GmresCall {
+  int n;
+  const int* rowptr;
+  const int* col;
+  const double* val;
+  const double* dinv;  // nullptr -> no preconditioner
+  const double* b;
+  double* x;
+  int guess_zero;
+  double rtol;
+  int maxit;
+  int restart;
+  KspOut* out;
+  int* err;
+};
+int gmres_grid(int n, int device_blocks);
+int gmres_max_blocks(int device);
+constexpr int kGmresPartStride = kMaxRestart + 4;
+cudaError_t launch_gmres(const GmresCall& c, KrylovWork& w, cudaStream_t s);
+
+}  // namespace cycas

@@ -1,0 +1,52 @@
+// Host-side case description shared by host_case.cpp and the C ABI.
+#pragma once
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace cycas {
+
+constexpr int VOID_CELL_ON_BOUNDARY = -10;   // NS/navier.h:17
+constexpr int VOID_CELL_ON_INTERFACE = -20;  // NS/navier.h:18
+constexpr int INNER_FACE_BOUNDARY = -10;     // NS/navier.h:19
+
+struct IoError : std::runtime_error { using std::runtime_error::runtime_error; };
+struct ParamError : std::runtime_error { using std::runtime_error::runtime_error; };
+struct MeshError : std::runtime_error { using std::runtime_error::runtime_error; };
+
+struct Region {   // BdRegion (NS/BasicType.h:247-310): types and initial values
+  int type1 = -1, type2 = -1;
+  double fixed = 0.0;
+  double init[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+struct HostCase {
+  // options pool defaults (NS/navier.cpp:475-516)
+  int steady = 1, max_step = 10000, turb_model = 0, density_model = 0, solve_energy = 0;
+  int limiter = 0, restart = 0, noutput = 1, cell_pressure_ref = 0;
+  double residual_steady = 1.e-6, pressure_reference = 1.01325e5;
+  double urf[8] = {0.6, 0.6, 0.6, 0.5, 0.8, 0.8, 0.8, 0.8};
+  double gravity[3] = {0, 0, 0};
+  std::string gridfile;
+  std::map<int, Region> regions;
+
+  int ncel = 0, nfac = 0, nbnd = 0, nvrt = 0;
+  std::vector<double> vert;
+  std::vector<int32_t> cell_vertices, cell_rid, cell_nface, cell_face, cell_cell;
+  std::vector<int32_t> bnd_vertices, bnd_rid, bnd_face, bnd_type;
+  std::vector<int32_t> face_cell1, face_cell2, face_bnd, face_vertices;
+
+  // InitFlowField state
+  std::vector<double> U, V, W, R, T, P, VisLam, VisTur, TE, ED;
+  std::vector<double> BU, BV, BW, BRo, BTem, BTE, BED;
+};
+
+void load_params(HostCase& hc, const std::string& path);
+void load_gmsh(HostCase& hc, const std::string& path);
+void build_faces(HostCase& hc);
+void init_fields(HostCase& hc);
+void load_case(HostCase& hc, const std::string& paramPath);
+
+}  // namespace cycas

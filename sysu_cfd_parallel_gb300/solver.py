@@ -1,0 +1,203 @@
+"""Host-side mirror of the reference's solver seams over the C ABI.
+
+``NavierStokesSolver`` follows NS/navier.h:30-226: a case is read from a ``param.in`` with
+its gmsh mesh, ``CalculateVelocity`` / ``CalculatePressure`` / ``UpdateTurKEpsilon`` run
+the corresponding stages on the GPU and ``NSSolve`` runs the steady outer loop
+(NS/navier.cpp:17-156).  A Krylov failure raises ``ConvergeError`` as the reference does
+(BasicType.h:62-68).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+
+
+class ConvergeError(RuntimeError):
+    """Raised when a Krylov solve ends with a negative converged reason."""
+
+    def __init__(self, iter_: int, residual: float, varname: str):
+        super().__init__(f"{varname} not converge in iter: {iter_}, res {residual:f}")
+        self.iter = iter_
+        self.residual = residual
+        self.varname = varname
+
+
+_SOLVE_NAMES = ("Un", "Vn", "Wn", "Pn", "Tn", "ED", "?", "?")
+
+
+class Case:
+    """param.in + mesh loaded by the library's host code (no GPU needed)."""
+
+    def __init__(self, param_path: str):
+        L = capi.load()
+        h = C.c_void_p()
+        capi.check(L.cycas_case_load(param_path.encode(), C.byref(h)))
+        self._h = h
+        d = (C.c_int64 * 8)()
+        capi.check(L.cycas_case_dims(h, d))
+        (self.ncel, self.nfac, self.nbnd, self.nvrt, self.turb_model, self.max_step, self.cell_pressure_ref,
+         self.nnz) = [int(x) for x in d]
+        rs = C.c_double()
+        urf = (C.c_double * 8)()
+        g = (C.c_double * 3)()
+        capi.check(L.cycas_case_params(h, C.byref(rs), urf, g))
+        self.residual_steady = rs.value
+        self.urf = list(urf)
+        self.gravity = list(g)
+
+    def get_int(self, name: str) -> np.ndarray:
+        sizes = {"face_cell1": self.nfac, "face_cell2": self.nfac, "face_bnd": self.nfac,
+                 "face_vertices": 4 * self.nfac, "cell_nface": self.ncel, "cell_face": 6 * self.ncel,
+                 "cell_cell": 6 * self.ncel, "cell_vertices": 8 * self.ncel, "cell_rid": self.ncel,
+                 "bnd_face": self.nbnd, "bnd_rid": self.nbnd, "bnd_type": self.nbnd, "bnd_vertices": 4 * self.nbnd}
+        out = np.empty(sizes[name], dtype=np.int32)
+        capi.check(capi.load().cycas_case_get_int(self._h, name.encode(), capi.ptr(out), out.size))
+        return out
+
+    def close(self):
+        if self._h:
+            capi.load().cycas_case_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class NavierStokesSolver:
+    """One device-resident case.  ``options`` is a ``capi.Options``."""
+
+    def __init__(self, case: Case, options: capi.Options | None = None):
+        L = capi.load()
+        self.case = case
+        self.options = options or capi.default_options()
+        h = C.c_void_p()
+        capi.check(L.cycas_create_from_case(case._h, C.byref(self.options), C.byref(h)))
+        self._h = h
+        self.step = 0
+        self.Residual = np.zeros(10)
+        self.last_stats = None
+
+    # ---- arrays
+    def _size(self, name):
+        n, f, b = self.case.ncel, self.case.nfac, self.case.nbnd
+        three = {"dUdX", "dVdX", "dWdX", "dPdX", "dPhidX", "cell_x"}
+        faces = {"RUFace", "face_area", "face_lambda", "face_rlencos"}
+        faces3 = {"face_x", "face_n", "face_xpac", "face_xnac"}
+        bnd = {"BRo", "BU", "BV", "BW", "BPre", "BTE", "BED", "BTem", "bnd_distance"}
+        if name in three:
+            return 3 * n
+        if name in faces:
+            return f
+        if name in faces3:
+            return 3 * f
+        if name in bnd:
+            return b
+        if name == "bnd_shear":
+            return 3 * b
+        if name == "old_uvw":
+            return 3 * n
+        if name in ("Au_val", "Ap_val", "As_val"):
+            return self.case.nnz
+        return n
+
+    def get(self, name: str) -> np.ndarray:
+        out = np.empty(self._size(name), dtype=np.float64)
+        capi.check(capi.load().cycas_get_field(self._h, name.encode(), capi.ptr(out), out.size))
+        return out
+
+    def set(self, name: str, values) -> None:
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        capi.check(capi.load().cycas_set_field(self._h, name.encode(), capi.ptr(a), a.size))
+
+    def get_int(self, name: str) -> np.ndarray:
+        n = self.case.ncel + 1 if name == "A_rowptr" else self.case.nnz
+        out = np.empty(n, dtype=np.int32)
+        capi.check(capi.load().cycas_get_int(self._h, name.encode(), capi.ptr(out), out.size))
+        return out
+
+    # ---- reference-facing operations
+    def _raise_for(self, rc, stats):
+        if rc == capi.CYCAS_NOT_CONVERGED and stats is not None and stats.failed_solve >= 0:
+            k = stats.failed_solve
+            raise ConvergeError(stats.its[k], stats.rnorm[k], _SOLVE_NAMES[k])
+        capi.check(rc)
+
+    def stage(self, name: str) -> None:
+        capi.check(capi.load().cycas_run_stage(self._h, name.encode()))
+
+    def CalculateVelocity(self):
+        self.stage("calculate_velocity")
+
+    def CalculatePressure(self):
+        self.stage("calculate_pressure")
+
+    def UpdateTurKEpsilon(self):
+        self.stage("keps")
+
+    def simple_iteration(self):
+        res = (C.c_double * 10)()
+        rm = C.c_double()
+        st = capi.IterStats()
+        rc = capi.load().cycas_simple_iteration(self._h, res, C.byref(rm), C.byref(st))
+        self.last_stats = st
+        self._raise_for(rc, st)
+        self.step += 1
+        self.Residual = np.array(list(res))
+        return rm.value
+
+    def iterate(self, n: int):
+        """n iterations; returns dict(residual [n,10], resmax [n], ksp_its [n,8], ksp_reason [n,8])."""
+        res = np.zeros((n, 10)); rm = np.zeros(n)
+        its = np.zeros((n, 8), dtype=np.int32); rs = np.zeros((n, 8), dtype=np.int32)
+        rc = capi.load().cycas_simple_iterations(self._h, n, capi.ptr(res), capi.ptr(rm), capi.ptr(its), capi.ptr(rs))
+        capi.check(rc)
+        self.step += n
+        return {"residual": res, "resmax": rm, "ksp_its": its, "ksp_reason": rs}
+
+    def NSSolve(self, max_step: int | None = None, residual_steady: float | None = None, callback=None):
+        """Steady outer loop (NS/navier.cpp:52-141): stop when ResMax < ResidualSteady."""
+        max_step = self.case.max_step if max_step is None else max_step
+        tol = self.case.residual_steady if residual_steady is None else residual_steady
+        rm = None
+        for _ in range(max_step):
+            rm = self.simple_iteration()
+            if callback:
+                callback(self.step, rm, self.Residual)
+            if rm < tol:
+                break
+        return rm
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.load().cycas_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def csr_solve(rowptr, col, val, b, x0=None, pc=capi.PC_JACOBI, restart=30, rtol=1e-8, maxit=1000,
+              guess_zero=True):
+    """Standalone GPU GMRES on a host CSR system (cycas_csr_solve)."""
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    vl = np.ascontiguousarray(val, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    n = rp.size - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    k = capi.KspOptions(restart=restart, pc=pc, rtol=0.0, maxit=0)
+    st = capi.SolveStats()
+    rc = capi.load().cycas_csr_solve(n, capi.ptr(rp), capi.ptr(cl), capi.ptr(vl), capi.ptr(bb), capi.ptr(x),
+                                     C.byref(k), rtol, maxit, 1 if guess_zero else 0, C.byref(st))
+    if rc not in (capi.CYCAS_OK, capi.CYCAS_NOT_CONVERGED):
+        capi.check(rc)
+    return x, st.its, st.reason, st.rnorm

@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Benchmark: steady SIMPLE-C iterations of the k-epsilon channel on one GB300.
+
+Workload (a "step" = one SIMPLE-C outer iteration over the whole case):
+  jittered-tet channel 10x1x1, 200x20x20 hexes x 6 Kuhn tets = 480,000 cells, interior nodes
+  jittered U(-0.15h, 0.15h) (seed 2026), inlet U=(1,0,0) with k=1.5(0.05U)^2 and
+  eps=0.09^0.75 k^1.5/0.07, outlet, no-slip walls, rho=1, mu=2e-5; FP64 SIMPLE-C + standard
+  k-epsilon with wall functions; the reference's Krylov methods and tolerances (GMRES(30)
+  rtol 1e-8 for velocity and k/eps with Jacobi, CG rtol 1e-6 for the pressure correction with
+  one aggregation-AMG V-cycle as preconditioner: the reference's ILU(0) needs ~390 CG
+  iterations per solve on this mesh and Jacobi does not converge within its 1000 cap).
+
+Metric: cell-iterations/s = cells x timed iterations / device time (CUDA events on the
+solver's stream).  The working set (fields, face geometry, three CSR systems, Krylov basis)
+is several hundred MB, well above the 129 MB L2, so no explicit L2 flush is done between
+iterations.
+
+--impl reference times the CPU restatement of the reference (oracle/, one core, the
+reference's PETSc defaults: ILU(0) preconditioning) on the same case.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG = {"nx": 200, "ny": 20, "nz": 20, "jitter": 0.15, "seed": 2026}
+WORKLOAD = "kepsilon channel 200x20x20x6 jittered tets (480000 cells), FP64 SIMPLE-C"
+METRIC = "cell-iters/s (steady SIMPLE-C, k-eps channel 480k tets)"
+
+
+def case_dir() -> str:
+    base = os.environ.get("CYCAS_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "cycas_bench_cases"))
+    d = os.path.join(base, "channel_%dx%dx%d_s%d" % (CONFIG["nx"], CONFIG["ny"], CONFIG["nz"], CONFIG["seed"]))
+    return d
+
+
+def make_case() -> str:
+    from sysu_cfd_parallel_gb300 import meshgen
+    d = case_dir()
+    param = os.path.join(d, "param.in")
+    done = os.path.join(d, "complete")
+    if not os.path.exists(done):
+        meshgen.write_case(d, "channel", nx=CONFIG["nx"], ny=CONFIG["ny"], nz=CONFIG["nz"], jitter=CONFIG["jitter"],
+                           seed=CONFIG["seed"], steps=500)
+        open(done, "w").close()
+    return param
+
+
+# ---------------------------------------------------------------- clocks
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.device = device
+        self.p = None
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- roofline bookkeeping
+def krylov_bytes(its_row, turb, n, nnz, restart=30):
+    """Algorithmic bytes of each Krylov launch of one iteration (solve slots in call order).
+
+    CG iteration: reads A (12 nnz + 4 (n+1)), p, z, r, w, x, D^-1 (48 n); writes p, w, x, r, z (40 n).
+    GMRES Arnoldi step j: SpMV + Jacobi (12 nnz + 4 (n+1) + 24 n), CGS dots (8 n (j+2)) and update
+    (8 n (j+1) + 16 n); per restart cycle: initial residual (12 nnz + 4 (n+1) + 40 n) and the
+    solution update (8 n (m_used + 2)).
+    """
+    spmv = 12 * nnz + 4 * (n + 1)
+    kinds = ["gmres", "gmres", "gmres", "cg"] + (["gmres", "gmres"] if turb else [])
+    out = []
+    for slot, kind in enumerate(kinds):
+        its = int(its_row[slot])
+        if its < 0:
+            continue
+        if kind == "cg":
+            b = (spmv + 40 * n) + its * (spmv + 88 * n)
+        else:
+            b = 0
+            left = its
+            while True:
+                m = min(left, restart)
+                b += spmv + 40 * n
+                for j in range(m):
+                    b += spmv + 24 * n + 8 * n * (j + 2) + 8 * n * (j + 1) + 16 * n
+                b += 8 * n * (m + 2)
+                left -= m
+                if left <= 0:
+                    break
+        out.append((kind, slot, its, b))
+    return out
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- arms
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def cpu_sample(param: str, iters: int):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    t0 = time.time()
+    o = po.OracleCase(param)
+    setup = time.time() - t0
+    t0 = time.time()
+    o.iterate(iters)
+    dt = time.time() - t0
+    n = o.ncel
+    o.close()
+    return n * iters / dt, dt, setup, n
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    param = make_case()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    o = po.OracleCase(param)
+    n = o.ncel
+    o.iterate(max(0, args.warmup))
+    t0 = time.time()
+    o.iterate(args.steps)
+    dt = time.time() - t0
+    value = n * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-iters/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": n, "solver": "oracle restatement, ILU(0) (PETSc one-rank default)"},
+        "cpu_baseline": {"value": value, "unit": "cell-iters/s", "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} full SIMPLE iterations of the workload after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": "cell-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from sysu_cfd_parallel_gb300 import capi
+    from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
+
+    param = make_case()
+    case = Case(param)
+    opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+    opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
+    s = NavierStokesSolver(case, opt)
+    n, nnz, turb = case.ncel, case.nnz, case.turb_model == 1
+    stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
+
+    if args.warmup > 0:
+        s.iterate(args.warmup)
+    s.set_profiling(True)
+    s.reset_profile()
+    clocks = Clocks(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    hist = s.iterate(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    prof = s.profile()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * args.steps * world / (ms / 1e3)
+
+    # roofline of the dominant Krylov system
+    per_sys_bytes = {"cg": 0.0, "gmres_vel": 0.0, "gmres_scalar": 0.0}
+    per_sys_launch = {"cg": 0, "gmres_vel": 0, "gmres_scalar": 0}
+    for row in hist["ksp_its"]:
+        for kind, slot, its, b in krylov_bytes(row, turb, n, nnz):
+            key = "cg" if kind == "cg" else ("gmres_vel" if slot < 3 else "gmres_scalar")
+            per_sys_bytes[key] += b
+            per_sys_launch[key] += 1
+    sys_ms = {"gmres_vel": prof["krylov_ms"][0], "cg": prof["krylov_ms"][1], "gmres_scalar": prof["krylov_ms"][2]}
+    dom = max(sys_ms, key=lambda k: sys_ms[k])
+    peak, peak_kind = measured_peak()
+    launches = max(1, per_sys_launch[dom])
+    achieved = (per_sys_bytes[dom] / launches) / (sys_ms[dom] / launches / 1e3) / 1e9 if sys_ms[dom] > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom)
+        except Exception:
+            traffic = None
+
+    # end to end through the C ABI: the caller's host arrays are the state (pinned buffers),
+    # uploaded before and read back after every iteration
+    names_in = ["U", "V", "W", "P", "R", "VisLam", "VisTur", "TE", "ED", "RUFace", "BRo", "BU", "BV", "BW",
+                "BTE", "BED"]
+    names_out = ["U", "V", "W", "P", "VisTur", "TE", "ED", "RUFace"]
+    host = {}
+    for nm in set(names_in) | set(names_out):
+        t = torch.empty(s._size(nm), dtype=torch.float64, pin_memory=True)
+        host[nm] = t.numpy()
+        host[nm][:] = s.get(nm)
+    h2d = sum(host[nm].nbytes for nm in names_in)
+    d2h = sum(host[nm].nbytes for nm in names_out) + 8 * 10
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(e2e_steps):
+        for nm in names_in:
+            s.set(nm, host[nm])
+        s.simple_iteration()
+        for nm in names_out:
+            host[nm][:] = s.get(nm)
+    f1.record(stream)
+    f1.synchronize()
+    e2e_ms = f0.elapsed_time(f1)
+    e2e_value = n * e2e_steps * world / (e2e_ms / 1e3)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_value = n * e2e_steps * world / (float(t.item()) / 1e3)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, setup, _ = cpu_sample(param, args.cpu_iters)
+        cpu = {"value": v, "unit": "cell-iters/s", "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_iters} full SIMPLE iteration(s) of the same 480k-cell case, oracle with "
+                         f"ILU(0) (PETSc one-rank default), {dt:.1f} s after {setup:.1f} s setup"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": n, "faces": case.nfac, "nnz": nnz,
+                       "parallelism": f"replicas{world}", "l2": "working set > 129 MB L2, no flush",
+                       "krylov": "GMRES(30)+Jacobi (u,v,w,k,eps), CG+AMG V-cycle (p'), reference tolerances",
+                       "krylov_its_last_step": [int(x) for x in hist["ksp_its"][-1]]},
+            "e2e": {"value": e2e_value, "unit": "cell-iters/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+            "roofline": {"bound": "hbm", "kernel": {"cg": "k_cg (pressure correction)",
+                                                    "gmres_vel": "k_gmres (momentum)",
+                                                    "gmres_scalar": "k_gmres (k, epsilon)"}[dom],
+                         "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "share_of_step": sys_ms[dom] / ms},
+            "cpu_baseline": cpu,
+            "gpu_launches": int(prof["kernel_launches"]),
+            "profile": {"krylov_ms": sys_ms, "assembly_ms": prof["assembly_ms"],
+                        "krylov_iters": prof["krylov_iters"]},
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-iters", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

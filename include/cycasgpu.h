@@ -50,8 +50,19 @@ enum {
 enum {
   CYCAS_PC_NONE = 0,
   CYCAS_PC_JACOBI = 1,   /* PCJACOBI: z = r / diag(A) */
-  CYCAS_PC_ILU0 = 2      /* ILU(0) in the natural (reference) cell order -- PETSc's
-                            one-rank default PC; triangular solves level-scheduled */
+  CYCAS_PC_ILU0 = 2,     /* ILU(0) in the natural (reference) cell order -- PETSc's
+                            one-rank default PC (not available in this build) */
+  CYCAS_PC_AMG = 3       /* one V-cycle of plain aggregation multigrid (pressure system, CG
+                            only): aggregates of <= 4 cells, weighted Jacobi w = 2/3, coarse
+                            correction scaled by 2, dense coarsest level (<= 64 rows) */
+};
+
+/* Krylov methods */
+enum {
+  CYCAS_KSP_DEFAULT = 0, /* the reference's choice: GMRES, except CG for the constant-density
+                            pressure correction (MPIStructure.cpp:462-464) */
+  CYCAS_KSP_GMRES = 1,
+  CYCAS_KSP_CG = 2       /* PETSc KSPCG algorithm (Hestenes-Stiefel, preconditioned norm) */
 };
 
 /* systems, in the order of the reference's three solve wrappers */
@@ -115,11 +126,11 @@ typedef struct {
 } cycas_params;
 
 typedef struct {
+  int32_t type;      /* CYCAS_KSP_* */
   int32_t restart;   /* GMRES(m), default 30 */
   int32_t pc;        /* CYCAS_PC_* */
   double rtol;       /* <= 0: the reference's per-call value (1e-8 velocity/scalar, 1e-6 pressure) */
   int32_t maxit;     /* <= 0: the reference's per-call value (1000 velocity/pressure, 500 scalar) */
-  int32_t reserved;
 } cycas_ksp_options;
 
 typedef struct {
@@ -128,7 +139,8 @@ typedef struct {
   int32_t reserved[7];
 } cycas_options;
 
-/* fills defaults: GMRES(30), Jacobi, reference tolerances, device 0 */
+/* fills defaults: the reference's Krylov methods (GMRES(30); CG for pressure), Jacobi,
+ * reference tolerances, device 0 */
 void cycas_options_default(cycas_options* o);
 
 /* ---- device context ------------------------------------------------------------------ */
@@ -182,6 +194,21 @@ typedef struct {
   int32_t reason;
   double rnorm;
 } cycas_solve_stats;
+
+/* ---- measurement hooks ------------------------------------------------------------- */
+/* The CUDA stream (cudaStream_t) all work of the context is issued on. */
+int cycas_get_stream(cycas_ctx* ctx, void** stream);
+typedef struct {
+  int64_t kernel_launches;   /* kernels this context launched since the last reset */
+  int64_t krylov_launches[3];/* persistent Krylov launches per system (CYCAS_SYS_*) */
+  int64_t krylov_iters[3];   /* Krylov iterations per system */
+  double krylov_ms[3];       /* CUDA-event time of those launches per system (profiling on) */
+  double assembly_ms;        /* CUDA-event time outside the Krylov launches (profiling on) */
+} cycas_profile;
+/* Profiling records CUDA events around every Krylov launch on the context's stream. */
+int cycas_set_profiling(cycas_ctx* ctx, int32_t on);
+int cycas_get_profile(cycas_ctx* ctx, cycas_profile* out);
+int cycas_reset_profile(cycas_ctx* ctx);
 
 /* Standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
  * col[nnz], double val[nnz]); b and x are host arrays, x holds the initial guess unless

@@ -67,7 +67,10 @@ struct Csr {
 
 enum PcType { PC_NONE = 0, PC_JACOBI = 1, PC_ILU0 = 2 };
 
+enum KspType { KSP_GMRES = 0, KSP_CG = 1 };
+
 struct KspSettings {       // one per system: velocity, pressure, scalar
+  int type = KSP_GMRES;    // the pressure system defaults to CG (see Case)
   int restart = 30;
   int pc = PC_ILU0;
   double rtol_override = -1.0;  // <0: use the caller's tol (the reference's per-solve value)
@@ -80,7 +83,8 @@ struct KspResult { int its = 0; int reason = 0; double rnorm = 0; };
 
 // KSPConvergedReason values used here (PETSc public enum values)
 enum { KSP_CONVERGED_RTOL = 2, KSP_CONVERGED_ATOL = 3, KSP_DIVERGED_ITS = -3, KSP_DIVERGED_DTOL = -4,
-       KSP_DIVERGED_BREAKDOWN = -5, KSP_DIVERGED_NANORINF = -9 };
+       KSP_DIVERGED_BREAKDOWN = -5, KSP_DIVERGED_INDEFINITE_PC = -8, KSP_DIVERGED_NANORINF = -9,
+       KSP_DIVERGED_INDEFINITE_MAT = -10 };
 
 struct Case {
   // options pool, navier.cpp:749-791 and defaults navier.cpp:475-516
@@ -112,7 +116,9 @@ struct Case {
   // linear systems (DataPartition Au/Ap/As + bu,bv,bw,bp,bs)
   Csr Au, Ap, As;
   std::vector<double> bu, bv, bw, bp, bs;
-  KspSettings ksp[3];                // 0 velocity, 1 pressure, 2 scalar
+  // 0 velocity, 1 pressure, 2 scalar.  solvePressureCorrection selects CG when the density
+  // is constant (MPIStructure.cpp:462-464), GMRES otherwise.
+  KspSettings ksp[3] = {KspSettings(), KspSettings{KSP_CG}, KspSettings()};
   std::vector<KspResult> kspLog;     // every solve of the last iteration, in call order
   int kspFailures = 0;
 

@@ -210,7 +210,14 @@ int orc_geti(void* hp, const char* name, int* dst, long n) {
   return copy_out(tmp, dst, n);
 }
 
-// which: 0 velocity, 1 pressure, 2 scalar; pc: 0 none, 1 jacobi, 2 ilu0
+// which: 0 velocity, 1 pressure, 2 scalar; type: 0 gmres, 1 cg; pc: 0 none, 1 jacobi, 2 ilu0
+int orc_set_ksp_type(void* hp, int which, int type) {
+  Case& cs = ((Handle*)hp)->cs;
+  if (which < 0 || which > 2 || type < 0 || type > 1) return -1;
+  cs.ksp[which].type = type;
+  return 0;
+}
+
 int orc_set_ksp(void* hp, int which, int pc, int restart, double rtol_override, int maxit_override) {
   Case& cs = ((Handle*)hp)->cs;
   if (which < 0 || which > 2) return -1;
@@ -288,7 +295,8 @@ int orc_iterate(void* hp, int nsteps, double* res_hist, double* resmax, int* ksp
 
 // standalone Krylov solve on an arbitrary CSR system (for solver unit tests)
 int orc_csr_solve(int n, const int* rowptr, const int* col, const double* val, const double* b, double* x,
-                  int pc, int restart, double rtol, int maxit, int guess_zero, int* its, int* reason, double* rnorm) {
+                  int type, int pc, int restart, double rtol, int maxit, int guess_zero, int* its, int* reason,
+                  double* rnorm) {
   try {
     Csr A;
     A.n = n;
@@ -300,6 +308,7 @@ int orc_csr_solve(int n, const int* rowptr, const int* col, const double* val, c
       for (int k = A.rowptr[i]; k < A.rowptr[i + 1]; k++)
         if (A.col[k] == i) A.diag[i] = k;
     KspSettings s;
+    s.type = type;
     s.pc = pc;
     s.restart = restart;
     KspResult r = ksp_solve(A, s, rtol, maxit, guess_zero != 0, b, x);

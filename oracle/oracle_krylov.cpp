@@ -127,11 +127,89 @@ double dot(const double* a, const double* b, int n) {
 
 }  // namespace
 
+// PETSc KSPCG (Hestenes-Stiefel form, preconditioned-norm convergence test).  It stops
+// only when beta or p'Ap changes sign between iterations, so the negative-definite
+// pressure-correction system is accepted as it stands.
+static KspResult cg_solve(const Csr& A, const Pc& pc, const KspSettings& s, double rtol, int maxit, bool guess_zero,
+                          const double* b, double* x) {
+  const int n = A.n;
+  std::vector<double> r(n), z(n), p(n), w(n);
+  KspResult res;
+  if (guess_zero) {
+    std::fill(x, x + n, 0.0);
+    std::copy(b, b + n, r.begin());
+  } else {
+    spmv(A, x, w.data());
+    for (int i = 0; i < n; i++) r[i] = b[i] - w[i];
+  }
+  pc.apply(r.data(), z.data());
+  double dp = std::sqrt(dot(z.data(), z.data(), n));
+  double rnorm0, ttol;
+  if (!guess_zero) {
+    std::vector<double> t(n);
+    pc.apply(b, t.data());
+    double snorm = std::sqrt(dot(t.data(), t.data(), n));
+    rnorm0 = snorm != 0.0 ? snorm : dp;
+  } else {
+    rnorm0 = dp;
+  }
+  ttol = std::max(rtol * rnorm0, s.abstol);
+  auto test = [&](double rn) -> int {
+    if (std::isnan(rn) || std::isinf(rn)) return KSP_DIVERGED_NANORINF;
+    if (rn <= ttol) return rn < s.abstol ? KSP_CONVERGED_ATOL : KSP_CONVERGED_RTOL;
+    if (rn >= s.dtol * rnorm0) return KSP_DIVERGED_DTOL;
+    return 0;
+  };
+  res.rnorm = dp;
+  res.reason = test(dp);
+  if (res.reason) return res;
+  double beta = dot(z.data(), r.data(), n), betaold = 0.0, dpi = 0.0, dpiold = 0.0;
+  int i = 0;
+  do {
+    res.its = i + 1;
+    if (beta == 0.0) {
+      res.reason = KSP_CONVERGED_ATOL;
+      break;
+    }
+    if (i > 0 && beta * betaold < 0.0) {
+      res.reason = KSP_DIVERGED_INDEFINITE_PC;
+      break;
+    }
+    if (i == 0) {
+      std::copy(z.begin(), z.end(), p.begin());
+    } else {
+      double bb = beta / betaold;
+      for (int k = 0; k < n; k++) p[k] = z[k] + bb * p[k];
+    }
+    dpiold = dpi;
+    spmv(A, p.data(), w.data());
+    dpi = dot(p.data(), w.data(), n);
+    betaold = beta;
+    if (dpi == 0.0 || (i > 0 && ((dpi > 0) - (dpi < 0)) * ((dpiold > 0) - (dpiold < 0)) < 0)) {
+      res.reason = KSP_DIVERGED_INDEFINITE_MAT;
+      break;
+    }
+    double a = beta / dpi;
+    for (int k = 0; k < n; k++) x[k] += a * p[k];
+    for (int k = 0; k < n; k++) r[k] += -a * w[k];
+    pc.apply(r.data(), z.data());
+    dp = std::sqrt(dot(z.data(), z.data(), n));
+    res.rnorm = dp;
+    res.reason = test(dp);
+    if (res.reason) break;
+    beta = dot(z.data(), r.data(), n);
+    i++;
+  } while (i < maxit);
+  if (i >= maxit) res.reason = KSP_DIVERGED_ITS;
+  return res;
+}
+
 KspResult ksp_solve(const Csr& A, const KspSettings& s, double rtol, int maxit, bool guess_zero,
                     const double* b, double* x) {
   const int n = A.n, m = s.restart;
   Pc pc;
   pc.setup(A, s);
+  if (s.type == KSP_CG) return cg_solve(A, pc, s, rtol, maxit, guess_zero, b, x);
   KspResult res;
   std::vector<std::vector<double>> V(m + 1, std::vector<double>(n));
   std::vector<double> hh((m + 1) * m, 0.0), cc(m, 0.0), ss(m, 0.0), grs(m + 1, 0.0), nrs(m, 0.0), t(n), w(n);

@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle_cycas.so")
 
 PC_NONE, PC_JACOBI, PC_ILU0 = 0, 1, 2
+KSP_GMRES, KSP_CG = 0, 1
 VELOCITY, PRESSURE, SCALAR = 0, 1, 2
 
 _lib = None
@@ -42,11 +43,12 @@ def lib():
             f.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_long]
         L.orc_geti.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_long]
         L.orc_set_ksp.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.orc_set_ksp_type.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_set_ksp_perm.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_long]
         L.orc_stage.argtypes = [C.c_void_p, C.c_char_p]
         L.orc_iterate.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_csr_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                    C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                     C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
         _lib = L
     return _lib
@@ -124,8 +126,10 @@ class OracleCase:
         lib().orc_get_params(self.h, _ptr(urf), _ptr(g))
         return urf, g
 
-    def set_ksp(self, which, pc=PC_ILU0, restart=30, rtol=-1.0, maxit=-1, perm=None):
+    def set_ksp(self, which, pc=PC_ILU0, restart=30, rtol=-1.0, maxit=-1, perm=None, ksp_type=None):
         lib().orc_set_ksp(self.h, which, pc, restart, rtol, maxit)
+        if ksp_type is not None:
+            lib().orc_set_ksp_type(self.h, which, ksp_type)
         if perm is not None:
             p = np.ascontiguousarray(perm, dtype=np.int32)
             lib().orc_set_ksp_perm(self.h, which, _ptr(p), p.size)
@@ -144,7 +148,8 @@ class OracleCase:
         return {"residual": res, "resmax": rm, "ksp_its": its, "ksp_reason": rs}
 
 
-def csr_solve(rowptr, col, val, b, x0=None, pc=PC_JACOBI, restart=30, rtol=1e-8, maxit=1000, guess_zero=True):
+def csr_solve(rowptr, col, val, b, x0=None, pc=PC_JACOBI, restart=30, rtol=1e-8, maxit=1000, guess_zero=True,
+              ksp_type=KSP_GMRES):
     n = len(rowptr) - 1
     rp = np.ascontiguousarray(rowptr, dtype=np.int32)
     cl = np.ascontiguousarray(col, dtype=np.int32)
@@ -152,7 +157,7 @@ def csr_solve(rowptr, col, val, b, x0=None, pc=PC_JACOBI, restart=30, rtol=1e-8,
     bb = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
     its = C.c_int(); reason = C.c_int(); rn = C.c_double()
-    rc = lib().orc_csr_solve(n, _ptr(rp), _ptr(cl), _ptr(vl), _ptr(bb), _ptr(x), pc, restart, rtol, maxit,
+    rc = lib().orc_csr_solve(n, _ptr(rp), _ptr(cl), _ptr(vl), _ptr(bb), _ptr(x), ksp_type, pc, restart, rtol, maxit,
                              1 if guess_zero else 0, C.byref(its), C.byref(reason), C.byref(rn))
     if rc != 0:
         raise RuntimeError(lib().orc_last_error().decode())

@@ -30,8 +30,22 @@ UNITS = [
     ("host_case.cpp", "cxx", []),
     ("assembly.cu", "nvcc", ["-fmad=false"]),
     ("krylov.cu", "nvcc", []),
+    ("gmres.cu", "nvcc", []),
+    ("amg.cu", "nvcc", []),
+    ("amg_setup.cpp", "cxx", []),
     ("capi.cu", "nvcc", []),
 ]
+
+
+def _cuda_home() -> str:
+    home = os.environ.get("CUDA_HOME") or os.environ.get("CUDA_PATH")
+    if home:
+        return home
+    import shutil
+    nvcc = shutil.which(NVCC)
+    if nvcc:
+        return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    return "/usr/local/cuda"
 
 
 def _sources_digest() -> str:
@@ -62,7 +76,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(obj)
         path = os.path.join(CSRC, src)
         if kind == "cxx":
-            cmd = [CXX, "-O2", "-std=c++17", "-fPIC", "-Wall", "-c", path, "-o", obj, "-I", INCLUDE]
+            cmd = [CXX, "-O2", "-std=c++17", "-fPIC", "-Wall", "-c", path, "-o", obj, "-I", INCLUDE,
+                   "-I", os.path.join(_cuda_home(), "include")]
         else:
             cmd = [NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
                    *extra, "-c", path, "-o", obj, "-I", INCLUDE]

@@ -23,7 +23,8 @@ CYCAS_ERR_TIMEOUT = 7
 CYCAS_ERR_MESH = 8
 CYCAS_ERR_UNSUPPORTED = 9
 
-PC_NONE, PC_JACOBI, PC_ILU0 = 0, 1, 2
+PC_NONE, PC_JACOBI, PC_ILU0, PC_AMG = 0, 1, 2, 3
+KSP_DEFAULT, KSP_GMRES, KSP_CG = 0, 1, 2
 SYS_VELOCITY, SYS_PRESSURE, SYS_SCALAR = 0, 1, 2
 
 _P = C.c_void_p
@@ -45,8 +46,8 @@ class Params(C.Structure):
 
 
 class KspOptions(C.Structure):
-    _fields_ = [("restart", C.c_int32), ("pc", C.c_int32), ("rtol", C.c_double), ("maxit", C.c_int32),
-                ("reserved", C.c_int32)]
+    _fields_ = [("type", C.c_int32), ("restart", C.c_int32), ("pc", C.c_int32), ("rtol", C.c_double),
+                ("maxit", C.c_int32)]
 
 
 class Options(C.Structure):
@@ -58,6 +59,11 @@ class IterStats(C.Structure):
                 ("nsolves", C.c_int32), ("failed_solve", C.c_int32)]
 
 
+class Profile(C.Structure):
+    _fields_ = [("kernel_launches", C.c_int64), ("krylov_launches", C.c_int64 * 3), ("krylov_iters", C.c_int64 * 3),
+                ("krylov_ms", C.c_double * 3), ("assembly_ms", C.c_double)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("its", C.c_int32), ("reason", C.c_int32), ("rnorm", C.c_double)]
 
@@ -67,7 +73,8 @@ EXPORTS = (
     "cycas_last_error", "cycas_options_default", "cycas_case_load", "cycas_case_free", "cycas_case_dims",
     "cycas_case_params", "cycas_case_get_int", "cycas_create", "cycas_create_from_case", "cycas_destroy",
     "cycas_get_field", "cycas_set_field", "cycas_get_int", "cycas_simple_iteration", "cycas_simple_iterations",
-    "cycas_run_stage", "cycas_csr_solve",
+    "cycas_run_stage", "cycas_csr_solve", "cycas_get_stream", "cycas_set_profiling", "cycas_get_profile",
+    "cycas_reset_profile",
 )
 
 _lib = None
@@ -115,6 +122,10 @@ def load(build_if_missing: bool = True):
     L.cycas_run_stage.argtypes = [_P, C.c_char_p]
     L.cycas_csr_solve.argtypes = [C.c_int32, _P, _P, _P, _P, _P, C.POINTER(KspOptions), C.c_double, C.c_int32,
                                   C.c_int32, C.POINTER(SolveStats)]
+    L.cycas_get_stream.argtypes = [_P, C.POINTER(_P)]
+    L.cycas_set_profiling.argtypes = [_P, C.c_int32]
+    L.cycas_get_profile.argtypes = [_P, C.POINTER(Profile)]
+    L.cycas_reset_profile.argtypes = [_P]
     _lib = L
     return L
 

@@ -908,10 +908,10 @@ __global__ void k_finish_keps(int ncel, const double* __restrict__ R, const doub
 
 // ------------------------------------------------------------------ launch wrappers
 void launch_geometry(const DevMesh& m, int* d_err, cudaStream_t s) {
-  k_cell_geometry<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vert, m.vert, m.c_vol, m.c_x);
-  k_face_geometry<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_vert, m.vert, m.f_c1, m.f_c2, m.c_x, m.f_x,
+  ++g_launch_count, k_cell_geometry<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vert, m.vert, m.c_vol, m.c_x);
+  ++g_launch_count, k_face_geometry<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_vert, m.vert, m.f_c1, m.f_c2, m.c_x, m.f_x,
                                                           m.f_n, m.f_area, m.f_lambda, d_err);
-  k_face_geometry2<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.c_x, m.f_x, m.f_n,
+  ++g_launch_count, k_face_geometry2<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.c_x, m.f_x, m.f_n,
                                                            m.f_area, m.f_rlencos, m.f_xpac, m.f_xnac, m.b_dist,
                                                            d_err);
 }
@@ -919,16 +919,16 @@ void launch_geometry(const DevMesh& m, int* d_err, cudaStream_t s) {
 void launch_bc_velocity(const DevMesh& m, const DevFields& f, int density_model, bool set_pressure,
                         cudaStream_t s) {
   if (m.nbnd > 0)
-    k_bc_velocity<<<blocks_for(m.nbnd), kThreads, 0, s>>>(m.nbnd, m.b_face, m.b_type, m.f_c1, m.f_n, m.f_area, f.R,
+    ++g_launch_count, k_bc_velocity<<<blocks_for(m.nbnd), kThreads, 0, s>>>(m.nbnd, m.b_face, m.b_type, m.f_c1, m.f_n, m.f_area, f.R,
                                                           f.U, f.V, f.W, f.P, f.BRo, f.BU, f.BV, f.BW, f.BPre,
                                                           set_pressure ? 1 : 0);
   if (density_model == 0 && m.n_outlet > 0)
-    k_bc_outlet<<<1, kThreads, 0, s>>>(m.n_inlet, m.inlet_list, m.n_outlet, m.outlet_list, m.b_face, m.f_n,
+    ++g_launch_count, k_bc_outlet<<<1, kThreads, 0, s>>>(m.n_inlet, m.inlet_list, m.n_outlet, m.outlet_list, m.b_face, m.f_n,
                                        m.f_area, f.BRo, f.BU, f.BV, f.BW);
 }
 
 void launch_bc_deltap(const DevMesh& m, const DevFields& f, cudaStream_t s) {
-  if (m.nbnd > 0) k_bc_copy<<<blocks_for(m.nbnd), kThreads, 0, s>>>(m.nbnd, m.b_face, m.f_c1, f.dp, f.BPre);
+  if (m.nbnd > 0) ++g_launch_count, k_bc_copy<<<blocks_for(m.nbnd), kThreads, 0, s>>>(m.nbnd, m.b_face, m.f_c1, f.dp, f.BPre);
 }
 
 void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
@@ -940,7 +940,7 @@ void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, con
       a.bphi[q] = bphi[q];
       a.grad[q] = grad[q];
     }
-    k_gradient<4><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2, m.f_bnd,
+    ++g_launch_count, k_gradient<4><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2, m.f_bnd,
                                                           m.f_lambda, m.f_n, m.c_vol, a);
   } else {
     for (int q = 0; q < nfield; q++) {
@@ -948,7 +948,7 @@ void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, con
       a.phi[0] = phi[q];
       a.bphi[0] = bphi[q];
       a.grad[0] = grad[q];
-      k_gradient<1><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2,
+      ++g_launch_count, k_gradient<1><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2,
                                                             m.f_bnd, m.f_lambda, m.f_n, m.c_vol, a);
     }
   }
@@ -1000,36 +1000,36 @@ void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, co
   a.g1 = gravity[1];
   a.g2 = gravity[2];
   a.warn = &st->warn_inlet;
-  k_momentum<<<blocks_for(m.ncel), kThreads, 0, s>>>(a);
+  ++g_launch_count, k_momentum<<<blocks_for(m.ncel), kThreads, 0, s>>>(a);
 }
 
 void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s) {
-  k_ruface2<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.f_n, m.f_area, m.f_lambda,
+  ++g_launch_count, k_ruface2<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.f_n, m.f_area, m.f_lambda,
                                                     m.f_xpac, m.f_xnac, m.c_x, m.c_vol, f.R, f.U, f.V, f.W, f.P,
                                                     f.Apr, f.dPdX, f.BRo, f.BU, f.BV, f.BW, f.RUFace);
 }
 
 void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s) {
-  k_pressure<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_face, m.c_slot, m.c_diag, m.f_c1,
+  ++g_launch_count, k_pressure<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_face, m.c_slot, m.c_diag, m.f_c1,
                                                      m.f_c2, m.f_lambda, m.f_rlencos, m.c_vol, f.R, f.Apr,
                                                      f.RUFace, f.Ap, f.bp, f.dinv_p);
 }
 
 void launch_correct_cells(const DevMesh& m, const DevFields& f, int cell_pref, double urf_p, double* red,
                           cudaStream_t s) {
-  k_correct_cells<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.dp, f.Apr, f.dPdX, cell_pref, urf_p,
+  ++g_launch_count, k_correct_cells<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.dp, f.Apr, f.dPdX, cell_pref, urf_p,
                                                           f.P, f.U, f.V, f.W, red);
 }
 
 void launch_correct_ruface(const DevMesh& m, const DevFields& f, double urf_p, cudaStream_t s) {
-  k_correct_ruface<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.f_n, m.f_lambda,
+  ++g_launch_count, k_correct_ruface<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.f_n, m.f_lambda,
                                                            m.f_rlencos, m.f_xpac, m.f_xnac, m.c_x, m.c_vol, f.R,
                                                            f.Apr, f.dp, f.dPdX, f.BRo, f.BU, f.BV, f.BW, urf_p,
                                                            f.RUFace);
 }
 
 void launch_keps_sources(const DevMesh& m, const DevFields& f, cudaStream_t s) {
-  k_keps_sources<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.VisLam, f.VisTur, f.dUdX, f.dVdX,
+  ++g_launch_count, k_keps_sources<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.VisLam, f.VisTur, f.dUdX, f.dVdX,
                                                          f.dWdX, f.R, f.TE, f.ED, f.VisTE, f.VisED, f.Prod, f.TES,
                                                          f.ApTE, f.EDS, f.ApED);
 }
@@ -1040,15 +1040,15 @@ void launch_keps_wall(const DevMesh& m, const DevFields& f, cudaStream_t s) {
   static const double cmu25 = __builtin_pow(0.09, 0.25);
   static const double cmu75 = __builtin_pow(0.09, 0.75);
   if (m.n_wallcell > 0)
-    k_keps_wall<<<blocks_for(m.n_wallcell), kThreads, 0, s>>>(m.n_wallcell, m.wc_cell, m.wc_start, m.wc_bnd,
+    ++g_launch_count, k_keps_wall<<<blocks_for(m.n_wallcell), kThreads, 0, s>>>(m.n_wallcell, m.wc_cell, m.wc_start, m.wc_bnd,
                                                               m.b_face, m.b_dist, m.f_n, m.f_area, m.c_vol, f.U, f.V,
                                                               f.W, f.R, f.VisLam, f.TE, f.ED, f.BTE, f.BED, f.Prod,
                                                               f.TES, f.ApTE, cmu25, cmu75);
   if (m.n_outlet > 0)
-    k_keps_bcopy<<<blocks_for(m.n_outlet), kThreads, 0, s>>>(m.n_outlet, m.outlet_list, m.b_face, m.f_c1, f.TE,
+    ++g_launch_count, k_keps_bcopy<<<blocks_for(m.n_outlet), kThreads, 0, s>>>(m.n_outlet, m.outlet_list, m.b_face, m.f_c1, f.TE,
                                                              f.ED, f.BTE, f.BED);
   if (m.n_sym > 0)
-    k_keps_bcopy<<<blocks_for(m.n_sym), kThreads, 0, s>>>(m.n_sym, m.sym_list, m.b_face, m.f_c1, f.TE, f.ED,
+    ++g_launch_count, k_keps_bcopy<<<blocks_for(m.n_sym), kThreads, 0, s>>>(m.n_sym, m.sym_list, m.b_face, m.f_c1, f.TE, f.ED,
                                                           f.BTE, f.BED);
 }
 
@@ -1081,22 +1081,22 @@ void launch_scalar(const DevMesh& m, const DevFields& f, const double* phi, cons
   a.dinv = f.dinv_s;
   a.urf = urf_s;
   a.err = &st->err;
-  k_scalar<<<blocks_for(m.ncel), kThreads, 0, s>>>(a);
+  ++g_launch_count, k_scalar<<<blocks_for(m.ncel), kThreads, 0, s>>>(a);
 }
 
 void launch_clip_te(const DevMesh& m, const DevFields& f, cudaStream_t s) {
-  k_clip_te_eps_sources<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.R, f.ED, f.Prod, f.TE, f.EDS,
+  ++g_launch_count, k_clip_te_eps_sources<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.R, f.ED, f.Prod, f.TE, f.EDS,
                                                                 f.ApED);
 }
 
 void launch_eps_wall_rows(const DevMesh& m, const DevFields& f, cudaStream_t s) {
   if (m.n_wallcell > 0)
-    k_eps_wall_rows<<<blocks_for(m.n_wallcell), kThreads, 0, s>>>(m.n_wallcell, m.wc_cell, m.rowptr, m.c_diag,
+    ++g_launch_count, k_eps_wall_rows<<<blocks_for(m.n_wallcell), kThreads, 0, s>>>(m.n_wallcell, m.wc_cell, m.rowptr, m.c_diag,
                                                                   f.ED, f.As, f.bs, f.dinv_s);
 }
 
 void launch_finish_keps(const DevMesh& m, const DevFields& f, cudaStream_t s) {
-  k_finish_keps<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, f.R, f.TE, f.ED, f.VisTur);
+  ++g_launch_count, k_finish_keps<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, f.R, f.TE, f.ED, f.VisTur);
 }
 
 }  // namespace cycas

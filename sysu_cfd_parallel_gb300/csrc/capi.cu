@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/cycasgpu.h"
+#include "cycas_amg.h"
 #include "cycas_device.h"
 #include "cycas_host.h"
 
@@ -24,6 +25,7 @@ struct cycas_case {
 namespace cycas {
 
 thread_local std::string g_last_error;
+thread_local long long g_launch_count = 0;
 
 struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
@@ -88,9 +90,19 @@ struct cycas_ctx {
   double urf[8], gravity[3];
   KspConf ksp[3];
   int nsolve = 0;                // solves issued in the current iteration
+  int solve_sys[8] = {0};        // system of each solve of the current iteration
   std::vector<void*> allocs;
   std::map<std::string, std::pair<double*, long>> dfields;
   std::map<std::string, std::pair<int*, long>> ifields;
+  // measurement
+  long long launches_base = 0;   // g_launch_count at the last profile reset
+  bool profiling = false;
+  cudaEvent_t ev_iter[2] = {nullptr, nullptr};
+  cudaEvent_t ev_solve[8][2] = {};
+  cycas_profile prof{};
+  bool iter_open = false;        // begin_iteration recorded ev_iter[0]
+  AmgHostView amg;               // pressure preconditioner hierarchy (PC_AMG)
+  std::vector<int> amg_sizes;
 
   template <class T>
   T* alloc(long n) {
@@ -115,6 +127,11 @@ struct cycas_ctx {
   }
   ~cycas_ctx() {
     if (stream) cudaStreamSynchronize(stream);
+    for (auto& e : ev_iter)
+      if (e) cudaEventDestroy(e);
+    for (auto& pr : ev_solve)
+      for (auto& e : pr)
+        if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     if (st_host) cudaFreeHost(st_host);
     if (stream) cudaStreamDestroy(stream);
@@ -343,19 +360,81 @@ void alloc_fields(cycas_ctx& c) {
 }
 
 void alloc_krylov(cycas_ctx& c) {
-  int maxm = 1;
+  int maxm = 3;  // CG needs four work vectors
   for (int s = 0; s < 3; s++) maxm = std::max(maxm, c.ksp[s].restart);
   require(maxm <= kMaxRestart, "GMRES restart above " + std::to_string(kMaxRestart));
   KrylovWork& w = c.kw;
   w.m = maxm;
   w.ldv = ((long)c.m.ncel + 31) / 32 * 32;
-  w.V = c.alloc<double>((maxm + 1) * w.ldv);
+  w.v_len = 3L * (maxm + 1) * w.ldv;  // three momentum systems in lockstep
+  w.V = c.alloc<double>(w.v_len);
   w.nblocks = gmres_max_blocks(c.device);
-  w.part = c.alloc<double>((long)w.nblocks * kGmresPartStride);
+  // per CTA and per lockstep system (up to the three momentum components)
+  w.part_len = 3L * w.nblocks * kGmresPartStride;
+  w.part = c.alloc<double>(w.part_len);
   w.bar = c.alloc<unsigned>(2);
   c.red_parts = std::min(residual_blocks(c.m.ncel), 1024);
   int cells_blocks = (c.m.ncel + 255) / 256;
   c.red = c.alloc<double>(3L * std::max(c.red_parts, cells_blocks));
+}
+
+// Aggregation hierarchy of the pressure system.  Strength of a connection = the face
+// coefficient area/|d.n| (Face.rlencos) of the face joining the two cells.
+void setup_amg(cycas_ctx& c) {
+  const int n = c.m.ncel, nf = c.m.nfac, nnz = c.m.nnz;
+  std::vector<double> rl(nf);
+  std::vector<int> rowptr(n + 1), col(nnz), slot(6L * n), faces(6L * n), nface(n);
+  CK(cudaMemcpyAsync(rl.data(), c.m.f_rlencos, sizeof(double) * nf, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(rowptr.data(), c.m.rowptr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(col.data(), c.m.col, sizeof(int) * nnz, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(slot.data(), c.m.c_slot, sizeof(int) * 6L * n, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(faces.data(), c.m.c_face, sizeof(int) * 6L * n, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(nface.data(), c.m.c_nface, sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  std::vector<double> w(nnz, 0.0);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < nface[i]; j++) {
+      int s = slot[(size_t)j * n + i];
+      if (s >= 0) w[s] = rl[faces[(size_t)j * n + i]];
+    }
+  AmgHostHierarchy H = amg_build(n, rowptr.data(), col.data(), w.data(), 4, kAmgCoarseMax, kAmgMaxLevels);
+  require(H.lv.back().n <= kAmgCoarseMax, "aggregation did not reach a small enough coarsest level");
+  AmgHostView& v = c.amg;
+  v.nlev = (int)H.lv.size();
+  for (int l = 0; l < v.nlev; l++) {
+    const AmgHostLevel& h = H.lv[l];
+    AmgDevLevel d{};
+    d.n = h.n;
+    d.nnz = h.nnz;
+    d.chunk = 0;
+    if (l == 0) {
+      d.rowptr = c.m.rowptr;
+      d.col = c.m.col;
+      d.val = c.f.Ap;
+      d.dinv = c.f.dinv_p;
+    } else {
+      d.rowptr = c.upload(h.rowptr.data(), h.n + 1L);
+      d.col = c.upload(h.col.data(), h.nnz);
+      d.val = c.alloc<double>(h.nnz);
+      d.dinv = c.alloc<double>(h.n);
+    }
+    d.diag = c.upload(h.diag.data(), h.n);
+    if (l + 1 < v.nlev) {
+      d.agg = c.upload(h.agg.data(), h.n);
+      d.ptptr = c.upload(h.ptptr.data(), (long)h.ptptr.size());
+      d.ptrow = c.upload(h.ptrow.data(), (long)h.ptrow.size());
+      d.cptr = c.upload(h.cptr.data(), (long)h.cptr.size());
+      d.csrc = c.upload(h.csrc.data(), (long)h.csrc.size());
+    }
+    d.x = c.alloc<double>(h.n);
+    d.t = c.alloc<double>(h.n);
+    d.r = c.alloc<double>(h.n);
+    v.lv[l] = d;
+  }
+  v.d_levels = c.upload(v.lv, v.nlev);
+  v.coarse_inv = c.alloc<double>((long)kAmgCoarseMax * kAmgCoarseMax);
+  c.amg_sizes.clear();
+  for (auto& h : H.lv) c.amg_sizes.push_back(h.n);
 }
 
 void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
@@ -374,8 +453,13 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
   for (int i = 0; i < 3; i++) c.gravity[i] = p->gravity[i];
   for (int s = 0; s < 3; s++) {
     const cycas_ksp_options& k = o->ksp[s];
-    require(k.pc == CYCAS_PC_NONE || k.pc == CYCAS_PC_JACOBI, "preconditioner not available in this build");
+    require(k.pc == CYCAS_PC_NONE || k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_AMG,
+            "preconditioner not available in this build");
     require(k.restart >= 1 && k.restart <= kMaxRestart, "restart out of range");
+    require(k.type >= CYCAS_KSP_DEFAULT && k.type <= CYCAS_KSP_CG, "unknown Krylov type");
+    c.ksp[s].type = k.type != CYCAS_KSP_DEFAULT ? k.type : (s == CYCAS_SYS_PRESSURE ? CYCAS_KSP_CG : CYCAS_KSP_GMRES);
+    require(k.pc != CYCAS_PC_AMG || (s == CYCAS_SYS_PRESSURE && c.ksp[s].type == CYCAS_KSP_CG),
+            "the AMG preconditioner is for the pressure system with CG");
     c.ksp[s].restart = k.restart;
     c.ksp[s].pc = k.pc;
     c.ksp[s].rtol = k.rtol > 0 ? k.rtol : kRefRtol[s];
@@ -403,10 +487,70 @@ void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const d
   g.rtol = k.rtol;
   g.maxit = k.maxit;
   g.restart = k.restart;
-  g.out = &c.st->ksp[c.nsolve++];
+  int slot = c.nsolve++;
+  c.solve_sys[slot] = sys;
+  g.out = &c.st->ksp[slot];
   g.err = &c.st->err;
   CK(cudaMemsetAsync(c.kw.bar, 0, 2 * sizeof(unsigned), c.stream));
-  CK(launch_gmres(g, c.kw, c.stream));
+  if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot][0], c.stream));
+  if (k.pc == CYCAS_PC_AMG) {
+    launch_amg_setup_values(c.amg, c.stream);
+    CK(launch_cg_amg(g, c.amg, c.kw, c.stream));
+  } else if (k.type == CYCAS_KSP_CG) {
+    CK(launch_cg(g, c.kw, c.stream));
+  } else {
+    CK(launch_gmres(g, c.kw, c.stream));
+  }
+  if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot][1], c.stream));
+  ++g_launch_count;
+  c.prof.krylov_launches[sys]++;
+}
+
+// solveVelocity_GMRES (MPIStructure.cpp:234-375): one operator, three right-hand sides, run in
+// lockstep by one persistent launch (each system keeps its own GMRES state)
+void solve_velocity(cycas_ctx& c) {
+  require(c.nsolve + 3 <= 8, "too many solves in one iteration");
+  const KspConf& k = c.ksp[CYCAS_SYS_VELOCITY];
+  if (k.type == CYCAS_KSP_CG || k.pc == CYCAS_PC_AMG) {  // non-default methods: one solve at a time
+    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bu, c.f.U, false);
+    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bv, c.f.V, false);
+    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bw, c.f.W, false);
+    return;
+  }
+  GmresCall g[3];
+  const double* bs[3] = {c.f.bu, c.f.bv, c.f.bw};
+  double* xs[3] = {c.f.U, c.f.V, c.f.W};
+  const int slot0 = c.nsolve;
+  for (int q = 0; q < 3; q++) {
+    g[q].n = c.m.ncel;
+    g[q].rowptr = c.m.rowptr;
+    g[q].col = c.m.col;
+    g[q].val = c.f.Au;
+    g[q].dinv = k.pc == CYCAS_PC_JACOBI ? c.f.dinv_u : nullptr;
+    g[q].b = bs[q];
+    g[q].x = xs[q];
+    g[q].guess_zero = 0;
+    g[q].rtol = k.rtol;
+    g[q].maxit = k.maxit;
+    g[q].restart = k.restart;
+    int slot = c.nsolve++;
+    c.solve_sys[slot] = CYCAS_SYS_VELOCITY;
+    g[q].out = &c.st->ksp[slot];
+    g[q].err = &c.st->err;
+  }
+  CK(cudaMemsetAsync(c.kw.bar, 0, 2 * sizeof(unsigned), c.stream));
+  if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot0][0], c.stream));
+  CK(launch_gmres_multi(g, 3, c.kw, c.stream));
+  if (c.profiling) {
+    CK(cudaEventRecord(c.ev_solve[slot0][1], c.stream));
+    // the two other slots share the launch: zero-length intervals
+    for (int q = 1; q < 3; q++) {
+      CK(cudaEventRecord(c.ev_solve[slot0 + q][0], c.stream));
+      CK(cudaEventRecord(c.ev_solve[slot0 + q][1], c.stream));
+    }
+  }
+  ++g_launch_count;
+  c.prof.krylov_launches[CYCAS_SYS_VELOCITY]++;
 }
 
 void bc_velocity(cycas_ctx& c, bool with_pressure) {
@@ -434,9 +578,7 @@ void build_velocity(cycas_ctx& c) {
 // CalculateVelocity (navier_velocity.cpp:10-60)
 void calculate_velocity(cycas_ctx& c) {
   build_velocity(c);
-  solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bu, c.f.U, false);
-  solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bv, c.f.V, false);
-  solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bw, c.f.W, false);
+  solve_velocity(c);
   launch_residual_uvw(c.m, c.f, c.red, c.st, c.stream);
 }
 
@@ -476,6 +618,8 @@ void update_keps(cycas_ctx& c) {
 void begin_iteration(cycas_ctx& c) {
   CK(cudaMemsetAsync(c.st, 0, sizeof(DevStatus), c.stream));
   c.nsolve = 0;
+  c.iter_open = true;
+  if (c.profiling) CK(cudaEventRecord(c.ev_iter[0], c.stream));
 }
 
 void issue_iteration(cycas_ctx& c) {
@@ -487,9 +631,24 @@ void issue_iteration(cycas_ctx& c) {
 // reads the status block; returns the C status of the iteration
 int finish_iteration(cycas_ctx& c, double* residual, double* resmax, cycas_iter_stats* stats) {
   CK(cudaGetLastError());
+  const bool timed = c.profiling && c.iter_open;
+  c.iter_open = false;
+  if (timed) CK(cudaEventRecord(c.ev_iter[1], c.stream));
   CK(cudaMemcpyAsync(c.st_host, c.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   const DevStatus& s = *c.st_host;
+  for (int k = 0; k < c.nsolve; k++) c.prof.krylov_iters[c.solve_sys[k]] += s.ksp[k].its;
+  if (timed) {
+    float total = 0.f, ksum = 0.f;
+    CK(cudaEventElapsedTime(&total, c.ev_iter[0], c.ev_iter[1]));
+    for (int k = 0; k < c.nsolve; k++) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, c.ev_solve[k][0], c.ev_solve[k][1]));
+      c.prof.krylov_ms[c.solve_sys[k]] += ms;
+      ksum += ms;
+    }
+    c.prof.assembly_ms += total - ksum;
+  }
   double mx = 0.0;
   for (int i = 0; i < 10; i++) {
     if (residual) residual[i] = s.localRes[i];
@@ -574,6 +733,7 @@ const char* cycas_last_error(void) { return g_last_error.c_str(); }
 void cycas_options_default(cycas_options* o) {
   std::memset(o, 0, sizeof(*o));
   for (int s = 0; s < 3; s++) {
+    o->ksp[s].type = CYCAS_KSP_DEFAULT;
     o->ksp[s].restart = 30;
     o->ksp[s].pc = CYCAS_PC_JACOBI;
     o->ksp[s].rtol = 0.0;
@@ -669,6 +829,7 @@ int cycas_create(const cycas_mesh_view* mesh, const cycas_params* params, const 
       build_device_mesh(*c, *mesh);
       alloc_fields(*c);
       alloc_krylov(*c);
+      if (c->ksp[CYCAS_SYS_PRESSURE].pc == CYCAS_PC_AMG) setup_amg(*c);
       CK(cudaStreamSynchronize(c->stream));
     } catch (...) {
       delete c;
@@ -818,6 +979,45 @@ int cycas_run_stage(cycas_ctx* c, const char* stage) {
   });
 }
 
+int cycas_get_stream(cycas_ctx* c, void** stream) {
+  return guard([&]() -> int {
+    require(c && stream, "null argument");
+    *stream = (void*)c->stream;
+    return CYCAS_OK;
+  });
+}
+
+int cycas_set_profiling(cycas_ctx* c, int32_t on) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    if (on && !c->ev_iter[0]) {
+      for (auto& e : c->ev_iter) CK(cudaEventCreate(&e));
+      for (auto& pr : c->ev_solve)
+        for (auto& e : pr) CK(cudaEventCreate(&e));
+    }
+    c->profiling = on != 0;
+    return CYCAS_OK;
+  });
+}
+
+int cycas_reset_profile(cycas_ctx* c) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    std::memset(&c->prof, 0, sizeof c->prof);
+    c->launches_base = g_launch_count;
+    return CYCAS_OK;
+  });
+}
+
+int cycas_get_profile(cycas_ctx* c, cycas_profile* out) {
+  return guard([&]() -> int {
+    require(c && out, "null argument");
+    *out = c->prof;
+    out->kernel_launches = g_launch_count - c->launches_base;
+    return CYCAS_OK;
+  });
+}
+
 int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
                     double* x, const cycas_ksp_options* ksp, double rtol, int32_t maxit, int32_t guess_zero,
                     cycas_solve_stats* stats) {
@@ -825,6 +1025,7 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
     require(n > 0 && rowptr && col && val && b && x && ksp, "bad argument");
     require(ksp->restart >= 1 && ksp->restart <= kMaxRestart, "restart out of range");
     require(ksp->pc == CYCAS_PC_NONE || ksp->pc == CYCAS_PC_JACOBI, "preconditioner not available in this build");
+    require(ksp->type >= CYCAS_KSP_DEFAULT && ksp->type <= CYCAS_KSP_CG, "unknown Krylov type");
     int nnz = rowptr[n];
     require(rowptr[0] == 0 && nnz >= 0, "bad rowptr");
     std::vector<double> dinv(n, 0.0);
@@ -847,11 +1048,13 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
     double* d_x = c.upload(x, n);
     double* d_dinv = c.upload(dinv.data(), n);
     DevStatus* st = c.alloc<DevStatus>(1);
-    c.kw.m = ksp->restart;
+    c.kw.m = std::max(ksp->restart, 3);
     c.kw.ldv = ((long)n + 31) / 32 * 32;
-    c.kw.V = c.alloc<double>((ksp->restart + 1) * c.kw.ldv);
+    c.kw.v_len = (c.kw.m + 1) * c.kw.ldv;
+    c.kw.V = c.alloc<double>(c.kw.v_len);
     c.kw.nblocks = gmres_max_blocks(0);
-    c.kw.part = c.alloc<double>((long)c.kw.nblocks * kGmresPartStride);
+    c.kw.part_len = (long)c.kw.nblocks * kGmresPartStride;
+    c.kw.part = c.alloc<double>(c.kw.part_len);
     c.kw.bar = c.alloc<unsigned>(2);
     GmresCall g;
     g.n = n;
@@ -867,7 +1070,8 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
     g.restart = ksp->restart;
     g.out = &st->ksp[0];
     g.err = &st->err;
-    CK(launch_gmres(g, c.kw, c.stream));
+    if (ksp->type == CYCAS_KSP_CG) CK(launch_cg(g, c.kw, c.stream));
+    else CK(launch_gmres(g, c.kw, c.stream));
     DevStatus hs;
     CK(cudaMemcpyAsync(&hs, st, sizeof hs, cudaMemcpyDeviceToHost, c.stream));
     CK(cudaMemcpyAsync(x, d_x, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));

@@ -7,6 +7,9 @@ namespace cycas {
 
 constexpr int kMaxRestart = 32;  // largest GMRES restart length supported
 
+// kernels launched by this library on the calling thread (measurement only)
+extern thread_local long long g_launch_count;
+
 // ---- mesh (structure of arrays; per-cell slot arrays are slot-major [6][ncel]) --------
 struct DevMesh {
   int ncel = 0, nfac = 0, nbnd = 0, nnz = 0, nvrt = 0;
@@ -79,8 +82,10 @@ struct DevStatus {
 };
 
 struct KrylovWork {
-  double* V = nullptr;       // (m+1) vectors of length ldv
+  double* V = nullptr;       // Krylov / work vectors of length ldv
   long ldv = 0;
+  long v_len = 0;            // doubles available at V
+  long part_len = 0;         // doubles available at part
   double* part = nullptr;    // block partial sums
   unsigned* bar = nullptr;   // grid barrier [count, generation]
   double* red = nullptr;     // residual reduction partials
@@ -90,6 +95,7 @@ struct KrylovWork {
 };
 
 struct KspConf {
+  int type;  // CYCAS_KSP_GMRES / CYCAS_KSP_CG
   int restart;
   int pc;
   double rtol;
@@ -147,5 +153,10 @@ int gmres_grid(int n, int device_blocks);
 int gmres_max_blocks(int device);
 constexpr int kGmresPartStride = kMaxRestart + 4;
 cudaError_t launch_gmres(const GmresCall& c, KrylovWork& w, cudaStream_t s);
+// nsys (1 or 3) systems sharing rowptr/col/val/dinv/tolerances, solved in lockstep; the
+// Krylov basis of system k starts at w.V + k*(restart+1)*w.ldv
+cudaError_t launch_gmres_multi(const GmresCall* calls, int nsys, KrylovWork& w, cudaStream_t s);
+// PETSc-style CG; needs at least four work vectors in w.V
+cudaError_t launch_cg(const GmresCall& c, KrylovWork& w, cudaStream_t s);
 
 }  // namespace cycas

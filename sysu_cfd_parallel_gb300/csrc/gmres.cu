@@ -1,0 +1,453 @@
+// GMRES(m) for one or several systems that share a matrix and preconditioner, as one
+// persistent cooperative kernel.
+//
+// Algorithm per system: PETSc's KSPGMRES as the reference uses it (MPIStructure.cpp:234-531):
+// restart m, classical Gram-Schmidt without refinement, left preconditioning, Givens least
+// squares, convergence when the preconditioned residual norm drops below
+// max(rtol * rnorm0, abstol) with rnorm0 = ||B b|| (nonzero initial guess) or the first
+// preconditioned residual (zero guess); DIVERGED_DTOL at dtol * rnorm0, NaN/Inf, breakdown,
+// and DIVERGED_ITS when the total iteration count reaches maxit.
+//
+// The momentum equations solve three right-hand sides with one operator
+// (solveVelocity_GMRES, MPIStructure.cpp:268-345); they run here in lockstep: every grid
+// phase and barrier is shared, one sweep over a CSR row gathers the operand of every active
+// system, and each system keeps its own Krylov basis, Hessenberg matrix and control state,
+// so its arithmetic is the same as a solve on its own.
+//
+// Each step is two grid barriers.  Per system the step is one of
+//   START / RESTART: (x update of the finished cycle) | residual z = D^-1 (b - A x) | beta, tests
+//   ARNOLDI:         w = D^-1 A v_j, partial <w, v_i> | h, w -= sum h_i v_i, ||w|| | Givens, tests
+//   FINAL:           x update of the last cycle, then idle
+// All CTAs reduce partial sums in the same fixed order, so every CTA takes the same decisions.
+#include <cuda_runtime.h>
+
+#include "cycas_device.h"
+#include "krylov_common.cuh"
+
+namespace cycas {
+
+namespace {
+
+using namespace kry;
+
+enum Mode { M_START = 0, M_ARNOLDI = 1, M_RESTART = 2, M_FINAL = 3, M_DONE = 4 };
+
+template <int NS>
+struct GmMsArgs {
+  int n, m, maxit, nb, chunk;
+  const int* __restrict__ rowptr;
+  const int* __restrict__ col;
+  const double* __restrict__ val;
+  const double* __restrict__ dinv;
+  const double* b[NS];
+  double* x[NS];
+  int guess_zero;
+  double* V;   // system s, vector q at (s*(m+1)+q)*ldv
+  long ldv;
+  double* part;  // [nb][NS][kPartStride]
+  unsigned* bar;
+  int* err;
+  KspOut* out[NS];
+  double rtol, abstol, dtol, haptol;
+};
+
+// sum over CSR row r of val[k] * vec_s[col[k]] for every system s in mask, column order
+template <int NS>
+__device__ __forceinline__ void row_gather_ms(const int* __restrict__ rowptr, const int* __restrict__ col,
+                                              const double* __restrict__ val, int r, const double* const* vec,
+                                              unsigned mask, double* out) {
+  const int k0 = __ldg(rowptr + r), k1 = __ldg(rowptr + r + 1);
+#pragma unroll
+  for (int s = 0; s < NS; s++) out[s] = 0.0;
+  for (int b = k0; b < k1; b += 4) {
+    int c[4];
+    double v[4], xv[NS][4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const bool ok = b + q < k1;
+      c[q] = ok ? __ldg(col + b + q) : 0;
+      v[q] = ok ? __ldg(val + b + q) : 0.0;
+    }
+#pragma unroll
+    for (int s = 0; s < NS; s++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) xv[s][q] = ((mask >> s) & 1u) && b + q < k1 ? ldcg(vec[s] + c[q]) : 0.0;
+#pragma unroll
+    for (int s = 0; s < NS; s++)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (b + q < k1) out[s] += v[q] * xv[s][q];
+  }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
+  constexpr int M = kMaxRestart;
+  constexpr int MAXP = NS * (M + 1);
+  __shared__ double s_hh[NS][(M + 1) * M];
+  __shared__ double s_cc[NS][M], s_ss[NS][M], s_grs[NS][M + 1], s_nrs[NS][M];
+  __shared__ double s_scale[NS][M + 1], s_h[NS][M + 1], s_coef[NS][M + 1];
+  __shared__ double s_pair[MAXP > 32 ? MAXP : 32];
+  __shared__ double s_red[kDotGroup], s_warp[kGmWarps * kDotGroup];
+  __shared__ double s_rnorm0[NS], s_ttol[NS], s_rnorm[NS];
+  __shared__ int s_mode[NS], s_it[NS], s_its[NS], s_reason[NS], s_first[NS], s_nupd[NS];
+  __shared__ unsigned char s_ps[MAXP], s_pq[MAXP];
+  __shared__ int s_npairs;
+
+  const int m = a.m, nb = a.nb, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int r0 = blockIdx.x * a.chunk;
+  const int r1 = min(a.n, r0 + a.chunk);
+  const int kNorm = M + 1, kInit = M + 2;
+  auto part_of = [&](int blk, int s) { return a.part + ((long)blk * NS + s) * kPartStride; };
+  auto Vv = [&](int s, int q) { return a.V + ((long)s * (m + 1) + q) * a.ldv; };
+
+  if (tid < NS) {
+    s_mode[tid] = M_START;
+    s_it[tid] = 0;
+    s_its[tid] = 0;
+    s_reason[tid] = 0;
+    s_first[tid] = 1;
+    s_nupd[tid] = 0;
+    s_rnorm[tid] = 0.0;
+  }
+  __syncthreads();
+
+  while (true) {
+    int mode[NS], itv[NS];
+    bool any = false;
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      mode[s] = s_mode[s];
+      itv[s] = s_it[s];
+      any |= mode[s] != M_DONE;
+    }
+    if (!any) break;
+
+    // ------------------------------------------------------------ phase X
+    unsigned arn = 0;
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      if (mode[s] == M_RESTART || mode[s] == M_FINAL) {
+        const int cnt = s_nupd[s];
+        for (int r = r0 + tid; r < r1; r += kGmThreads) {
+          double t = vec_combine(0.0, Vv(s, 0), a.ldv, r, s_coef[s], cnt, 1.0);
+          a.x[s][r] += t;
+        }
+      } else if (mode[s] == M_START && a.guess_zero) {
+        for (int r = r0 + tid; r < r1; r += kGmThreads) a.x[s][r] = 0.0;
+      }
+      if (mode[s] == M_ARNOLDI) arn |= 1u << s;
+    }
+    if (arn) {
+      const double* vj[NS];
+      double sj[NS];
+#pragma unroll
+      for (int s = 0; s < NS; s++) {
+        vj[s] = Vv(s, itv[s]);
+        sj[s] = s_scale[s][itv[s]];
+      }
+      for (int r = r0 + tid; r < r1; r += kGmThreads) {
+        double acc[NS];
+        row_gather_ms<NS>(a.rowptr, a.col, a.val, r, vj, arn, acc);
+        const double d = a.dinv ? a.dinv[r] : 1.0;
+#pragma unroll
+        for (int s = 0; s < NS; s++)
+          if ((arn >> s) & 1u) Vv(s, itv[s] + 1)[r] = (acc[s] * sj[s]) * d;
+      }
+      // pairs (system, basis vector) for the dot products
+      if (tid == 0) {
+        int p = 0;
+        for (int s = 0; s < NS; s++)
+          if ((arn >> s) & 1u)
+            for (int q = 0; q <= itv[s]; q++) {
+              s_ps[p] = (unsigned char)s;
+              s_pq[p] = (unsigned char)q;
+              p++;
+            }
+        s_npairs = p;
+      }
+      __syncthreads();
+      // partial dots <w_s, v_{s,q}>, pair-major: one or more warps stream one basis vector
+      const int P = s_npairs;
+      const int wpp = P >= kGmWarps ? 1 : kGmWarps / P;
+      for (int pb = wid / wpp; pb < P; pb += (kGmWarps / wpp)) {
+        const int sub = wid % wpp;
+        if (wid / wpp >= (kGmWarps / wpp)) break;
+        const int s = s_ps[pb], q = s_pq[pb];
+        const double* vq = Vv(s, q);
+        const double* w = Vv(s, itv[s] + 1);
+        const int step = wpp * 32;
+        double acc = 0.0;
+        for (int base = r0 + sub * 32 + lane; base < r1; base += 8 * step) {
+          double wv[8], vv[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const int r = base + k * step;
+            wv[k] = r < r1 ? ldcg(w + r) : 0.0;
+            vv[k] = r < r1 ? ldcg(vq + r) : 0.0;
+          }
+#pragma unroll
+          for (int k = 0; k < 8; k++) acc += wv[k] * vv[k];
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) s_pair[pb * wpp + sub < (MAXP > 32 ? MAXP : 32) ? pb * wpp + sub : 0] = acc;
+      }
+      __syncthreads();
+      for (int p = tid; p < P; p += kGmThreads) {
+        double sum = 0.0;
+        for (int k = 0; k < wpp; k++) sum += s_pair[p * wpp + k];
+        part_of(blockIdx.x, s_ps[p])[s_pq[p]] = sum;
+      }
+    }
+    if (!grid_barrier(a.bar, nb, a.err)) return;
+
+    // ------------------------------------------------------------ phase Y
+    unsigned res_mask = 0;
+#pragma unroll
+    for (int s = 0; s < NS; s++)
+      if (mode[s] == M_START || mode[s] == M_RESTART) res_mask |= 1u << s;
+    if (arn) {
+      const int P = s_npairs;
+      for (int p = wid; p < P; p += kGmWarps) {
+        const int s = s_ps[p], q = s_pq[p];
+        const double* base = a.part + (long)s * kPartStride + q;
+        double sum = 0.0;
+        for (int blk = lane; blk < nb; blk += 32) sum += ldcg(base + (long)blk * NS * kPartStride);
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+        if (lane == 0) {
+          const double h = sum * s_scale[s][q];
+          s_h[s][q] = h;
+          s_coef[s][q] = h * s_scale[s][q];
+        }
+      }
+      __syncthreads();
+      double nrm[NS];
+#pragma unroll
+      for (int s = 0; s < NS; s++) nrm[s] = 0.0;
+#pragma unroll
+      for (int s = 0; s < NS; s++) {
+        if (!((arn >> s) & 1u)) continue;
+        double* w = Vv(s, itv[s] + 1);
+        for (int r = r0 + tid; r < r1; r += kGmThreads) {
+          const double wr = vec_combine(ldcg(w + r), Vv(s, 0), a.ldv, r, s_coef[s], itv[s] + 1, -1.0);
+          w[r] = wr;
+          nrm[s] += wr * wr;
+        }
+      }
+      block_reduce<NS>(nrm, s_warp, s_red);
+      if (tid < NS && ((arn >> tid) & 1u)) part_of(blockIdx.x, tid)[kNorm] = s_red[tid];
+    }
+    if (res_mask) {
+      const double* xs[NS];
+#pragma unroll
+      for (int s = 0; s < NS; s++) xs[s] = a.x[s];
+      double acc[2 * NS];
+#pragma unroll
+      for (int k = 0; k < 2 * NS; k++) acc[k] = 0.0;
+      for (int r = r0 + tid; r < r1; r += kGmThreads) {
+        unsigned gmask = res_mask;
+        if (a.guess_zero) {
+#pragma unroll
+          for (int s = 0; s < NS; s++)
+            if (mode[s] == M_START) gmask &= ~(1u << s);  // x = 0: residual is b
+        }
+        double ax[NS];
+        if (gmask) row_gather_ms<NS>(a.rowptr, a.col, a.val, r, xs, gmask, ax);
+        const double d = a.dinv ? a.dinv[r] : 1.0;
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+          if (!((res_mask >> s) & 1u)) continue;
+          const double br = a.b[s][r];
+          const double t = ((gmask >> s) & 1u) ? br - ax[s] : br;
+          const double z = t * d;
+          Vv(s, 0)[r] = z;
+          acc[2 * s] += z * z;
+          if (mode[s] == M_START && !a.guess_zero) {
+            const double zb = br * d;
+            acc[2 * s + 1] += zb * zb;
+          }
+        }
+      }
+      block_reduce<2 * NS>(acc, s_warp, s_red);
+      if (tid < 2 * NS && ((res_mask >> (tid >> 1)) & 1u)) part_of(blockIdx.x, tid >> 1)[kInit + (tid & 1)] = s_red[tid];
+    }
+    if (!grid_barrier(a.bar, nb, a.err)) return;
+
+    // ------------------------------------------------------------ phase Z (warp s controls system s)
+    if (wid < NS) {
+      const int s = wid;
+      const int md = mode[s];
+      if (md == M_ARNOLDI) {
+        double sum = 0.0;
+        for (int blk = lane; blk < nb; blk += 32) sum += ldcg(part_of(blk, s) + kNorm);
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+        if (lane == 0) {
+          const int it = itv[s];
+          const double tt = sqrt(sum);
+          double* hh = s_hh[s] + it * (m + 1);
+          for (int q = 0; q <= it; q++) hh[q] = s_h[s][q];
+          hh[it + 1] = tt;
+          s_scale[s][it + 1] = 1.0 / tt;
+          double hapbnd = fabs(tt / s_grs[s][it]);
+          if (hapbnd > a.haptol) hapbnd = a.haptol;
+          const bool hapend = tt < hapbnd;
+          for (int j = 1; j <= it; j++) {
+            const double t0 = hh[j - 1];
+            hh[j - 1] = s_cc[s][j - 1] * t0 + s_ss[s][j - 1] * hh[j];
+            hh[j] = s_cc[s][j - 1] * hh[j] - s_ss[s][j - 1] * t0;
+          }
+          int rs = 0, used = it;
+          bool brk = false;
+          double res = s_rnorm[s];
+          if (!hapend) {
+            const double d = sqrt(hh[it] * hh[it] + hh[it + 1] * hh[it + 1]);
+            if (d == 0.0) {
+              rs = -5;
+              brk = true;
+            } else {
+              s_cc[s][it] = hh[it] / d;
+              s_ss[s][it] = hh[it + 1] / d;
+              s_grs[s][it + 1] = -(s_ss[s][it] * s_grs[s][it]);
+              s_grs[s][it] = s_cc[s][it] * s_grs[s][it];
+              hh[it] = s_cc[s][it] * hh[it] + s_ss[s][it] * hh[it + 1];
+              res = fabs(s_grs[s][it + 1]);
+            }
+          } else {
+            res = 0.0;
+          }
+          if (!brk) {
+            used = it + 1;
+            s_its[s]++;
+            s_rnorm[s] = res;
+            if (isnan(res) || isinf(res)) rs = -9;
+            else if (res <= s_ttol[s]) rs = res < a.abstol ? 3 : 2;
+            else if (res >= a.dtol * s_rnorm0[s]) rs = -4;
+            if (hapend && !rs) rs = -5;
+          }
+          s_reason[s] = rs;
+          const bool end_cycle = brk || rs != 0 || used == m || s_its[s] >= a.maxit;
+          if (!end_cycle) {
+            s_it[s] = used;
+          } else {
+            // least-squares solution of the cycle (back substitution on the rotated Hessenberg)
+            int nup = 0;
+            if (used > 0) {
+              const int k = used - 1;
+              const double* H = s_hh[s];
+              auto HH = [&](int row, int c) { return H[c * (m + 1) + row]; };
+              if (HH(k, k) == 0.0) {
+                s_reason[s] = -5;
+              } else {
+                s_nrs[s][k] = s_grs[s][k] / HH(k, k);
+                for (int ii = 1; ii <= k; ii++) {
+                  const int q = k - ii;
+                  double t = s_grs[s][q];
+                  for (int j = q + 1; j <= k; j++) t = t - HH(q, j) * s_nrs[s][j];
+                  s_nrs[s][q] = t / HH(q, q);
+                }
+                for (int j = 0; j <= k; j++) s_coef[s][j] = s_nrs[s][j] * s_scale[s][j];
+                nup = used;
+              }
+            }
+            s_nupd[s] = nup;
+            if (s_reason[s] == 0 && s_its[s] >= a.maxit) s_reason[s] = -3;
+            const bool finished = s_reason[s] != 0;
+            s_mode[s] = finished ? (nup > 0 ? M_FINAL : M_DONE) : (nup > 0 ? M_RESTART : M_START);
+            s_it[s] = 0;
+          }
+        }
+      } else if (md == M_START || md == M_RESTART) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int blk = lane; blk < nb; blk += 32) {
+          s0 += ldcg(part_of(blk, s) + kInit);
+          s1 += ldcg(part_of(blk, s) + kInit + 1);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          s0 += __shfl_down_sync(0xffffffffu, s0, o);
+          s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        }
+        if (lane == 0) {
+          const double beta = sqrt(s0);
+          if (s_first[s]) {
+            if (a.guess_zero) s_rnorm0[s] = beta;
+            else {
+              const double snorm = sqrt(s1);
+              s_rnorm0[s] = snorm != 0.0 ? snorm : beta;
+            }
+          }
+          s_grs[s][0] = beta;
+          s_scale[s][0] = 1.0 / beta;
+          s_rnorm[s] = beta;
+          int rs = 0;
+          if (beta == 0.0) {
+            rs = 3;
+          } else {
+            if (s_its[s] == 0) s_ttol[s] = fmax(a.rtol * s_rnorm0[s], a.abstol);
+            if (isnan(beta) || isinf(beta)) rs = -9;
+            else if (beta <= s_ttol[s]) rs = beta < a.abstol ? 3 : 2;
+            else if (beta >= a.dtol * s_rnorm0[s]) rs = -4;
+          }
+          s_reason[s] = rs;
+          s_first[s] = 0;
+          s_it[s] = 0;
+          s_mode[s] = rs ? M_DONE : M_ARNOLDI;
+        }
+      } else if (md == M_FINAL) {
+        if (lane == 0) s_mode[s] = M_DONE;
+      }
+    }
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && tid < NS) {
+    a.out[tid]->its = s_its[tid];
+    a.out[tid]->reason = s_reason[tid];
+    a.out[tid]->rnorm = s_rnorm[tid];
+  }
+}
+
+template <int NS>
+cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s) {
+  GmMsArgs<NS> a;
+  const GmresCall& c = calls[0];
+  // workspace bounds: basis NS*(m+1) vectors, partials nb*NS*stride
+  const int nb = gmres_grid(c.n, w.nblocks);
+  if (c.restart < 1 || c.restart > kMaxRestart || (long)NS * (c.restart + 1) * w.ldv > w.v_len ||
+      (long)nb * NS * kPartStride > w.part_len || w.ldv < c.n)
+    return cudaErrorInvalidValue;
+  a.n = c.n;
+  a.m = c.restart;
+  a.maxit = c.maxit;
+  a.nb = gmres_grid(c.n, w.nblocks);
+  a.chunk = (c.n + a.nb - 1) / a.nb;
+  a.rowptr = c.rowptr;
+  a.col = c.col;
+  a.val = c.val;
+  a.dinv = c.dinv;
+  for (int k = 0; k < NS; k++) {
+    a.b[k] = calls[k].b;
+    a.x[k] = calls[k].x;
+    a.out[k] = calls[k].out;
+  }
+  a.guess_zero = c.guess_zero;
+  a.V = w.V;
+  a.ldv = w.ldv;
+  a.part = w.part;
+  a.bar = w.bar;
+  a.err = c.err;
+  a.rtol = c.rtol;
+  a.abstol = 1e-50;
+  a.dtol = 1e4;
+  a.haptol = 1e-30;
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel((const void*)k_gmres_ms<NS>, dim3(a.nb), dim3(kGmThreads), args, 0, s);
+}
+
+}  // namespace
+
+cudaError_t launch_gmres_multi(const GmresCall* calls, int nsys, KrylovWork& w, cudaStream_t s) {
+  if (nsys == 1) return launch_ms<1>(calls, w, s);
+  if (nsys == 3) return launch_ms<3>(calls, w, s);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace cycas

@@ -1,0 +1,125 @@
+// Device helpers shared by the persistent Krylov kernels: bounded grid barrier and
+// deterministic block / grid reductions.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "cycas_device.h"
+
+namespace cycas {
+namespace kry {
+
+constexpr int kGmThreads = 1024;
+constexpr int kGmWarps = kGmThreads / 32;
+constexpr int kDotGroup = 8;
+constexpr long long kSpinLimit = 4000000000LL;  // ~2 s of SM clock before a barrier gives up
+constexpr int kPartStride = kMaxRestart + 4;
+
+
+
+__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+
+// bounded grid barrier for a cooperative launch
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nb, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = bar + 1;
+    unsigned g = *gen;
+    __threadfence();
+    unsigned arrived = atomicAdd(bar, 1u);
+    int ok = 1;
+    if (arrived == nb - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long t0 = clock64();
+      while (*gen == g) {
+        if (clock64() - t0 > kSpinLimit) {
+          atomicOr(err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)err) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// reduce K per-thread values over the block; result valid in s_out[0..K) after the call
+template <int K>
+__device__ __forceinline__ void block_reduce(double (&v)[K], double* s_warp /*[kGmWarps*K]*/, double* s_out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double t = v[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) s_warp[wid * K + k] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+    for (int w = 0; w < kGmWarps; w++) s += s_warp[w * K + threadIdx.x];
+    s_out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// sum part[b*stride + q] over b = 0..nb-1 in a fixed order; executed by one warp
+__device__ __forceinline__ double warp_sum_blocks(const double* part, int stride, int q, int nb) {
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  for (int b = lane; b < nb; b += 32) s += ldcg(part + (long)b * stride + q);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  return __shfl_sync(0xffffffffu, s, 0);
+}
+
+// sum over the CSR row r of val[k] * f(col[k]), accumulated in column order.  The loads of up
+// to 8 entries are issued together (predicated), so a row costs three dependent memory round
+// trips (row pointers, column/value, gathered operand) instead of one per entry.
+template <class F>
+__device__ __forceinline__ double row_gather(const int* __restrict__ rowptr, const int* __restrict__ col,
+                                             const double* __restrict__ val, int r, F f) {
+  const int k0 = __ldg(rowptr + r), k1 = __ldg(rowptr + r + 1);
+  double s = 0.0;
+  for (int b = k0; b < k1; b += 8) {
+    int c[8];
+    double v[8], xv[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const bool ok = b + q < k1;
+      c[q] = ok ? __ldg(col + b + q) : 0;
+      v[q] = ok ? __ldg(val + b + q) : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) xv[q] = (b + q < k1) ? f(c[q]) : 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      if (b + q < k1) s += v[q] * xv[q];
+  }
+  return s;
+}
+
+// w + sign * sum_{q < cnt} coef[q] * V[q*ldv + r], terms applied in ascending q; the vector
+// loads are issued 16 at a time
+__device__ __forceinline__ double vec_combine(double w, const double* V, long ldv, int r, const double* coef, int cnt,
+                                              double sign) {
+  for (int q0 = 0; q0 < cnt; q0 += 8) {
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = (q0 + k < cnt) ? ldcg(V + (long)(q0 + k) * ldv + r) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (q0 + k < cnt) w += (sign * coef[q0 + k]) * v[k];
+  }
+  return w;
+}
+
+
+}  // namespace kry
+}  // namespace cycas

@@ -1,0 +1,48 @@
+"""Run a few SIMPLE iterations of a generated case (for profilers such as ncu).
+
+    python -m sysu_cfd_parallel_gb300.profile_case --kind channel --nx 100 --ny 10 --nz 10 --iters 2
+
+prints one JSON line with the per-iteration Krylov iteration counts and timings.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import tempfile
+import time
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--kind", default="channel", choices=["channel", "cavity"])
+    ap.add_argument("--nx", type=int, default=100)
+    ap.add_argument("--ny", type=int, default=10)
+    ap.add_argument("--nz", type=int, default=10)
+    ap.add_argument("--n", type=int, default=20, help="cavity cells per side")
+    ap.add_argument("--iters", type=int, default=2)
+    ap.add_argument("--pressure-pc", default="amg", choices=["amg", "jacobi"])
+    args = ap.parse_args(argv)
+
+    from . import capi, meshgen
+    from .solver import Case, NavierStokesSolver
+
+    d = tempfile.mkdtemp(prefix="cycas_prof_")
+    if args.kind == "channel":
+        param = meshgen.write_case(d, "channel", nx=args.nx, ny=args.ny, nz=args.nz, steps=args.iters)
+    else:
+        param = meshgen.write_case(d, "cavity", n=args.n, steps=args.iters)
+    opt = capi.default_options(pc=capi.PC_JACOBI)
+    opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG if args.pressure_pc == "amg" else capi.PC_JACOBI
+    s = NavierStokesSolver(Case(param), opt)
+    s.set_profiling(True)
+    t0 = time.time()
+    r = s.iterate(args.iters)
+    dt = time.time() - t0
+    print(json.dumps({"cells": s.case.ncel, "iters": args.iters, "seconds": dt,
+                      "ksp_its": r["ksp_its"].tolist(), "profile": s.profile()}))
+    s.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -173,6 +173,24 @@ class NavierStokesSolver:
                 break
         return rm
 
+    # ---- measurement hooks
+    def stream_handle(self) -> int:
+        s = C.c_void_p()
+        capi.check(capi.load().cycas_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def set_profiling(self, on: bool) -> None:
+        capi.check(capi.load().cycas_set_profiling(self._h, 1 if on else 0))
+
+    def reset_profile(self) -> None:
+        capi.check(capi.load().cycas_reset_profile(self._h))
+
+    def profile(self) -> dict:
+        p = capi.Profile()
+        capi.check(capi.load().cycas_get_profile(self._h, C.byref(p)))
+        return {"kernel_launches": p.kernel_launches, "krylov_launches": list(p.krylov_launches),
+                "krylov_iters": list(p.krylov_iters), "krylov_ms": list(p.krylov_ms), "assembly_ms": p.assembly_ms}
+
     def close(self):
         if getattr(self, "_h", None):
             capi.load().cycas_destroy(self._h)
@@ -186,7 +204,7 @@ class NavierStokesSolver:
 
 
 def csr_solve(rowptr, col, val, b, x0=None, pc=capi.PC_JACOBI, restart=30, rtol=1e-8, maxit=1000,
-              guess_zero=True):
+              guess_zero=True, ksp_type=capi.KSP_GMRES):
     """Standalone GPU GMRES on a host CSR system (cycas_csr_solve)."""
     rp = np.ascontiguousarray(rowptr, dtype=np.int32)
     cl = np.ascontiguousarray(col, dtype=np.int32)
@@ -194,7 +212,7 @@ def csr_solve(rowptr, col, val, b, x0=None, pc=capi.PC_JACOBI, restart=30, rtol=
     bb = np.ascontiguousarray(b, dtype=np.float64)
     n = rp.size - 1
     x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
-    k = capi.KspOptions(restart=restart, pc=pc, rtol=0.0, maxit=0)
+    k = capi.KspOptions(type=ksp_type, restart=restart, pc=pc, rtol=0.0, maxit=0)
     st = capi.SolveStats()
     rc = capi.load().cycas_csr_solve(n, capi.ptr(rp), capi.ptr(cl), capi.ptr(vl), capi.ptr(bb), capi.ptr(x),
                                      C.byref(k), rtol, maxit, 1 if guess_zero else 0, C.byref(st))

@@ -49,6 +49,8 @@ def cases(tmp_path_factory):
             p = meshgen.write_case(d, "cavity", n=8, jitter=0.1, seed=3, steps=50, mu=0.02)
         elif name == "cavity12":
             p = meshgen.write_case(d, "cavity", n=12, steps=50)
+        elif name == "cavity36":  # > 152 * 256 cells: the persistent kernels use every SM
+            p = meshgen.write_case(d, "cavity", n=36, steps=50)
         elif name == "channel_tiny":
             p = meshgen.write_case(d, "channel", nx=10, ny=2, nz=2, steps=20)
         elif name == "channel_small":

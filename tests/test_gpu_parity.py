@@ -104,6 +104,18 @@ def test_iterations_match_oracle(cases, name, steps):
         assert err < 1e-8, f"{nm}: relative L2 {err:.3e}"
 
 
+def test_full_grid_iterations_match_oracle(cases):
+    """46k cells: every persistent kernel runs on all SMs (the grid size of the small cases
+    is a handful of CTAs)."""
+    o, g = _pair(cases("cavity36"))
+    ro = o.iterate(2)
+    rg = g.iterate(2)
+    assert np.all(np.abs(rg["ksp_its"] - ro["ksp_its"]) <= 1), (rg["ksp_its"], ro["ksp_its"])
+    for nm in ("U", "V", "W", "P"):
+        err = _rel_l2(g.get(nm), o.get(nm))
+        assert err < 1e-8, f"{nm}: relative L2 {err:.3e}"
+
+
 def test_csr_gmres_matches_oracle():
     from sysu_cfd_parallel_gb300.solver import csr_solve
     rng = np.random.default_rng(1)
@@ -129,3 +141,41 @@ def test_csr_gmres_matches_oracle():
     assert rg_ > 0 and ro_ > 0
     assert abs(itg - ito) <= 1
     assert _rel_l2(xg, xo) < 1e-9
+
+
+def _opts(pressure_pc, rtol_p=0.0, rtol_v=0.0):
+    o = capi.default_options(pc=capi.PC_JACOBI)
+    o.ksp[capi.SYS_PRESSURE].pc = pressure_pc
+    o.ksp[capi.SYS_PRESSURE].rtol = rtol_p
+    for s in (capi.SYS_VELOCITY, capi.SYS_SCALAR):
+        o.ksp[s].rtol = rtol_v
+    return o
+
+
+@pytest.mark.parametrize("name,steps", [("cavity8", 6), ("channel_small", 4)])
+def test_amg_pressure_matches_reference_ilu(cases, name, steps):
+    """Pressure CG with the AMG V-cycle vs the reference's ILU(0)-CG, both solved tightly:
+    the preconditioner changes the Krylov path, not the solution."""
+    p = cases(name)
+    o = po.OracleCase(p)
+    o.set_ksp(po.VELOCITY, po.PC_JACOBI, rtol=1e-12)
+    o.set_ksp(po.SCALAR, po.PC_JACOBI, rtol=1e-12)
+    o.set_ksp(po.PRESSURE, po.PC_ILU0, rtol=1e-12, ksp_type=po.KSP_CG)
+    g = NavierStokesSolver(Case(p), _opts(capi.PC_AMG, rtol_p=1e-12, rtol_v=1e-12))
+    o.iterate(steps)
+    rg = g.iterate(steps)
+    assert np.all(rg["ksp_reason"][:, :4] > 0)
+    fields = ["U", "V", "W", "P"] + (["TE", "ED"] if o.turb == 1 else [])
+    for nm in fields:
+        err = _rel_l2(g.get(nm), o.get(nm))
+        assert err < 1e-8, f"{nm}: relative L2 {err:.3e}"
+
+
+def test_amg_cuts_pressure_iterations(cases):
+    p = cases("channel_small")
+    g1 = NavierStokesSolver(Case(p), _opts(capi.PC_JACOBI))
+    g2 = NavierStokesSolver(Case(p), _opts(capi.PC_AMG))
+    r1 = g1.iterate(3)
+    r2 = g2.iterate(3)
+    assert np.all(r2["ksp_reason"][:, 3] > 0)
+    assert r2["ksp_its"][:, 3].max() * 3 < r1["ksp_its"][:, 3].min()

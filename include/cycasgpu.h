@@ -217,6 +217,22 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
                     double* x, const cycas_ksp_options* ksp, double rtol, int32_t maxit, int32_t guess_zero,
                     cycas_solve_stats* stats);
 
+/* No counterpart in the reference: the GMRES solve of cycas_csr_solve for callers that cannot
+ * allocate device memory (their HBM is pre-reserved by another allocator, or they must not add
+ * the device-wide synchronisation of cudaMalloc/cudaFree between their kernels).  rowptr, col,
+ * val, b and x are DEVICE pointers owned by the caller (a well-formed CSR: rowptr ascending
+ * from 0, columns in [0, n)); x holds the initial guess unless guess_zero and receives the
+ * solution.  Scratch comes from one static device array of 8,987,136 bytes per GPU: n above
+ * 32768 rows or restart above 32 is rejected with CYCAS_ERR_INVALID, as are preconditioners
+ * other than NONE/JACOBI and Krylov types other than DEFAULT/GMRES.  Work is issued on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) and the call returns after the
+ * stream has finished it.  The first call on a device looks the array's address up with that
+ * device current: make it before any stream capture.  All calls on a device share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+int cycas_csr_solve_noalloc(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                            const double* b, double* x, const cycas_ksp_options* ksp, double rtol, int32_t maxit,
+                            int32_t guess_zero, void* stream, cycas_solve_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,7 @@ UNITS = [
     ("amg.cu", "nvcc", []),
     ("amg_setup.cpp", "cxx", []),
     ("capi.cu", "nvcc", []),
+    ("noalloc.cu", "nvcc", []),
 ]
 
 

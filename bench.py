@@ -15,8 +15,8 @@ solver's stream).  The working set (fields, face geometry, three CSR systems, Kr
 is several hundred MB, well above the 129 MB L2, so no explicit L2 flush is done between
 iterations.
 
---impl reference times the CPU restatement of the reference (oracle/, one core, the
-reference's PETSc defaults: ILU(0) preconditioning) on the same case.
+--impl reference times the CPU restatement of the reference (oracle/, the reference's PETSc
+defaults: ILU(0) preconditioning) on the same case, one single-threaded replica per host core.
 """
 from __future__ import annotations
 
@@ -103,15 +103,33 @@ class Clocks:
 
 
 # ---------------------------------------------------------------- roofline bookkeeping
-def krylov_bytes(its_row, turb, n, nnz, restart=30):
+def vcycle_bytes(levels):
+    """Algorithmic bytes of one AMG V-cycle.  Per level with a coarser one (n rows, nnz
+    entries, nc coarse rows): pre-smoothing + residual 12 nnz + 36 n, restriction 12 n + 12 nc,
+    prolongation + post-smoothing 12 nnz + 40 n + 8 nc; coarsest level: dense inverse
+    8 nc^2 + 16 nc."""
+    rows, nnz = levels
+    if len(rows) == 0:
+        return 0
+    b = 0
+    for l in range(len(rows) - 1):
+        n, z, nc = int(rows[l]), int(nnz[l]), int(rows[l + 1])
+        b += 24 * z + 88 * n + 20 * nc
+    nc = int(rows[-1])
+    return b + 8 * nc * nc + 16 * nc
+
+
+def krylov_bytes(its_row, turb, n, nnz, restart=30, levels=None):
     """Algorithmic bytes of each Krylov launch of one iteration (solve slots in call order).
 
-    CG iteration: reads A (12 nnz + 4 (n+1)), p, z, r, w, x, D^-1 (48 n); writes p, w, x, r, z (40 n).
+    CG iteration: reads A (12 nnz + 4 (n+1)), p, z, r, w, x, D^-1 (48 n); writes p, w, x, r, z
+    (40 n); with the AMG preconditioner one V-cycle (vcycle_bytes) replaces D^-1.
     GMRES Arnoldi step j: SpMV + Jacobi (12 nnz + 4 (n+1) + 24 n), CGS dots (8 n (j+2)) and update
     (8 n (j+1) + 16 n); per restart cycle: initial residual (12 nnz + 4 (n+1) + 40 n) and the
     solution update (8 n (m_used + 2)).
     """
     spmv = 12 * nnz + 4 * (n + 1)
+    vc = vcycle_bytes(levels) if levels is not None else 0
     kinds = ["gmres", "gmres", "gmres", "cg"] + (["gmres", "gmres"] if turb else [])
     out = []
     for slot, kind in enumerate(kinds):
@@ -119,7 +137,7 @@ def krylov_bytes(its_row, turb, n, nnz, restart=30):
         if its < 0:
             continue
         if kind == "cg":
-            b = (spmv + 40 * n) + its * (spmv + 88 * n)
+            b = (spmv + 40 * n + vc) + its * (spmv + 88 * n + vc)
         else:
             b = 0
             left = its
@@ -146,6 +164,23 @@ def measured_peak():
 
 
 # ---------------------------------------------------------------- arms
+def reduce_max(x: float, device="cpu") -> float:
+    """Max of a per-rank float over all ranks (identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(cells: int, steps: int, world: int, ms: float) -> float:
+    """Cell-iterations per second of all ranks: every rank advances its own replica of the case
+    by `steps` iterations; `ms` is the slowest rank's time."""
+    return cells * steps * world / (ms / 1e3)
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -164,27 +199,74 @@ def cpu_sample(param: str, iters: int):
     return n * iters / dt, dt, setup, n
 
 
+def _ref_replica(param, warmup, steps, barrier, q):
+    """One replica of the CPU restatement (spawned process): warm up, wait for the others,
+    time `steps` SIMPLE iterations."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    o = po.OracleCase(param)
+    if warmup > 0:
+        o.iterate(warmup)
+    barrier.wait()
+    t0 = time.perf_counter()
+    o.iterate(steps)
+    q.put((o.ncel, time.perf_counter() - t0))
+    o.close()
+
+
+def host_replicas(per_replica_gb=0.8):
+    """Replicas of the CPU path that fit the host: one per usable core, capped so that their
+    resident memory stays within half of MemAvailable."""
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except AttributeError:
+        cores = os.cpu_count() or 1
+    avail_gb = None
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    avail_gb = int(line.split()[1]) / 2**20
+    except OSError:
+        pass
+    cap = cores if avail_gb is None else max(1, int(0.5 * avail_gb / per_replica_gb))
+    return max(1, min(cores, cap)), cores
+
+
 def run_reference(args):
+    """The reference's CPU path on the host: the oracle restatement (the reference itself needs
+    MPI + PETSc + METIS + CGNS and does not build here), one single-threaded replica of the
+    workload per host core, ILU(0) preconditioning (PETSc's one-rank default)."""
+    import multiprocessing as mp
     rank, world, _ = dist_env()
     if rank != 0:
         return
     param = make_case()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
-    o = po.OracleCase(param)
-    n = o.ncel
-    o.iterate(max(0, args.warmup))
-    t0 = time.time()
-    o.iterate(args.steps)
-    dt = time.time() - t0
-    value = n * args.steps / dt
+    po.build()
+    nproc, cores = host_replicas()
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(nproc)
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_ref_replica, args=(param, args.warmup, args.steps, barrier, q)) for _ in range(nproc)]
+    for p in procs:
+        p.start()
+    res = [q.get() for _ in range(nproc)]
+    for p in procs:
+        p.join()
+    n = res[0][0]
+    dt = max(r[1] for r in res)
+    value = n * args.steps * nproc / dt
+    sample = (f"{nproc} concurrent single-threaded replicas of the 480k-cell case (one per host core of {cores}), "
+              f"{args.steps} timed SIMPLE iterations each after {args.warmup} warm-up; max over replicas")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-iters/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": n, "solver": "oracle restatement, ILU(0) (PETSc one-rank default)"},
-        "cpu_baseline": {"value": value, "unit": "cell-iters/s", "cores": 1, "kind": "port",
-                         "sample": f"{args.steps} full SIMPLE iterations of the workload after {args.warmup} warm-up"},
+        "config": {"workload": WORKLOAD, "cells": n, "replicas": nproc,
+                   "solver": "oracle restatement of the reference, ILU(0) (PETSc one-rank default)"},
+        "cpu_baseline": {"value": value, "unit": "cell-iters/s", "cores": nproc, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cell-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -228,17 +310,15 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     prof = s.profile()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * args.steps * world / (ms / 1e3)
+    ms = reduce_max(ms, device="cuda")
+    value = whole_job_rate(n, args.steps, world, ms)
 
     # roofline of the dominant Krylov system
+    levels = s.amg_levels()
     per_sys_bytes = {"cg": 0.0, "gmres_vel": 0.0, "gmres_scalar": 0.0}
     per_sys_launch = {"cg": 0, "gmres_vel": 0, "gmres_scalar": 0}
     for row in hist["ksp_its"]:
-        for kind, slot, its, b in krylov_bytes(row, turb, n, nnz):
+        for kind, slot, its, b in krylov_bytes(row, turb, n, nnz, levels=levels):
             key = "cg" if kind == "cg" else ("gmres_vel" if slot < 3 else "gmres_scalar")
             per_sys_bytes[key] += b
             per_sys_launch[key] += 1
@@ -281,11 +361,8 @@ def run_gpu(args):
     f1.record(stream)
     f1.synchronize()
     e2e_ms = f0.elapsed_time(f1)
-    e2e_value = n * e2e_steps * world / (e2e_ms / 1e3)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_value = n * e2e_steps * world / (float(t.item()) / 1e3)
+    e2e_ms = reduce_max(e2e_ms, device="cuda")
+    e2e_value = whole_job_rate(n, e2e_steps, world, e2e_ms)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -302,12 +379,13 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "cells": n, "faces": case.nfac, "nnz": nnz,
                        "parallelism": f"replicas{world}", "l2": "working set > 129 MB L2, no flush",
                        "krylov": "GMRES(30)+Jacobi (u,v,w,k,eps), CG+AMG V-cycle (p'), reference tolerances",
-                       "krylov_its_last_step": [int(x) for x in hist["ksp_its"][-1]]},
+                       "krylov_its_last_step": [int(x) for x in hist["ksp_its"][-1]],
+                       "amg_levels_rows": [int(x) for x in levels[0]]},
             "e2e": {"value": e2e_value, "unit": "cell-iters/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
-            "roofline": {"bound": "hbm", "kernel": {"cg": "k_cg (pressure correction)",
-                                                    "gmres_vel": "k_gmres (momentum)",
-                                                    "gmres_scalar": "k_gmres (k, epsilon)"}[dom],
+            "roofline": {"bound": "hbm", "kernel": {"cg": "k_cg_amg (pressure correction: CG + AMG V-cycle)",
+                                                    "gmres_vel": "k_gmres_ms<3> (u, v, w in lockstep)",
+                                                    "gmres_scalar": "k_gmres_ms<1> (k, epsilon)"}[dom],
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "share_of_step": sys_ms[dom] / ms},
@@ -329,7 +407,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--cpu-iters", type=int, default=1)
+    ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

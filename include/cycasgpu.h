@@ -68,6 +68,11 @@ enum {
 /* systems, in the order of the reference's three solve wrappers */
 enum { CYCAS_SYS_VELOCITY = 0, CYCAS_SYS_PRESSURE = 1, CYCAS_SYS_SCALAR = 2 };
 
+/* Text of the last error on the calling thread (the message the reference prints before
+ * MPI_Abort in ErrorHandler::fatalRuntimeError, NS/BasicType.h:23-55); valid until the next
+ * failing call on that thread. */
+const char* cycas_last_error(void);
+
 /* ---- host-side case (param.in + gmsh v2 ASCII mesh) ------------------------------- */
 typedef struct cycas_case cycas_case;
 
@@ -209,6 +214,9 @@ typedef struct {
 int cycas_set_profiling(cycas_ctx* ctx, int32_t on);
 int cycas_get_profile(cycas_ctx* ctx, cycas_profile* out);
 int cycas_reset_profile(cycas_ctx* ctx);
+/* Sizes of the pressure AMG hierarchy (0 levels unless CYCAS_PC_AMG is in use): *nlev levels,
+ * rows[l] and stored entries nnz[l] for the first max_levels of them, fine to coarse. */
+int cycas_get_amg_levels(cycas_ctx* ctx, int32_t max_levels, int32_t* nlev, int32_t* rows, int32_t* nnz);
 
 /* Standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
  * col[nnz], double val[nnz]); b and x are host arrays, x holds the initial guess unless

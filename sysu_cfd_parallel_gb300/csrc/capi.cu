@@ -102,7 +102,8 @@ struct cycas_ctx {
   cycas_profile prof{};
   bool iter_open = false;        // begin_iteration recorded ev_iter[0]
   AmgHostView amg;               // pressure preconditioner hierarchy (PC_AMG)
-  std::vector<int> amg_sizes;
+  std::vector<int> amg_sizes;  // rows per AMG level (fine to coarse)
+  std::vector<int> amg_nnz;    // stored entries per AMG level
 
   template <class T>
   T* alloc(long n) {
@@ -434,7 +435,11 @@ void setup_amg(cycas_ctx& c) {
   v.d_levels = c.upload(v.lv, v.nlev);
   v.coarse_inv = c.alloc<double>((long)kAmgCoarseMax * kAmgCoarseMax);
   c.amg_sizes.clear();
-  for (auto& h : H.lv) c.amg_sizes.push_back(h.n);
+  c.amg_nnz.clear();
+  for (auto& h : H.lv) {
+    c.amg_sizes.push_back(h.n);
+    c.amg_nnz.push_back(h.nnz);
+  }
 }
 
 void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
@@ -996,6 +1001,19 @@ int cycas_set_profiling(cycas_ctx* c, int32_t on) {
         for (auto& e : pr) CK(cudaEventCreate(&e));
     }
     c->profiling = on != 0;
+    return CYCAS_OK;
+  });
+}
+
+int cycas_get_amg_levels(cycas_ctx* c, int32_t max_levels, int32_t* nlev, int32_t* rows, int32_t* nnz) {
+  return guard([&]() -> int {
+    require(c && nlev, "null argument");
+    int L = (int)c->amg_sizes.size();
+    *nlev = L;
+    for (int l = 0; l < L && l < max_levels; l++) {
+      if (rows) rows[l] = c->amg_sizes[l];
+      if (nnz) nnz[l] = c->amg_nnz[l];
+    }
     return CYCAS_OK;
   });
 }

@@ -182,6 +182,15 @@ class NavierStokesSolver:
     def set_profiling(self, on: bool) -> None:
         capi.check(capi.load().cycas_set_profiling(self._h, 1 if on else 0))
 
+    def amg_levels(self):
+        """(rows, nnz) per level of the pressure AMG hierarchy, fine to coarse."""
+        nl = C.c_int32()
+        rows = np.zeros(16, dtype=np.int32)
+        nnz = np.zeros(16, dtype=np.int32)
+        capi.check(capi.load().cycas_get_amg_levels(self._h, 16, C.byref(nl), capi.ptr(rows), capi.ptr(nnz)))
+        k = min(nl.value, 16)
+        return rows[:k].copy(), nnz[:k].copy()
+
     def reset_profile(self) -> None:
         capi.check(capi.load().cycas_reset_profile(self._h))
 

@@ -407,18 +407,19 @@ void setup_amg(cycas_ctx& c) {
     AmgDevLevel d{};
     d.n = h.n;
     d.nnz = h.nnz;
-    d.chunk = 0;
+    d.maxagg = 0;
+    for (size_t I = 0; I + 1 < h.ptptr.size(); I++) d.maxagg = std::max(d.maxagg, h.ptptr[I + 1] - h.ptptr[I]);
     if (l == 0) {
       d.rowptr = c.m.rowptr;
       d.col = c.m.col;
-      d.val = c.f.Ap;
-      d.dinv = c.f.dinv_p;
+      d.val64 = c.f.Ap;
     } else {
       d.rowptr = c.upload(h.rowptr.data(), h.n + 1L);
       d.col = c.upload(h.col.data(), h.nnz);
-      d.val = c.alloc<double>(h.nnz);
-      d.dinv = c.alloc<double>(h.n);
+      d.val64 = nullptr;
     }
+    d.val = c.alloc<float>(h.nnz);
+    d.wdinv = c.alloc<float>(h.n);
     d.diag = c.upload(h.diag.data(), h.n);
     if (l + 1 < v.nlev) {
       d.agg = c.upload(h.agg.data(), h.n);
@@ -427,13 +428,12 @@ void setup_amg(cycas_ctx& c) {
       d.cptr = c.upload(h.cptr.data(), (long)h.cptr.size());
       d.csrc = c.upload(h.csrc.data(), (long)h.csrc.size());
     }
-    d.x = c.alloc<double>(h.n);
-    d.t = c.alloc<double>(h.n);
-    d.r = c.alloc<double>(h.n);
+    d.r = c.alloc<float>(h.n);
+    d.t = c.alloc<float>(h.n);
     v.lv[l] = d;
   }
   v.d_levels = c.upload(v.lv, v.nlev);
-  v.coarse_inv = c.alloc<double>((long)kAmgCoarseMax * kAmgCoarseMax);
+  v.coarse_inv = c.alloc<float>((long)kAmgCoarseMax * kAmgCoarseMax);
   c.amg_sizes.clear();
   c.amg_nnz.clear();
   for (auto& h : H.lv) {

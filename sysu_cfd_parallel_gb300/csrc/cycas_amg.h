@@ -24,37 +24,41 @@ struct AmgHostHierarchy {
 AmgHostHierarchy amg_build(int n, const int* rowptr, const int* col, const double* weight, int maxsize,
                            int coarse_max, int max_levels);
 
+// One level of the device hierarchy.  The V-cycle runs in FP32 (it is only a preconditioner;
+// the CG around it is FP64), so every level keeps FP32 values; level 0 also points at the
+// FP64 pressure matrix the FP32 copy is made from.
 struct AmgDevLevel {
-  int n, nnz, chunk;
+  int n, nnz;
+  int maxagg;  // largest aggregate (fine rows per coarse row); 0 on the coarsest level
   const int* rowptr;
   const int* col;
-  const int* diag;
-  double* val;
-  double* dinv;
+  const int* diag;     // position of the diagonal in each row
+  const double* val64; // level 0 only: the FP64 system matrix
+  float* val;          // FP32 matrix values (level 0: rounded copy; coarser: Galerkin sums)
+  float* wdinv;        // w / a_ii
   const int* agg;
   const int* ptptr;
   const int* ptrow;
   const int* cptr;
   const int* csrc;
-  double* x;  // smoothed correction
-  double* t;  // post-smoothed correction
-  double* r;  // residual (level 0: the caller's vector)
+  float* r;  // residual on this level (level 0: FP32 copy of the CG residual)
+  float* t;  // correction returned to the finer level
 };
 
 // host-side record of the device hierarchy
 struct AmgHostView {
   int nlev = 0;
-  double omega = 2.0 / 3.0, alpha = 2.0;
-  double* coarse_inv = nullptr;
+  float omega = 2.0f / 3.0f, alpha = 2.0f;
+  float* coarse_inv = nullptr;
   AmgDevLevel* d_levels = nullptr;
   AmgDevLevel lv[kAmgMaxLevels];
 };
 
 struct AmgDev {
   int nlev;
-  double omega;   // Jacobi weight
-  double alpha;   // coarse-correction scaling
-  double* coarse_inv;  // dense inverse of the (regularised) coarsest matrix, row-major
+  float omega;          // Jacobi weight
+  float alpha;          // coarse-correction scaling
+  float* coarse_inv;    // dense inverse of the (regularised) coarsest matrix, row-major
   AmgDevLevel* levels;  // device array [nlev]
 };
 

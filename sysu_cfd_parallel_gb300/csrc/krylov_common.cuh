@@ -80,26 +80,26 @@ __device__ __forceinline__ double warp_sum_blocks(const double* part, int stride
 }
 
 // sum over the CSR row r of val[k] * f(col[k]), accumulated in column order.  The loads of up
-// to 8 entries are issued together (predicated), so a row costs three dependent memory round
+// to W entries are issued together (predicated), so a row costs three dependent memory round
 // trips (row pointers, column/value, gathered operand) instead of one per entry.
-template <class F>
+template <int W = 8, class F>
 __device__ __forceinline__ double row_gather(const int* __restrict__ rowptr, const int* __restrict__ col,
                                              const double* __restrict__ val, int r, F f) {
   const int k0 = __ldg(rowptr + r), k1 = __ldg(rowptr + r + 1);
   double s = 0.0;
-  for (int b = k0; b < k1; b += 8) {
-    int c[8];
-    double v[8], xv[8];
+  for (int b = k0; b < k1; b += W) {
+    int c[W];
+    double v[W], xv[W];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
+    for (int q = 0; q < W; q++) {
       const bool ok = b + q < k1;
       c[q] = ok ? __ldg(col + b + q) : 0;
       v[q] = ok ? __ldg(val + b + q) : 0.0;
     }
 #pragma unroll
-    for (int q = 0; q < 8; q++) xv[q] = (b + q < k1) ? f(c[q]) : 0.0;
+    for (int q = 0; q < W; q++) xv[q] = (b + q < k1) ? f(c[q]) : 0.0;
 #pragma unroll
-    for (int q = 0; q < 8; q++)
+    for (int q = 0; q < W; q++)
       if (b + q < k1) s += v[q] * xv[q];
   }
   return s;

@@ -51,19 +51,21 @@ struct GmMsArgs {
   double rtol, abstol, dtol, haptol;
 };
 
-// sum over CSR row r of val[k] * vec_s[col[k]] for every system s in mask, column order
+// sum over CSR row r of val[k] * vec_s[col[k]] for every system s in mask, column order; W
+// entries per batch (a tetrahedral row, 5 entries, is one batch for a single system)
 template <int NS>
 __device__ __forceinline__ void row_gather_ms(const int* __restrict__ rowptr, const int* __restrict__ col,
                                               const double* __restrict__ val, int r, const double* const* vec,
                                               unsigned mask, double* out) {
+  constexpr int W = NS == 1 ? 5 : 3;
   const int k0 = __ldg(rowptr + r), k1 = __ldg(rowptr + r + 1);
 #pragma unroll
   for (int s = 0; s < NS; s++) out[s] = 0.0;
-  for (int b = k0; b < k1; b += 4) {
-    int c[4];
-    double v[4], xv[NS][4];
+  for (int b = k0; b < k1; b += W) {
+    int c[W];
+    double v[W], xv[NS][W];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < W; q++) {
       const bool ok = b + q < k1;
       c[q] = ok ? __ldg(col + b + q) : 0;
       v[q] = ok ? __ldg(val + b + q) : 0.0;
@@ -71,11 +73,11 @@ __device__ __forceinline__ void row_gather_ms(const int* __restrict__ rowptr, co
 #pragma unroll
     for (int s = 0; s < NS; s++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) xv[s][q] = ((mask >> s) & 1u) && b + q < k1 ? ldcg(vec[s] + c[q]) : 0.0;
+      for (int q = 0; q < W; q++) xv[s][q] = ((mask >> s) & 1u) && b + q < k1 ? ldcg(vec[s] + c[q]) : 0.0;
 #pragma unroll
     for (int s = 0; s < NS; s++)
 #pragma unroll
-      for (int q = 0; q < 4; q++)
+      for (int q = 0; q < W; q++)
         if (b + q < k1) out[s] += v[q] * xv[s][q];
   }
 }
@@ -130,7 +132,7 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
       if (mode[s] == M_RESTART || mode[s] == M_FINAL) {
         const int cnt = s_nupd[s];
         for (int r = r0 + tid; r < r1; r += kGmThreads) {
-          double t = vec_combine(0.0, Vv(s, 0), a.ldv, r, s_coef[s], cnt, 1.0);
+          double t = vec_axpy(0.0, Vv(s, 0), a.ldv, r, s_coef[s], cnt);
           a.x[s][r] += t;
         }
       } else if (mode[s] == M_START && a.guess_zero) {
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
         if (lane == 0) {
           const double h = sum * s_scale[s][q];
           s_h[s][q] = h;
-          s_coef[s][q] = h * s_scale[s][q];
+          s_coef[s][q] = -(h * s_scale[s][q]);  // w -= h v_q / |v_q|
         }
       }
       __syncthreads();
@@ -229,7 +231,7 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
         if (!((arn >> s) & 1u)) continue;
         double* w = Vv(s, itv[s] + 1);
         for (int r = r0 + tid; r < r1; r += kGmThreads) {
-          const double wr = vec_combine(ldcg(w + r), Vv(s, 0), a.ldv, r, s_coef[s], itv[s] + 1, -1.0);
+          const double wr = vec_axpy(ldcg(w + r), Vv(s, 0), a.ldv, r, s_coef[s], itv[s] + 1);
           w[r] = wr;
           nrm[s] += wr * wr;
         }
@@ -288,9 +290,8 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
           for (int q = 0; q <= it; q++) hh[q] = s_h[s][q];
           hh[it + 1] = tt;
           s_scale[s][it + 1] = 1.0 / tt;
-          double hapbnd = fabs(tt / s_grs[s][it]);
-          if (hapbnd > a.haptol) hapbnd = a.haptol;
-          const bool hapend = tt < hapbnd;
+          // happy breakdown: tt < min(|tt / g_it|, haptol); the division only when tt < haptol
+          const bool hapend = tt < a.haptol && tt < fabs(tt / s_grs[s][it]);
           for (int j = 1; j <= it; j++) {
             const double t0 = hh[j - 1];
             hh[j - 1] = s_cc[s][j - 1] * t0 + s_ss[s][j - 1] * hh[j];
@@ -305,8 +306,9 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
               rs = -5;
               brk = true;
             } else {
-              s_cc[s][it] = hh[it] / d;
-              s_ss[s][it] = hh[it + 1] / d;
+              const double rd = 1.0 / d;
+              s_cc[s][it] = hh[it] * rd;
+              s_ss[s][it] = hh[it + 1] * rd;
               s_grs[s][it + 1] = -(s_ss[s][it] * s_grs[s][it]);
               s_grs[s][it] = s_cc[s][it] * s_grs[s][it];
               hh[it] = s_cc[s][it] * hh[it] + s_ss[s][it] * hh[it + 1];

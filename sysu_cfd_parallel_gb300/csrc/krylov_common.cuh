@@ -105,17 +105,17 @@ __device__ __forceinline__ double row_gather(const int* __restrict__ rowptr, con
   return s;
 }
 
-// w + sign * sum_{q < cnt} coef[q] * V[q*ldv + r], terms applied in ascending q; the vector
-// loads are issued 16 at a time
-__device__ __forceinline__ double vec_combine(double w, const double* V, long ldv, int r, const double* coef, int cnt,
-                                              double sign) {
+// w + sum_{q < cnt} coef[q] * V[q*ldv + r], terms applied in ascending q; the vector loads are
+// issued 8 at a time.  Callers pass coefficients with their sign folded in, so each term is a
+// single FP64 FMA.
+__device__ __forceinline__ double vec_axpy(double w, const double* V, long ldv, int r, const double* coef, int cnt) {
   for (int q0 = 0; q0 < cnt; q0 += 8) {
     double v[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) v[k] = (q0 + k < cnt) ? ldcg(V + (long)(q0 + k) * ldv + r) : 0.0;
 #pragma unroll
     for (int k = 0; k < 8; k++)
-      if (q0 + k < cnt) w += (sign * coef[q0 + k]) * v[k];
+      if (q0 + k < cnt) w = fma(coef[q0 + k], v[k], w);
   }
   return w;
 }

@@ -42,8 +42,6 @@ namespace {
 using namespace kry;
 
 constexpr int kThreads = 256;
-constexpr int kDownBuf = 8192;             // floats of the per-CTA restriction buffer
-constexpr int kTailBudget = 160 * 1024;    // shared-memory bytes for the tail levels
 
 // ---------------------------------------------------------------- per-solve setup
 __global__ void k_amg_level0(int nnz, const double* __restrict__ val64, float* __restrict__ val) {
@@ -66,23 +64,28 @@ __global__ void k_amg_wdinv(int n, float omega, const int* __restrict__ diag, co
   if (i < n) wdinv[i] = omega / val[diag[i]];
 }
 
-// dense inverse of A_L + s 11^T, s = mean(diag)/n, by in-place Gauss-Jordan in shared memory.
-// A_L is singular with the constant null vector (row sums vanish); the shift has the sign of
-// the diagonal, so the shifted matrix is definite.  Pivoting is not needed for a definite matrix.
-__global__ void k_amg_coarse_inverse(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
-                                     const int* __restrict__ diag, const float* __restrict__ val,
-                                     float* __restrict__ inv) {
+// dense inverse of A_L + s 11^T, s = mean(diag)/n, for the coarsest level of case blockIdx.x,
+// by in-place Gauss-Jordan in shared memory.  A_L is singular with the constant null vector
+// (row sums vanish); the shift has the sign of the diagonal, so the shifted matrix is
+// definite and needs no pivoting.  A case with a single level is inverted on its own rows of
+// the system (global numbering).
+__global__ void k_amg_coarse_inverse(const AmgCaseDesc* __restrict__ cases) {
   __shared__ float M[kAmgCoarseMax * kAmgCoarseMax];
   __shared__ float colk[kAmgCoarseMax];
   __shared__ float s_shift;
+  const AmgCaseDesc& cd = cases[blockIdx.x];
+  const AmgDevLevel K = cd.levels[cd.nlev - 1];
+  const int n = K.n;
+  const int row0 = cd.nlev == 1 ? cd.lo : 0;
+  float* inv = const_cast<float*>(cd.coarse_inv);
   const int tid = threadIdx.x;
   for (int e = tid; e < n * n; e += blockDim.x) M[e] = 0.0f;
   __syncthreads();
   for (int i = tid; i < n; i += blockDim.x)
-    for (int k = rowptr[i]; k < rowptr[i + 1]; k++) M[i * n + col[k]] = val[k];
+    for (int k = K.rowptr[row0 + i]; k < K.rowptr[row0 + i + 1]; k++) M[i * n + K.col[k] - row0] = K.val[k];
   if (tid == 0) {
     float d = 0.0f;
-    for (int i = 0; i < n; i++) d += val[diag[i]];
+    for (int i = 0; i < n; i++) d += K.val[K.diag[row0 + i] - K.nnz_off];
     s_shift = d / ((float)n * (float)n);
   }
   __syncthreads();
@@ -105,17 +108,6 @@ __global__ void k_amg_coarse_inverse(int n, const int* __restrict__ rowptr, cons
 }
 
 // ---------------------------------------------------------------- V-cycle
-struct TailLevelOff {  // byte offsets of one tail level's arrays in dynamic shared memory
-  int rowptr, col, val, wdinv, agg, ptptr, ptrow, R, X, T;
-};
-
-struct TailLayout {
-  int tail;   // first level cycled by CTA 0 from shared memory (levels tail..nlev-1)
-  int bytes;  // dynamic shared memory taken by the tail (multiple of 16)
-  int inv;    // offset of the coarsest level's dense inverse
-  TailLevelOff lv[kAmgMaxLevels];
-};
-
 struct CgAmgArgs {
   int n, maxit, guess_zero, nb;
   const int* __restrict__ rowptr;
@@ -127,19 +119,28 @@ struct CgAmgArgs {
   double* part;
   unsigned* bar;
   int* err;
-  KspOut* out;
+  KspOut* out;  // [ncases]
   double rtol, abstol, dtol;
-  AmgDev amg;
-  TailLayout tl;
+  float alpha;
+  const AmgCaseDesc* cases;
+  const BatchSchedule* sched;
+};
+
+// the CTAs that solve one case together
+struct Team {
+  int rank, size;
+  unsigned* bar;
+  double* part;  // [size][kPartStride]
 };
 
 struct Rows {
   int r0, r1;
 };
-__device__ __forceinline__ Rows own_rows(int n, int nb) {
-  int ch = (n + nb - 1) / nb;
-  int r0 = blockIdx.x * ch;
-  return {min(r0, n), min(n, r0 + ch)};
+// the team member's share of rows [lo, hi)
+__device__ __forceinline__ Rows share(int lo, int hi, const Team& T) {
+  const int ch = (hi - lo + T.size - 1) / T.size;
+  const int r0 = min(hi, lo + T.rank * ch);
+  return {r0, min(hi, r0 + ch)};
 }
 
 __device__ __forceinline__ float ldcgf(const float* p) { return __ldcg(p); }
@@ -173,25 +174,27 @@ __device__ __forceinline__ T* at(unsigned char* sb, int off) {
   return reinterpret_cast<T*>(sb + off);
 }
 
+// rank 0 of a team: the tail levels of its case (matrices, transfer lists, the coarsest
+// inverse) into shared memory; level 0 is renumbered from the system's rows to the case's
 template <class T>
-__device__ __forceinline__ void copy_in(T* dst, const T* src, int cnt) {
-  for (int i = threadIdx.x; i < cnt; i += kGmThreads) dst[i] = src[i];
+__device__ __forceinline__ void copy_in(T* dst, const T* src, int cnt, T shift = T(0)) {
+  for (int i = threadIdx.x; i < cnt; i += kGmThreads) dst[i] = src[i] - shift;
 }
-
-// CTA 0: the tail levels' matrices, transfer lists and the coarsest inverse into shared memory
-__device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, const float* coarse_inv,
+__device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, const float* coarse_inv, int lo,
                           unsigned char* sb) {
   for (int l = T.tail; l < nlev; l++) {
     const AmgDevLevel& F = L[l];
     const TailLevelOff& o = T.lv[l];
+    const int row0 = l == 0 ? lo : 0;
     if (l + 1 < nlev) {
-      copy_in(at<int>(sb, o.rowptr), F.rowptr, F.n + 1);
-      copy_in(at<int>(sb, o.col), F.col, F.nnz);
-      copy_in(at<float>(sb, o.val), (const float*)F.val, F.nnz);
-      copy_in(at<float>(sb, o.wdinv), (const float*)F.wdinv, F.n);
-      copy_in(at<int>(sb, o.agg), F.agg, F.n);
+      const int k0 = l == 0 ? __ldg(F.rowptr + lo) : 0;
+      copy_in(at<int>(sb, o.rowptr), F.rowptr + row0, F.n + 1, k0);
+      copy_in(at<int>(sb, o.col), F.col + k0, F.nnz, row0);
+      copy_in(at<float>(sb, o.val), (const float*)F.val + k0, F.nnz);
+      copy_in(at<float>(sb, o.wdinv), (const float*)F.wdinv + row0, F.n);
+      copy_in(at<int>(sb, o.agg), F.agg + row0, F.n);
       copy_in(at<int>(sb, o.ptptr), F.ptptr, L[l + 1].n + 1);
-      copy_in(at<int>(sb, o.ptrow), F.ptrow, F.n);
+      copy_in(at<int>(sb, o.ptrow), F.ptrow, F.n, row0);
     } else {
       copy_in(at<float>(sb, T.inv), coarse_inv, F.n * F.n);
     }
@@ -199,16 +202,16 @@ __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, c
   __syncthreads();
 }
 
-// CTA 0: the V-cycle from level T.tail down, in shared memory; its input residual is
-// L[tail].r and its correction goes to L[tail].t (or, when the tail is the whole hierarchy,
-// to the FP64 vector z)
+// rank 0 of a team: the V-cycle from level T.tail down, in shared memory; its input residual
+// is the tail level's r, its correction goes to the tail level's t (or, when the tail is the
+// whole hierarchy, to rows [lo, hi) of the FP64 vector z)
 __device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, unsigned char* sb,
-                           double* z) {
+                           int lo, double* z) {
   const int tid = threadIdx.x;
   const int t0 = T.tail;
   {
     float* R = at<float>(sb, T.lv[t0].R);
-    const float* rin = L[t0].r;
+    const float* rin = t0 == 0 ? L[0].r + lo : L[t0].r;
     for (int i = tid; i < L[t0].n; i += kGmThreads) R[i] = ldcgf(rin + i);
   }
   __syncthreads();
@@ -278,7 +281,7 @@ __device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, 
   {
     const float* X = at<float>(sb, T.lv[t0].X);
     if (t0 == 0) {
-      for (int i = tid; i < L[0].n; i += kGmThreads) z[i] = (double)X[i];
+      for (int i = tid; i < L[0].n; i += kGmThreads) z[lo + i] = (double)X[i];
     } else {
       float* out = L[t0].t;
       for (int i = tid; i < L[t0].n; i += kGmThreads) out[i] = X[i];
@@ -286,13 +289,13 @@ __device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, 
   }
 }
 
-// grid level l -> l+1: each CTA takes a block of coarse rows, computes the smoothed residual
-// t_i = r_i - A_i (w D^-1 r) of their fine rows (in aggregate order) into shared memory and
-// sums each aggregate: r_{l+1} = P^T t.  Only r_l is read, so no barrier separates smoothing
-// from restriction.
-__device__ __forceinline__ void grid_down(const AmgDevLevel& F, const AmgDevLevel& C, int nb, float* buf) {
-  const Rows cr = own_rows(C.n, nb);
-  const int G = max(1, kDownBuf / max(1, F.maxagg));
+// level l -> l+1 on the team: each member takes a block of coarse rows, computes the smoothed
+// residual t_i = r_i - A_i (w D^-1 r) of their fine rows (in aggregate order) into shared
+// memory and sums each aggregate: r_{l+1} = P^T t.  Only r_l is read, so no barrier separates
+// smoothing from restriction.
+__device__ __forceinline__ void grid_down(const AmgDevLevel& F, const AmgDevLevel& C, const Team& Tm, float* buf) {
+  const Rows cr = share(0, C.n, Tm);
+  const int G = max(1, kAmgDownBuf / max(1, F.maxagg));
   const float* rl = F.r;
   const float* wd = F.wdinv;
   for (int I0 = cr.r0; I0 < cr.r1; I0 += G) {
@@ -315,8 +318,8 @@ __device__ __forceinline__ void grid_down(const AmgDevLevel& F, const AmgDevLeve
   }
 }
 
-// prolongation of the coarse correction and post-smoothing on the CTA's rows of grid level
-// l: out = y + w D^-1 (r - A y),  y = w D^-1 r + a P x_C; level 0 writes the FP64 z
+// prolongation of the coarse correction and post-smoothing on rows rw of a level:
+// out = y + w D^-1 (r - A y),  y = w D^-1 r + a P x_C; level 0 writes the FP64 z
 __device__ __forceinline__ void grid_up(const AmgDevLevel& F, const float* xc, float alpha, Rows rw, float* outf,
                                         double* outd) {
   const float* rl = F.r;
@@ -335,42 +338,56 @@ __device__ __forceinline__ void grid_up(const AmgDevLevel& F, const float* xc, f
   }
 }
 
-// z = M r for the residual held in L[0].r; every CTA participates; false after a barrier timeout
+// z = M r for the case's rows [lo, hi) of the residual held in L[0].r; false after a barrier
+// timeout
 __device__ bool vcycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, unsigned char* sb,
-                       float* buf, double* z, unsigned* bar, unsigned nb, int* err) {
+                       float* buf, int lo, int hi, double* z, const Team& Tm, int* err) {
   const int t0 = T.tail;
   for (int l = 0; l < t0; l++) {
-    grid_down(L[l], L[l + 1], nb, buf);
-    if (!grid_barrier(bar, nb, err)) return false;
+    grid_down(L[l], L[l + 1], Tm, buf);
+    if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   }
-  if (blockIdx.x == 0) tail_cycle(L, nlev, T, alpha, sb, z);
-  if (!grid_barrier(bar, nb, err)) return false;
+  if (Tm.rank == 0) tail_cycle(L, nlev, T, alpha, sb, lo, z);
+  if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   for (int l = t0 - 1; l >= 0; l--) {
-    grid_up(L[l], L[l + 1].t, alpha, own_rows(L[l].n, nb), l == 0 ? nullptr : L[l].t, l == 0 ? z : nullptr);
-    if (!grid_barrier(bar, nb, err)) return false;
+    const Rows rw = l == 0 ? share(lo, hi, Tm) : share(0, L[l].n, Tm);
+    grid_up(L[l], L[l + 1].t, alpha, rw, l == 0 ? nullptr : L[l].t, l == 0 ? z : nullptr);
+    if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   }
   return true;
 }
 
 __device__ __forceinline__ int sgn(double v) { return (v > 0) - (v < 0); }
 
-__global__ void __launch_bounds__(kGmThreads, 1) k_cg_amg(CgAmgArgs a) {
+// FCG(1) in Chronopoulos-Gear form on rows [lo, hi) of case c by team Tm
+__device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ double s_warp[kGmWarps * kDotGroup];
   __shared__ double s_red[kDotGroup];
   __shared__ double s_g[5];
   __shared__ AmgDevLevel s_lv[kAmgMaxLevels];
-  const int nb = a.nb, tid = threadIdx.x;
-  const int nlev = a.amg.nlev;
-  for (int l = tid; l < nlev; l += kGmThreads) s_lv[l] = a.amg.levels[l];
+  __shared__ TailLayout s_tl;
+  __shared__ int s_case[3];  // lo, hi, nlev
+  const int tid = threadIdx.x;
+  const AmgCaseDesc* cd = a.cases + c;
+  if (tid == 0) {
+    s_case[0] = cd->lo;
+    s_case[1] = cd->hi;
+    s_case[2] = cd->nlev;
+  }
+  for (int k = tid; k < (int)(sizeof(TailLayout) / sizeof(int)); k += kGmThreads)
+    reinterpret_cast<int*>(&s_tl)[k] = reinterpret_cast<const int*>(&cd->tl)[k];
+  __syncthreads();
+  const int lo = s_case[0], hi = s_case[1], nlev = s_case[2];
+  for (int l = tid; l < nlev; l += kGmThreads) s_lv[l] = cd->levels[l];
   __syncthreads();
   unsigned char* sb = s_dyn;
-  float* buf = reinterpret_cast<float*>(s_dyn + a.tl.bytes);
-  if (blockIdx.x == 0) tail_load(s_lv, nlev, a.tl, a.amg.coarse_inv, sb);
-  const Rows own = own_rows(a.n, nb);
+  float* buf = reinterpret_cast<float*>(s_dyn + s_tl.bytes);
+  if (Tm.rank == 0) tail_load(s_lv, nlev, s_tl, cd->coarse_inv, lo, sb);
+  const Rows own = share(lo, hi, Tm);
   const int stride = kPartStride;
-  double* mypart = a.part + (long)blockIdx.x * stride;
-  const float alc = a.amg.alpha;
+  double* mypart = Tm.part + (long)Tm.rank * stride;
+  const float alc = a.alpha;
   float* r32 = s_lv[0].r;
 
   // initial residual r = b - A x (or b); the V-cycle input is its FP32 copy
@@ -382,15 +399,15 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_cg_amg(CgAmgArgs a) {
       t = br;
     } else {
       const double* vv_ = a.x;
-      double s = row_gather<5>(a.rowptr, a.col, a.val, r, [&](int c) { return ldcg(vv_ + c); });
+      double s = row_gather<5>(a.rowptr, a.col, a.val, r, [&](int cc) { return ldcg(vv_ + cc); });
       t = br - s;
     }
     a.r[r] = t;
     r32[r] = (float)br;
   }
-  if (!grid_barrier(a.bar, nb, a.err)) return;
+  if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
   if (!a.guess_zero) {  // |M b| is the reference norm of a nonzero initial guess
-    if (!vcycle(s_lv, nlev, a.tl, alc, sb, buf, a.u, a.bar, nb, a.err)) return;
+    if (!vcycle(s_lv, nlev, s_tl, alc, sb, buf, lo, hi, a.u, Tm, a.err)) return;
     double acc[1] = {0.0};
     for (int r = own.r0 + tid; r < own.r1; r += kGmThreads) {
       const double zb = ldcg(a.u + r);
@@ -399,26 +416,20 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_cg_amg(CgAmgArgs a) {
     }
     block_reduce<1>(acc, s_warp, s_red);
     if (tid == 0) mypart[kMaxRestart + 3] = s_red[0];
-    if (!grid_barrier(a.bar, nb, a.err)) return;
+    if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
   }
-  if (!vcycle(s_lv, nlev, a.tl, alc, sb, buf, a.u, a.bar, nb, a.err)) return;
+  if (!vcycle(s_lv, nlev, s_tl, alc, sb, buf, lo, hi, a.u, Tm, a.err)) return;
 
-  double rnorm0 = 0.0, ttol = 0.0, dp = 0.0;
-  double gam_old = 0.0, dpi_old = 0.0;
-  int reason = 0, its = 0;
-  auto test = [&](double rn) -> int {
-    if (isnan(rn) || isinf(rn)) return -9;
-    if (rn <= ttol) return rn < a.abstol ? 3 : 2;
-    if (rn >= a.dtol * rnorm0) return -4;
-    return 0;
-  };
+  // CG scalars are uniform over the CTA: thread 0 keeps them in shared memory
+  __shared__ double s_sc[8];  // rnorm0, ttol, dp, gam_old, dpi_old, alpha, beta
+  __shared__ int s_st[3];     // reason, its, stop
   for (int i = 0;; i++) {
     // w = A u and the inner products (r,u), (w,u), (u,u), (u, s_old) of u = M r
     {
       double acc[4] = {0.0, 0.0, 0.0, 0.0};
       const double* uu = a.u;
       for (int r = own.r0 + tid; r < own.r1; r += kGmThreads) {
-        const double s = row_gather<5>(a.rowptr, a.col, a.val, r, [&](int c) { return ldcg(uu + c); });
+        const double s = row_gather<5>(a.rowptr, a.col, a.val, r, [&](int cc) { return ldcg(uu + cc); });
         a.w[r] = s;
         const double ur = ldcg(uu + r);
         acc[0] += ur * ldcg(a.r + r);
@@ -429,47 +440,56 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_cg_amg(CgAmgArgs a) {
       block_reduce<4>(acc, s_warp, s_red);
       if (tid < 4) mypart[tid] = s_red[tid];
     }
-    if (!grid_barrier(a.bar, nb, a.err)) return;
+    if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
     if (tid < 160) {
       const int q = tid >> 5;
       if (q < 4 || (i == 0 && !a.guess_zero)) {
-        double s = warp_sum_blocks(a.part, stride, q < 4 ? q : kMaxRestart + 3, nb);
+        double s = warp_sum_blocks(Tm.part, stride, q < 4 ? q : kMaxRestart + 3, Tm.size);
         if ((tid & 31) == 0) s_g[q] = s;
       }
     }
     __syncthreads();
-    const double gam = s_g[0], del = s_g[1], mu = s_g[3];
-    dp = sqrt(s_g[2]);
-    if (i == 0) {
-      rnorm0 = a.guess_zero ? dp : (s_g[4] != 0.0 ? sqrt(s_g[4]) : dp);
-      ttol = fmax(a.rtol * rnorm0, a.abstol);
+    if (tid == 0) {
+      const double gam = s_g[0], del = s_g[1], mu = s_g[3];
+      const double dp = sqrt(s_g[2]);
+      if (i == 0) {
+        s_sc[0] = a.guess_zero ? dp : (s_g[4] != 0.0 ? sqrt(s_g[4]) : dp);
+        s_sc[1] = fmax(a.rtol * s_sc[0], a.abstol);
+      }
+      const double rnorm0 = s_sc[0], ttol = s_sc[1], gam_old = s_sc[3], dpi_old = s_sc[4];
+      s_sc[2] = dp;
+      int reason = 0, its = i + 1, stop = 1;
+      if (isnan(dp) || isinf(dp)) reason = -9;
+      else if (dp <= ttol) reason = dp < a.abstol ? 3 : 2;
+      else if (dp >= a.dtol * rnorm0) reason = -4;
+      if (reason) its = i;
+      else if (i >= a.maxit) {
+        reason = -3;
+        its = i;
+      } else if (gam == 0.0) {
+        reason = 3;
+      } else if (i > 0 && gam * gam_old < 0.0) {
+        reason = -8;
+      } else {
+        const double beta = i == 0 ? 0.0 : -mu / dpi_old;
+        const double dpi = i == 0 ? del : del + beta * mu;  // (p, A p)
+        if (dpi == 0.0 || (i > 0 && sgn(dpi) * sgn(dpi_old) < 0)) {
+          reason = -10;
+        } else {
+          stop = 0;
+          s_sc[3] = gam;
+          s_sc[4] = dpi;
+          s_sc[5] = gam / dpi;
+          s_sc[6] = beta;
+        }
+      }
+      s_st[0] = reason;
+      s_st[1] = its;
+      s_st[2] = stop;
     }
-    reason = test(dp);
-    if (reason) {
-      its = i;
-      break;
-    }
-    if (i >= a.maxit) {
-      reason = -3;
-      its = i;
-      break;
-    }
-    its = i + 1;
-    if (gam == 0.0) {
-      reason = 3;
-      break;
-    }
-    if (i > 0 && gam * gam_old < 0.0) {
-      reason = -8;
-      break;
-    }
-    const double beta = i == 0 ? 0.0 : -mu / dpi_old;
-    const double dpi = i == 0 ? del : del + beta * mu;  // (p, A p)
-    if (dpi == 0.0 || (i > 0 && sgn(dpi) * sgn(dpi_old) < 0)) {
-      reason = -10;
-      break;
-    }
-    const double alpha = gam / dpi;
+    __syncthreads();
+    if (s_st[2]) break;
+    const double alpha = s_sc[5], beta = s_sc[6];
     {
       const double* __restrict__ U = a.u;
       const double* __restrict__ Wv = a.w;
@@ -509,96 +529,72 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_cg_amg(CgAmgArgs a) {
         }
       }
     }
-    gam_old = gam;
-    dpi_old = dpi;
-    if (!grid_barrier(a.bar, nb, a.err)) return;
-    if (!vcycle(s_lv, nlev, a.tl, alc, sb, buf, a.u, a.bar, nb, a.err)) return;
+    if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
+    if (!vcycle(s_lv, nlev, s_tl, alc, sb, buf, lo, hi, a.u, Tm, a.err)) return;
   }
-  if (blockIdx.x == 0 && tid == 0) {
-    a.out->its = its;
-    a.out->reason = reason;
-    a.out->rnorm = dp;
+  if (Tm.rank == 0 && tid == 0) {
+    a.out[c].its = s_st[1];
+    a.out[c].reason = s_st[0];
+    a.out[c].rnorm = s_sc[2];
   }
+  __syncthreads();
 }
 
-constexpr int align16(long b) { return (int)((b + 15) / 16 * 16); }
-
-// tail = the shortest suffix of levels ending at the coarsest whose arrays fit kTailBudget
-TailLayout tail_layout(const AmgHostView& h) {
-  TailLayout T{};
-  const int L = h.nlev;
-  auto level_bytes = [&](int l) -> long {
-    const AmgDevLevel& F = h.lv[l];
-    if (l == L - 1) return align16(4L * F.n * F.n) + 2L * align16(4L * F.n);
-    const int nc = h.lv[l + 1].n;
-    return align16(4L * (F.n + 1)) + align16(4L * F.nnz) + align16(4L * F.nnz) + align16(4L * F.n) +
-           align16(4L * F.n) + align16(4L * (nc + 1)) + align16(4L * F.n) + 3L * align16(4L * F.n);
-  };
-  long total = level_bytes(L - 1);
-  int t = L - 1;
-  while (t > 0 && total + level_bytes(t - 1) <= kTailBudget) total += level_bytes(--t);
-  T.tail = t;
-  int off = 0;
-  auto take = [&](long b) {
-    int o = off;
-    off += align16(b);
-    return o;
-  };
-  for (int l = 0; l < kAmgMaxLevels; l++) T.lv[l] = TailLevelOff{-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
-  for (int l = t; l < L; l++) {
-    const AmgDevLevel& F = h.lv[l];
-    TailLevelOff& o = T.lv[l];
-    if (l + 1 < L) {
-      o.rowptr = take(4L * (F.n + 1));
-      o.col = take(4L * F.nnz);
-      o.val = take(4L * F.nnz);
-      o.wdinv = take(4L * F.n);
-      o.agg = take(4L * F.n);
-      o.ptptr = take(4L * (h.lv[l + 1].n + 1));
-      o.ptrow = take(4L * F.n);
-      o.T = take(4L * F.n);
-    } else {
-      T.inv = take(4L * F.n * F.n);
-    }
-    o.R = take(4L * F.n);
-    o.X = take(4L * F.n);
+__global__ void __launch_bounds__(kGmThreads, 1) k_cg_amg(CgAmgArgs a) {
+  if (!a.sched) {
+    const Team T{(int)blockIdx.x, a.nb, a.bar, a.part};
+    cg_amg_team(a, T, 0);
+    return;
   }
-  T.bytes = off;
-  return T;
+  const BatchSchedule& S = *a.sched;
+  const int team = S.cta_team[blockIdx.x];
+  const Team T{S.cta_rank[blockIdx.x], S.team_size[team], a.bar + 2L * team,
+               a.part + (long)S.team_cta0[team] * kPartStride};
+  for (int k = S.team_case0[team]; k < S.team_case0[team + 1]; k++) {
+    cg_amg_team(a, T, S.case_list[k]);
+    if (*(volatile int*)a.err) return;
+  }
 }
 
 }  // namespace
 
 void launch_amg_setup_values(const AmgHostView& h, cudaStream_t s) {
-  // FP32 copy of the pressure matrix, Galerkin sums down the hierarchy, Jacobi weights, and
-  // the dense inverse of the coarsest level
-  const AmgDevLevel& F0 = h.lv[0];
-  ++g_launch_count, k_amg_level0<<<(F0.nnz + kThreads - 1) / kThreads, kThreads, 0, s>>>(F0.nnz, F0.val64, F0.val);
-  ++g_launch_count, k_amg_wdinv<<<(F0.n + kThreads - 1) / kThreads, kThreads, 0, s>>>(F0.n, h.omega, F0.diag, F0.val,
-                                                                                     F0.wdinv);
-  for (int l = 0; l + 1 < h.nlev; l++) {
-    const AmgDevLevel& F = h.lv[l];
-    const AmgDevLevel& C = h.lv[l + 1];
+  // FP32 copy of the pressure matrix, Galerkin sums down every hierarchy, Jacobi weights, and
+  // the dense inverse of every case's coarsest level
+  const int D = (int)h.dep.size();
+  const AmgHostView::Depth& d0 = h.dep[0];
+  ++g_launch_count, k_amg_level0<<<(d0.nnz + kThreads - 1) / kThreads, kThreads, 0, s>>>(d0.nnz, h.val64, d0.val);
+  ++g_launch_count, k_amg_wdinv<<<(d0.nrows + kThreads - 1) / kThreads, kThreads, 0, s>>>(d0.nrows, h.omega, d0.diag,
+                                                                                         d0.val, d0.wdinv);
+  for (int l = 0; l + 1 < D; l++) {
+    const AmgHostView::Depth& F = h.dep[l];
+    const AmgHostView::Depth& C = h.dep[l + 1];
     ++g_launch_count, k_amg_galerkin<<<(C.nnz + kThreads - 1) / kThreads, kThreads, 0, s>>>(C.nnz, F.cptr, F.csrc,
                                                                                            F.val, C.val);
-    ++g_launch_count, k_amg_wdinv<<<(C.n + kThreads - 1) / kThreads, kThreads, 0, s>>>(C.n, h.omega, C.diag, C.val,
-                                                                                      C.wdinv);
+    ++g_launch_count, k_amg_wdinv<<<(C.nrows + kThreads - 1) / kThreads, kThreads, 0, s>>>(C.nrows, h.omega, C.diag,
+                                                                                          C.val, C.wdinv);
   }
-  const AmgDevLevel& K = h.lv[h.nlev - 1];
-  ++g_launch_count, k_amg_coarse_inverse<<<1, 1024, 0, s>>>(K.n, K.rowptr, K.col, K.diag, K.val, h.coarse_inv);
+  ++g_launch_count, k_amg_coarse_inverse<<<h.ncases, 1024, 0, s>>>(h.d_cases);
 }
 
-cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& w, cudaStream_t s) {
-  if (5L * w.ldv > w.v_len || (long)gmres_grid(c.n, w.nblocks) * kPartStride > w.part_len || w.ldv < c.n ||
-      h.nlev < 1 || h.nlev > kAmgMaxLevels || h.lv[h.nlev - 1].n > kAmgCoarseMax || h.lv[0].n != c.n)
+cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& w, const BatchSchedule* sched,
+                          int grid, KspOut* out, cudaStream_t s) {
+  if (5L * w.ldv > w.v_len || (long)grid * kPartStride > w.part_len || w.ldv < c.n || h.ncases < 1 ||
+      grid < 1 || (!sched && h.ncases != 1))
     return cudaErrorInvalidValue;
-  for (int l = 0; l + 1 < h.nlev; l++)
-    if (h.lv[l].maxagg > kDownBuf) return cudaErrorInvalidValue;
+  for (int k = 0; k < h.ncases; k++) {
+    const AmgCaseDesc& cd = h.cases[k];
+    if (cd.nlev < 1 || cd.nlev > kAmgMaxLevels || h.levels[k][cd.nlev - 1].n > kAmgCoarseMax || cd.lo < 0 ||
+        cd.hi > c.n || cd.lo >= cd.hi)
+      return cudaErrorInvalidValue;
+    for (int l = 0; l + 1 < cd.nlev; l++)
+      if (h.levels[k][l].maxagg > kAmgDownBuf) return cudaErrorInvalidValue;
+  }
   CgAmgArgs a;
   a.n = c.n;
   a.maxit = c.maxit;
   a.guess_zero = c.guess_zero;
-  a.nb = gmres_grid(c.n, w.nblocks);
+  a.nb = grid;
   a.rowptr = c.rowptr;
   a.col = c.col;
   a.val = c.val;
@@ -612,21 +608,18 @@ cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& 
   a.part = w.part;
   a.bar = w.bar;
   a.err = c.err;
-  a.out = c.out;
+  a.out = out;
   a.rtol = c.rtol;
   a.abstol = 1e-50;
   a.dtol = 1e4;
-  a.amg.nlev = h.nlev;
-  a.amg.omega = h.omega;
-  a.amg.alpha = h.alpha;
-  a.amg.coarse_inv = h.coarse_inv;
-  a.amg.levels = h.d_levels;
-  a.tl = tail_layout(h);
-  const int smem = a.tl.bytes + kDownBuf * (int)sizeof(float);
+  a.alpha = h.alpha;
+  a.cases = h.d_cases;
+  a.sched = sched;
+  const int smem = h.smem_bytes;
   cudaError_t e = cudaFuncSetAttribute((const void*)k_cg_amg, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)k_cg_amg, dim3(a.nb), dim3(kGmThreads), args, smem, s);
+  return cudaLaunchCooperativeKernel((const void*)k_cg_amg, dim3(grid), dim3(kGmThreads), args, smem, s);
 }
 
 }  // namespace cycas

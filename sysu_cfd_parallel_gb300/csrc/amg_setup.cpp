@@ -139,3 +139,233 @@ AmgHostHierarchy amg_build(int n, const int* rowptr, const int* col, const doubl
 }
 
 }  // namespace cycas
+
+// ------------------------------------------------------------------ multi-case upload
+namespace cycas {
+
+namespace {
+
+int align16(long b) { return (int)((b + 15) / 16 * 16); }
+
+// tail = the shortest suffix of levels ending at the coarsest whose arrays fit the budget
+TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz) {
+  TailLayout T{};
+  const int L = (int)n.size();
+  auto level_bytes = [&](int l) -> long {
+    if (l == L - 1) return align16(4L * n[l] * n[l]) + 2L * align16(4L * n[l]);
+    return align16(4L * (n[l] + 1)) + 2L * align16(4L * nnz[l]) + align16(4L * n[l]) + align16(4L * n[l]) +
+           align16(4L * (n[l + 1] + 1)) + align16(4L * n[l]) + 3L * align16(4L * n[l]);
+  };
+  long total = level_bytes(L - 1);
+  int t = L - 1;
+  while (t > 0 && total + level_bytes(t - 1) <= kAmgTailBudget) total += level_bytes(--t);
+  T.tail = t;
+  int off = 0;
+  auto take = [&](long b) {
+    int o = off;
+    off += align16(b);
+    return o;
+  };
+  for (int l = 0; l < kAmgMaxLevels; l++) T.lv[l] = TailLevelOff{-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  for (int l = t; l < L; l++) {
+    TailLevelOff& o = T.lv[l];
+    if (l + 1 < L) {
+      o.rowptr = take(4L * (n[l] + 1));
+      o.col = take(4L * nnz[l]);
+      o.val = take(4L * nnz[l]);
+      o.wdinv = take(4L * n[l]);
+      o.agg = take(4L * n[l]);
+      o.ptptr = take(4L * (n[l + 1] + 1));
+      o.ptrow = take(4L * n[l]);
+      o.T = take(4L * n[l]);
+    } else {
+      T.inv = take(4L * n[l] * n[l]);
+    }
+    o.R = take(4L * n[l]);
+    o.X = take(4L * n[l]);
+  }
+  T.bytes = off;
+  return T;
+}
+
+}  // namespace
+
+void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, const double* weight,
+                     const int* rowptr_dev, const int* col_dev, const int* diag_dev, const double* val64_dev,
+                     const std::vector<int>& lo, const std::vector<int>& hi, AmgUploader& up) {
+  const int nc = (int)lo.size();
+  std::vector<AmgHostHierarchy> H(nc);
+  int D = 0;
+  for (int c = 0; c < nc; c++) {
+    const int l0 = lo[c], nr = hi[c] - lo[c], k0 = rowptr[l0];
+    if (nr < 1 || hi[c] > n) throw std::runtime_error("AMG: empty or out-of-range case");
+    std::vector<int> rp(nr + 1), cl(rowptr[hi[c]] - k0);
+    std::vector<double> w(cl.size());
+    for (int i = 0; i <= nr; i++) rp[i] = rowptr[l0 + i] - k0;
+    for (size_t k = 0; k < cl.size(); k++) {
+      const int j = col[k0 + k];
+      if (j < l0 || j >= hi[c]) throw std::runtime_error("AMG: the pressure system couples two cases");
+      cl[k] = j - l0;
+      w[k] = weight[k0 + k];
+    }
+    H[c] = amg_build(nr, rp.data(), cl.data(), w.data(), 4, kAmgCoarseMax, kAmgMaxLevels);
+    if (H[c].lv.back().n > kAmgCoarseMax)
+      throw std::runtime_error("aggregation did not reach a small enough coarsest level");
+    D = std::max(D, (int)H[c].lv.size());
+  }
+  v.ncases = nc;
+  v.val64 = val64_dev;
+  v.dep.assign(D, AmgHostView::Depth{});
+  v.levels.assign(nc, std::vector<AmgDevLevel>());
+  v.cases.assign(nc, AmgCaseDesc{});
+  for (int c = 0; c < nc; c++) v.levels[c].assign(H[c].lv.size(), AmgDevLevel{});
+
+  // offsets of every case's slice per depth (cases without the level get none)
+  std::vector<std::vector<int>> row_off(D, std::vector<int>(nc, -1)), nnz_off(D, std::vector<int>(nc, -1)),
+      rp_off(D, std::vector<int>(nc, -1)), pt_off(D, std::vector<int>(nc, -1)), ptr_off(D, std::vector<int>(nc, -1)),
+      cp_off(D, std::vector<int>(nc, -1));
+  std::vector<int> nrows(D, 0), nnzs(D, 0), nrp(D, 0), npt(D, 0), nptr(D, 0), ncp(D, 0);
+  for (int l = 0; l < D; l++)
+    for (int c = 0; c < nc; c++) {
+      if ((int)H[c].lv.size() <= l) continue;
+      const AmgHostLevel& L = H[c].lv[l];
+      row_off[l][c] = l == 0 ? lo[c] : nrows[l];
+      nnz_off[l][c] = l == 0 ? rowptr[lo[c]] : nnzs[l];
+      rp_off[l][c] = nrp[l];
+      if (l > 0) {
+        nrows[l] += L.n;
+        nnzs[l] += L.nnz;
+        nrp[l] += L.n + 1;
+      }
+      if (l + 1 < (int)H[c].lv.size()) {
+        pt_off[l][c] = npt[l];
+        npt[l] += (int)L.ptptr.size();
+        ptr_off[l][c] = nptr[l];
+        nptr[l] += L.n;
+        cp_off[l][c] = ncp[l];
+        ncp[l] += (int)L.csrc.size();
+      }
+    }
+  nrows[0] = n;
+  nnzs[0] = rowptr[n];
+
+  // host arrays per depth
+  for (int l = 0; l < D; l++) {
+    std::vector<int> rp, cl, dg, ag, pp, pr, cptr, csrc;
+    if (l > 0) {
+      rp.reserve(nrp[l]);
+      cl.reserve(nnzs[l]);
+      dg.reserve(nrows[l]);
+    }
+    ag.assign(l == 0 ? n : nrows[l], -1);
+    for (int c = 0; c < nc; c++) {
+      if ((int)H[c].lv.size() <= l) continue;
+      const AmgHostLevel& L = H[c].lv[l];
+      if (l > 0) {
+        rp.insert(rp.end(), L.rowptr.begin(), L.rowptr.end());
+        cl.insert(cl.end(), L.col.begin(), L.col.end());
+        for (int i = 0; i < L.n; i++) dg.push_back(L.diag[i] + nnz_off[l][c]);
+      }
+      if (l + 1 < (int)H[c].lv.size()) {
+        for (int i = 0; i < L.n; i++) ag[row_off[l][c] + i] = L.agg[i];
+        pp.insert(pp.end(), L.ptptr.begin(), L.ptptr.end());
+        for (int i = 0; i < L.n; i++) pr.push_back(L.ptrow[i] + (l == 0 ? lo[c] : 0));
+      }
+    }
+    // Galerkin map into depth l+1, in the depth l+1 order of cases
+    if (l + 1 < D) {
+      cptr.push_back(0);
+      for (int c = 0; c < nc; c++) {
+        if ((int)H[c].lv.size() <= l + 1) continue;
+        const AmgHostLevel& L = H[c].lv[l];
+        const int base = cptr.back();
+        for (size_t q = 1; q < L.cptr.size(); q++) cptr.push_back(base + L.cptr[q]);
+        for (int k : L.csrc) csrc.push_back(k + nnz_off[l][c]);
+      }
+    }
+    AmgHostView::Depth& d = v.dep[l];
+    d.nrows = nrows[l];
+    d.nnz = nnzs[l];
+    const int* d_rp = l == 0 ? rowptr_dev : up.upload_int(rp.data(), (long)rp.size());
+    const int* d_cl = l == 0 ? col_dev : up.upload_int(cl.data(), (long)cl.size());
+    d.diag = l == 0 ? diag_dev : up.upload_int(dg.data(), (long)dg.size());
+    d.val = up.alloc_float(std::max(1, nnzs[l]));
+    d.wdinv = up.alloc_float(std::max(1, nrows[l]));
+    float* d_r = up.alloc_float(std::max(1, nrows[l]));
+    float* d_t = l == 0 ? nullptr : up.alloc_float(std::max(1, nrows[l]));
+    const int* d_ag = up.upload_int(ag.data(), (long)ag.size());
+    const int* d_pp = pp.empty() ? nullptr : up.upload_int(pp.data(), (long)pp.size());
+    const int* d_pr = pr.empty() ? nullptr : up.upload_int(pr.data(), (long)pr.size());
+    if (l + 1 < D) {
+      d.cptr = up.upload_int(cptr.data(), (long)cptr.size());
+      d.csrc = up.upload_int(csrc.data(), (long)csrc.size());
+      d.nnz_next = (int)cptr.size() - 1;
+    }
+    for (int c = 0; c < nc; c++) {
+      if ((int)H[c].lv.size() <= l) continue;
+      const AmgHostLevel& L = H[c].lv[l];
+      AmgDevLevel& e = v.levels[c][l];
+      e.n = L.n;
+      e.nnz = L.nnz;
+      e.maxagg = 0;
+      for (size_t I = 0; I + 1 < L.ptptr.size(); I++) e.maxagg = std::max(e.maxagg, L.ptptr[I + 1] - L.ptptr[I]);
+      if (l == 0) {
+        e.nnz_off = 0;
+        e.rowptr = d_rp;
+        e.col = d_cl;
+        e.diag = d.diag;
+        e.val = d.val;
+        e.wdinv = d.wdinv;
+        e.agg = d_ag;
+        e.r = d_r;
+        e.t = nullptr;
+      } else {
+        e.nnz_off = nnz_off[l][c];
+        e.rowptr = d_rp + rp_off[l][c];
+        e.col = d_cl + nnz_off[l][c];
+        e.diag = d.diag + row_off[l][c];
+        e.val = d.val + nnz_off[l][c];
+        e.wdinv = d.wdinv + row_off[l][c];
+        e.agg = d_ag + row_off[l][c];
+        e.r = d_r + row_off[l][c];
+        e.t = d_t + row_off[l][c];
+      }
+      e.ptptr = pt_off[l][c] >= 0 ? d_pp + pt_off[l][c] : nullptr;
+      e.ptrow = ptr_off[l][c] >= 0 ? d_pr + ptr_off[l][c] : nullptr;
+    }
+  }
+
+  // dense inverses, per-case descriptors
+  long ninv = 0;
+  std::vector<long> inv_off(nc);
+  for (int c = 0; c < nc; c++) {
+    inv_off[c] = ninv;
+    const int m = H[c].lv.back().n;
+    ninv += (long)m * m;
+  }
+  v.coarse_inv = up.alloc_float(std::max(1L, ninv));
+  int tail_max = 0;
+  for (int c = 0; c < nc; c++) {
+    std::vector<int> ln, lz;
+    for (const AmgHostLevel& L : H[c].lv) {
+      ln.push_back(L.n);
+      lz.push_back(L.nnz);
+    }
+    AmgCaseDesc& cd = v.cases[c];
+    cd.lo = lo[c];
+    cd.hi = hi[c];
+    cd.nlev = (int)H[c].lv.size();
+    cd.coarse_inv = v.coarse_inv + inv_off[c];
+    cd.levels = (const AmgDevLevel*)up.upload_bytes(v.levels[c].data(), sizeof(AmgDevLevel) * cd.nlev);
+    cd.tl = tail_layout(ln, lz);
+    tail_max = std::max(tail_max, cd.tl.bytes);
+    if (c == 0) {
+      v.rows0 = ln;
+      v.nnz0 = lz;
+    }
+  }
+  v.d_cases = (AmgCaseDesc*)up.upload_bytes(v.cases.data(), sizeof(AmgCaseDesc) * nc);
+  v.smem_bytes = tail_max + kAmgDownBuf * (int)sizeof(float);
+}
+
+}  // namespace cycas

@@ -104,6 +104,7 @@ struct cycas_ctx {
   AmgHostView amg;               // pressure preconditioner hierarchy (PC_AMG)
   std::vector<int> amg_sizes;  // rows per AMG level (fine to coarse)
   std::vector<int> amg_nnz;    // stored entries per AMG level
+  std::vector<int> case_lo, case_hi;  // row ranges of the independent cases (one for a context)
 
   template <class T>
   T* alloc(long n) {
@@ -398,48 +399,17 @@ void setup_amg(cycas_ctx& c) {
       int s = slot[(size_t)j * n + i];
       if (s >= 0) w[s] = rl[faces[(size_t)j * n + i]];
     }
-  AmgHostHierarchy H = amg_build(n, rowptr.data(), col.data(), w.data(), 4, kAmgCoarseMax, kAmgMaxLevels);
-  require(H.lv.back().n <= kAmgCoarseMax, "aggregation did not reach a small enough coarsest level");
-  AmgHostView& v = c.amg;
-  v.nlev = (int)H.lv.size();
-  for (int l = 0; l < v.nlev; l++) {
-    const AmgHostLevel& h = H.lv[l];
-    AmgDevLevel d{};
-    d.n = h.n;
-    d.nnz = h.nnz;
-    d.maxagg = 0;
-    for (size_t I = 0; I + 1 < h.ptptr.size(); I++) d.maxagg = std::max(d.maxagg, h.ptptr[I + 1] - h.ptptr[I]);
-    if (l == 0) {
-      d.rowptr = c.m.rowptr;
-      d.col = c.m.col;
-      d.val64 = c.f.Ap;
-    } else {
-      d.rowptr = c.upload(h.rowptr.data(), h.n + 1L);
-      d.col = c.upload(h.col.data(), h.nnz);
-      d.val64 = nullptr;
-    }
-    d.val = c.alloc<float>(h.nnz);
-    d.wdinv = c.alloc<float>(h.n);
-    d.diag = c.upload(h.diag.data(), h.n);
-    if (l + 1 < v.nlev) {
-      d.agg = c.upload(h.agg.data(), h.n);
-      d.ptptr = c.upload(h.ptptr.data(), (long)h.ptptr.size());
-      d.ptrow = c.upload(h.ptrow.data(), (long)h.ptrow.size());
-      d.cptr = c.upload(h.cptr.data(), (long)h.cptr.size());
-      d.csrc = c.upload(h.csrc.data(), (long)h.csrc.size());
-    }
-    d.r = c.alloc<float>(h.n);
-    d.t = c.alloc<float>(h.n);
-    v.lv[l] = d;
-  }
-  v.d_levels = c.upload(v.lv, v.nlev);
-  v.coarse_inv = c.alloc<float>((long)kAmgCoarseMax * kAmgCoarseMax);
-  c.amg_sizes.clear();
-  c.amg_nnz.clear();
-  for (auto& h : H.lv) {
-    c.amg_sizes.push_back(h.n);
-    c.amg_nnz.push_back(h.nnz);
-  }
+  struct Up : AmgUploader {
+    cycas_ctx& c;
+    explicit Up(cycas_ctx& cc) : c(cc) {}
+    const int* upload_int(const int* h, long n) override { return c.upload(h, n); }
+    float* alloc_float(long n) override { return c.alloc<float>(n); }
+    void* upload_bytes(const void* h, long bytes) override { return c.upload((const unsigned char*)h, bytes); }
+  } up(c);
+  amg_setup_cases(c.amg, n, rowptr.data(), col.data(), w.data(), c.m.rowptr, c.m.col, c.m.c_diag, c.f.Ap,
+                  c.case_lo, c.case_hi, up);
+  c.amg_sizes = c.amg.rows0;
+  c.amg_nnz = c.amg.nnz0;
 }
 
 void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
@@ -500,7 +470,7 @@ void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const d
   if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot][0], c.stream));
   if (k.pc == CYCAS_PC_AMG) {
     launch_amg_setup_values(c.amg, c.stream);
-    CK(launch_cg_amg(g, c.amg, c.kw, c.stream));
+    CK(launch_cg_amg(g, c.amg, c.kw, nullptr, gmres_grid(g.n, c.kw.nblocks), g.out, c.stream));
   } else if (k.type == CYCAS_KSP_CG) {
     CK(launch_cg(g, c.kw, c.stream));
   } else {
@@ -834,6 +804,8 @@ int cycas_create(const cycas_mesh_view* mesh, const cycas_params* params, const 
       build_device_mesh(*c, *mesh);
       alloc_fields(*c);
       alloc_krylov(*c);
+      c->case_lo = {0};
+      c->case_hi = {c->m.ncel};
       if (c->ksp[CYCAS_SYS_PRESSURE].pc == CYCAS_PC_AMG) setup_amg(*c);
       CK(cudaStreamSynchronize(c->stream));
     } catch (...) {

@@ -1,4 +1,11 @@
 // Aggregation multigrid for the pressure-correction system: host hierarchy and device levels.
+//
+// Several independent cases (the members of a batch, or the single case of a context) each
+// get their own hierarchy.  On the device, level l of every case that has one is stored in
+// one concatenated array per level depth (so the per-solve setup is one launch per depth),
+// and every case carries a descriptor with pointers to its slices.  Level 0 is the pressure
+// system itself, in the system's global row numbering; coarser levels are numbered locally
+// within their case.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -7,7 +14,9 @@
 namespace cycas {
 
 constexpr int kAmgMaxLevels = 12;
-constexpr int kAmgCoarseMax = 64;  // the coarsest level is inverted densely by one CTA
+constexpr int kAmgCoarseMax = 64;            // the coarsest level is inverted densely by one CTA
+constexpr int kAmgDownBuf = 8192;            // floats of the per-CTA restriction buffer
+constexpr int kAmgTailBudget = 160 * 1024;   // shared-memory bytes for a case's tail levels
 
 struct AmgHostLevel {
   int n = 0, nnz = 0;
@@ -24,49 +33,94 @@ struct AmgHostHierarchy {
 AmgHostHierarchy amg_build(int n, const int* rowptr, const int* col, const double* weight, int maxsize,
                            int coarse_max, int max_levels);
 
-// One level of the device hierarchy.  The V-cycle runs in FP32 (it is only a preconditioner;
-// the CG around it is FP64), so every level keeps FP32 values; level 0 also points at the
-// FP64 pressure matrix the FP32 copy is made from.
+// One level of one case, as the V-cycle sees it.
 struct AmgDevLevel {
   int n, nnz;
-  int maxagg;  // largest aggregate (fine rows per coarse row); 0 on the coarsest level
-  const int* rowptr;
-  const int* col;
-  const int* diag;     // position of the diagonal in each row
-  const double* val64; // level 0 only: the FP64 system matrix
-  float* val;          // FP32 matrix values (level 0: rounded copy; coarser: Galerkin sums)
-  float* wdinv;        // w / a_ii
-  const int* agg;
-  const int* ptptr;
-  const int* ptrow;
-  const int* cptr;
-  const int* csrc;
-  float* r;  // residual on this level (level 0: FP32 copy of the CG residual)
-  float* t;  // correction returned to the finer level
+  int maxagg;         // largest aggregate (rows per coarse row); 0 on the coarsest level
+  int nnz_off;        // position of this case's first entry in the depth's concatenated values
+  const int* rowptr;  // level 0: the system's row pointers (global positions); else local
+  const int* col;     // level 0: global columns; else local
+  const int* diag;    // global position of each row's diagonal in the depth's values
+  float* val;         // FP32 values (level 0: all rows of the system, global positions)
+  float* wdinv;       // w / a_ii (level 0: indexed by global row)
+  const int* agg;     // row -> coarse row (level 0: indexed by global row)
+  const int* ptptr;   // coarse row -> range in ptrow (local)
+  const int* ptrow;   // rows of each aggregate (level 0: global rows)
+  float* r;           // residual (level 0: FP32 copy of the CG residual, global rows)
+  float* t;           // correction returned to the finer level (levels >= 1)
 };
 
-// host-side record of the device hierarchy
-struct AmgHostView {
-  int nlev = 0;
-  float omega = 2.0f / 3.0f, alpha = 2.0f;
-  float* coarse_inv = nullptr;
-  AmgDevLevel* d_levels = nullptr;
-  AmgDevLevel lv[kAmgMaxLevels];
+// byte offsets of one tail level's arrays in dynamic shared memory
+struct TailLevelOff {
+  int rowptr, col, val, wdinv, agg, ptptr, ptrow, R, X, T;
 };
 
-struct AmgDev {
+// the coarsest levels of a case, cycled by one CTA out of shared memory
+struct TailLayout {
+  int tail;   // first level of the tail (levels tail..nlev-1)
+  int bytes;  // dynamic shared memory taken by the tail (multiple of 16)
+  int inv;    // offset of the coarsest level's dense inverse
+  TailLevelOff lv[kAmgMaxLevels];
+};
+
+struct AmgCaseDesc {
+  int lo, hi;                 // rows of the case in the pressure system
   int nlev;
-  float omega;          // Jacobi weight
-  float alpha;          // coarse-correction scaling
-  float* coarse_inv;    // dense inverse of the (regularised) coarsest matrix, row-major
-  AmgDevLevel* levels;  // device array [nlev]
+  const float* coarse_inv;    // dense inverse of the (regularised) coarsest level, row-major
+  const AmgDevLevel* levels;  // device array [nlev]
+  TailLayout tl;
 };
+
+// host-side record of the device hierarchies of all cases
+struct AmgHostView {
+  int ncases = 0;
+  float omega = 2.0f / 3.0f, alpha = 2.0f;
+  std::vector<AmgCaseDesc> cases;                // host copies (level pointers are device arrays)
+  std::vector<std::vector<AmgDevLevel>> levels;  // [case][level] host copies
+  AmgCaseDesc* d_cases = nullptr;                // device [ncases]
+  int smem_bytes = 0;                            // dynamic shared memory of the solver kernel
+  // per-depth concatenated arrays, for the per-solve setup launches
+  struct Depth {
+    int nrows = 0, nnz = 0;
+    const int* diag = nullptr;  // [nrows] global positions of the diagonals
+    float* val = nullptr;       // [nnz]
+    float* wdinv = nullptr;     // [nrows]
+    const int* cptr = nullptr;  // depth+1 nnz -> range in csrc (null for the deepest depth)
+    const int* csrc = nullptr;  // positions in this depth's values
+    int nnz_next = 0;           // entries of depth+1
+  };
+  std::vector<Depth> dep;
+  const double* val64 = nullptr;  // FP64 pressure matrix (depth 0 source)
+  float* coarse_inv = nullptr;    // all cases' inverses
+  std::vector<int> rows0, nnz0;   // level sizes of case 0, for reporting
+};
+
+// Device memory for the hierarchy (implemented by the owner of the device allocations).
+struct AmgUploader {
+  virtual const int* upload_int(const int* h, long n) = 0;
+  virtual float* alloc_float(long n) = 0;
+  virtual void* upload_bytes(const void* h, long bytes) = 0;
+  virtual ~AmgUploader() = default;
+};
+
+// Builds and uploads the hierarchies of the cases [lo[c], hi[c]) of one pattern: rowptr/col
+// (host, all rows, global columns) with strength weights per entry; the *_dev pointers are the
+// same pattern on the device, diag_dev its diagonal positions and val64_dev the FP64 values.
+void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, const double* weight,
+                     const int* rowptr_dev, const int* col_dev, const int* diag_dev, const double* val64_dev,
+                     const std::vector<int>& lo, const std::vector<int>& hi, AmgUploader& up);
 
 struct GmresCall;
 struct KrylovWork;
-// Galerkin values and diagonal inverses of levels 1.., dense inverse of the coarsest level
+struct BatchSchedule;
+struct KspOut;
+// FP32 values of every level (Galerkin sums down each hierarchy), Jacobi weights, and the
+// dense inverse of every case's coarsest level
 void launch_amg_setup_values(const AmgHostView& h, cudaStream_t s);
-// PETSc-style CG preconditioned by one V-cycle (persistent cooperative kernel)
-cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& w, cudaStream_t s);
+// CG preconditioned by one V-cycle (persistent cooperative kernel of `grid` CTAs); case 0 over
+// the whole grid when sched is null, else the teams of sched solve their cases.  Case c
+// reports to out[c].
+cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& w, const BatchSchedule* sched,
+                          int grid, KspOut* out, cudaStream_t s);
 
 }  // namespace cycas

@@ -134,6 +134,19 @@ void launch_finalize_residual(const double* red, int nparts, int slot, DevStatus
 int residual_blocks(int n);
 
 // Krylov
+// Batched Krylov solves: the CTAs of one cooperative launch are split into teams; each team
+// solves the row ranges of its cases one after another, synchronising only its own CTAs.
+struct BatchSchedule {
+  const int* cta_team;    // [grid] team of each CTA
+  const int* cta_rank;    // [grid] rank of each CTA in its team
+  const int* team_size;   // [nteams] CTAs per team
+  const int* team_cta0;   // [nteams] first CTA of the team (its partial-sum slots)
+  const int* team_case0;  // [nteams + 1] the team's cases are case_list[team_case0[t] .. team_case0[t+1])
+  const int* case_list;   // case indices in team order
+  const int* case_lo;     // [ncases] first row of each case
+  const int* case_hi;     // [ncases] one past its last row
+};
+
 struct GmresCall {
   int n;
   const int* rowptr;

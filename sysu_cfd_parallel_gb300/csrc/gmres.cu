@@ -34,7 +34,7 @@ enum Mode { M_START = 0, M_ARNOLDI = 1, M_RESTART = 2, M_FINAL = 3, M_DONE = 4 }
 
 template <int NS>
 struct GmMsArgs {
-  int n, m, maxit, nb, chunk;
+  int n, m, maxit, nb;
   const int* __restrict__ rowptr;
   const int* __restrict__ col;
   const double* __restrict__ val;
@@ -49,6 +49,16 @@ struct GmMsArgs {
   int* err;
   KspOut* out[NS];
   double rtol, abstol, dtol, haptol;
+  // batched solves: teams of CTAs, each solving its cases' row ranges in turn (null: one team
+  // of the whole grid solving rows [0, n))
+  const BatchSchedule* sched;
+};
+
+// the CTAs that solve one row range together
+struct Team {
+  int rank, size;  // this CTA's index in the team, CTAs in the team
+  unsigned* bar;   // the team's barrier words
+  double* part;    // the team's partial sums [size][NS][kPartStride]
 };
 
 // sum over CSR row r of val[k] * vec_s[col[k]] for every system s in mask, column order; W
@@ -83,7 +93,7 @@ __device__ __forceinline__ void row_gather_ms(const int* __restrict__ rowptr, co
 }
 
 template <int NS>
-__global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
+__device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T, int lo, int hi, KspOut* const* out) {
   constexpr int M = kMaxRestart;
   constexpr int MAXP = NS * (M + 1);
   __shared__ double s_hh[NS][(M + 1) * M];
@@ -96,11 +106,12 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
   __shared__ unsigned char s_ps[MAXP], s_pq[MAXP];
   __shared__ int s_npairs;
 
-  const int m = a.m, nb = a.nb, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int r0 = blockIdx.x * a.chunk;
-  const int r1 = min(a.n, r0 + a.chunk);
+  const int m = a.m, nb = T.size, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int chunk = (hi - lo + nb - 1) / nb;
+  const int r0 = min(hi, lo + T.rank * chunk);
+  const int r1 = min(hi, r0 + chunk);
   const int kNorm = M + 1, kInit = M + 2;
-  auto part_of = [&](int blk, int s) { return a.part + ((long)blk * NS + s) * kPartStride; };
+  auto part_of = [&](int blk, int s) { return T.part + ((long)blk * NS + s) * kPartStride; };
   auto Vv = [&](int s, int q) { return a.V + ((long)s * (m + 1) + q) * a.ldv; };
 
   if (tid < NS) {
@@ -198,10 +209,10 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
       for (int p = tid; p < P; p += kGmThreads) {
         double sum = 0.0;
         for (int k = 0; k < wpp; k++) sum += s_pair[p * wpp + k];
-        part_of(blockIdx.x, s_ps[p])[s_pq[p]] = sum;
+        part_of(T.rank, s_ps[p])[s_pq[p]] = sum;
       }
     }
-    if (!grid_barrier(a.bar, nb, a.err)) return;
+    if (!grid_barrier(T.bar, nb, a.err)) return;
 
     // ------------------------------------------------------------ phase Y
     unsigned res_mask = 0;
@@ -212,7 +223,7 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
       const int P = s_npairs;
       for (int p = wid; p < P; p += kGmWarps) {
         const int s = s_ps[p], q = s_pq[p];
-        const double* base = a.part + (long)s * kPartStride + q;
+        const double* base = T.part + (long)s * kPartStride + q;
         double sum = 0.0;
         for (int blk = lane; blk < nb; blk += 32) sum += ldcg(base + (long)blk * NS * kPartStride);
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
@@ -237,7 +248,7 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
         }
       }
       block_reduce<NS>(nrm, s_warp, s_red);
-      if (tid < NS && ((arn >> tid) & 1u)) part_of(blockIdx.x, tid)[kNorm] = s_red[tid];
+      if (tid < NS && ((arn >> tid) & 1u)) part_of(T.rank, tid)[kNorm] = s_red[tid];
     }
     if (res_mask) {
       const double* xs[NS];
@@ -271,9 +282,9 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
         }
       }
       block_reduce<2 * NS>(acc, s_warp, s_red);
-      if (tid < 2 * NS && ((res_mask >> (tid >> 1)) & 1u)) part_of(blockIdx.x, tid >> 1)[kInit + (tid & 1)] = s_red[tid];
+      if (tid < 2 * NS && ((res_mask >> (tid >> 1)) & 1u)) part_of(T.rank, tid >> 1)[kInit + (tid & 1)] = s_red[tid];
     }
-    if (!grid_barrier(a.bar, nb, a.err)) return;
+    if (!grid_barrier(T.bar, nb, a.err)) return;
 
     // ------------------------------------------------------------ phase Z (warp s controls system s)
     if (wid < NS) {
@@ -400,10 +411,32 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
     }
     __syncthreads();
   }
-  if (blockIdx.x == 0 && tid < NS) {
-    a.out[tid]->its = s_its[tid];
-    a.out[tid]->reason = s_reason[tid];
-    a.out[tid]->rnorm = s_rnorm[tid];
+  if (T.rank == 0 && tid < NS) {
+    out[tid]->its = s_its[tid];
+    out[tid]->reason = s_reason[tid];
+    out[tid]->rnorm = s_rnorm[tid];
+  }
+  __syncthreads();
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
+  if (!a.sched) {
+    const Team T{(int)blockIdx.x, a.nb, a.bar, a.part};
+    gmres_team<NS>(a, T, 0, a.n, a.out);
+    return;
+  }
+  const BatchSchedule& S = *a.sched;
+  const int team = S.cta_team[blockIdx.x];
+  const Team T{S.cta_rank[blockIdx.x], S.team_size[team], a.bar + 2L * team,
+               a.part + (long)S.team_cta0[team] * NS * kPartStride};
+  for (int k = S.team_case0[team]; k < S.team_case0[team + 1]; k++) {
+    const int c = S.case_list[k];
+    KspOut* out[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++) out[s] = a.out[s] + c;
+    gmres_team<NS>(a, T, S.case_lo[c], S.case_hi[c], out);
+    if (*(volatile int*)a.err) return;
   }
 }
 
@@ -420,7 +453,7 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s) {
   a.m = c.restart;
   a.maxit = c.maxit;
   a.nb = gmres_grid(c.n, w.nblocks);
-  a.chunk = (c.n + a.nb - 1) / a.nb;
+  a.sched = nullptr;
   a.rowptr = c.rowptr;
   a.col = c.col;
   a.val = c.val;

@@ -225,6 +225,27 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
                     double* x, const cycas_ksp_options* ksp, double rtol, int32_t maxit, int32_t guess_zero,
                     cycas_solve_stats* stats);
 
+/* ---- batches (no counterpart in the reference: it runs one case per job) -------------
+ * A batch context holds several independent cases in one device mesh and advances them
+ * together: every assembly kernel is one launch over all cases, and every Krylov solve is one
+ * cooperative launch whose CTAs are split into teams (one team per large case, single-CTA
+ * teams working through the small ones), each team synchronising only its own CTAs.  Each
+ * case keeps its own pressure reference cell, outlet mass balance, residuals, AMG hierarchy
+ * and Krylov state, so its iteration is the one it would have alone (up to the summation
+ * order of its inner products).  The cases must share TurModel, DensityModel, URF and gravity;
+ * the pressure preconditioner must be CYCAS_PC_AMG.  Fields of the batch are the cases'
+ * fields concatenated (cycas_batch_offsets gives each case's cell and boundary range); the
+ * other calls of a context (get/set field, profiling) work on a batch context too. */
+int cycas_batch_create(const cycas_case* const* cases, int32_t ncases, const cycas_options* opt, cycas_ctx** out);
+int cycas_batch_size(cycas_ctx* ctx, int32_t* ncases);
+/* kind 0: off[c] = first cell of case c, off[ncases] = total cells; kind 1: boundary faces */
+int cycas_batch_offsets(cycas_ctx* ctx, int32_t kind, int32_t* off);
+/* One SIMPLE-C iteration of every case: resmax[c] = vec_max of case c's localRes;
+ * its/reasons[c*8 + k] = Krylov report of solve k of case c (-1 / 0 when not run). */
+int cycas_batch_iteration(cycas_ctx* ctx, double* resmax, int32_t* its, int32_t* reasons);
+/* residual[c*10 + i] = localRes[i] of case c in the last iteration */
+int cycas_batch_residuals(cycas_ctx* ctx, double* residual);
+
 /* No counterpart in the reference: the GMRES solve of cycas_csr_solve for callers that cannot
  * allocate device memory (their HBM is pre-reserved by another allocator, or they must not add
  * the device-wide synchronisation of cudaMalloc/cudaFree between their kernels).  rowptr, col,

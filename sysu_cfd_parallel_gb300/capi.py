@@ -74,7 +74,8 @@ EXPORTS = (
     "cycas_case_params", "cycas_case_get_int", "cycas_create", "cycas_create_from_case", "cycas_destroy",
     "cycas_get_field", "cycas_set_field", "cycas_get_int", "cycas_simple_iteration", "cycas_simple_iterations",
     "cycas_run_stage", "cycas_csr_solve", "cycas_get_stream", "cycas_set_profiling", "cycas_get_profile",
-    "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels",
+    "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels", "cycas_batch_create",
+    "cycas_batch_size", "cycas_batch_offsets", "cycas_batch_iteration", "cycas_batch_residuals",
 )
 
 _lib = None
@@ -127,6 +128,11 @@ def load(build_if_missing: bool = True):
     L.cycas_get_profile.argtypes = [_P, C.POINTER(Profile)]
     L.cycas_reset_profile.argtypes = [_P]
     L.cycas_get_amg_levels.argtypes = [_P, C.c_int32, C.POINTER(C.c_int32), _P, _P]
+    L.cycas_batch_create.argtypes = [_P, C.c_int32, C.POINTER(Options), C.POINTER(_P)]
+    L.cycas_batch_size.argtypes = [_P, C.POINTER(C.c_int32)]
+    L.cycas_batch_offsets.argtypes = [_P, C.c_int32, _P]
+    L.cycas_batch_iteration.argtypes = [_P, _P, _P, _P]
+    L.cycas_batch_residuals.argtypes = [_P, _P]
     L.cycas_csr_solve_noalloc.argtypes = [C.c_int32, _P, _P, _P, _P, _P, C.POINTER(KspOptions), C.c_double,
                                           C.c_int32, C.c_int32, _P, C.POINTER(SolveStats)]
     _lib = L

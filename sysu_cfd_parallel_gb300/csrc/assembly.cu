@@ -227,7 +227,16 @@ __global__ void k_bc_velocity(int nbnd, const int* __restrict__ b_face, const in
 // compute the per-face terms in chunks and then rescale the outlet faces.
 __global__ void k_bc_outlet(int n_in, const int* __restrict__ in_list, int n_out, const int* __restrict__ out_list,
                             const int* __restrict__ b_face, const double* __restrict__ f_n,
-                            const double* __restrict__ f_area, double* BRo, double* BU, double* BV, double* BW) {
+                            const double* __restrict__ f_area, double* BRo, double* BU, double* BV, double* BW,
+                            const int* __restrict__ in0, const int* __restrict__ out0) {
+  // batches: block c takes the inlet and outlet boundaries of case c (in0/out0 ranges)
+  if (in0) {
+    in_list += in0[blockIdx.x];
+    n_in = in0[blockIdx.x + 1] - in0[blockIdx.x];
+    out_list += out0[blockIdx.x];
+    n_out = out0[blockIdx.x + 1] - out0[blockIdx.x];
+    if (n_out == 0) return;
+  }
   __shared__ double term[kThreads], aterm[kThreads];
   __shared__ double s_min, s_mout, s_aout;
   if (threadIdx.x == 0) s_min = s_mout = s_aout = 0.0;
@@ -640,6 +649,38 @@ __global__ void k_correct_cells(int ncel, const double* __restrict__ c_vol, cons
   }
 }
 
+// the same correction for a batch: block b takes rows [blk_lo[b], blk_hi[b]) of one case, whose
+// reference cell is case_pref[blk_case[b]]; red[b] receives the block's residual
+__global__ void k_correct_cells_batch(const int* __restrict__ blk_lo, const int* __restrict__ blk_hi,
+                                      const int* __restrict__ blk_case, const int* __restrict__ case_pref,
+                                      const double* __restrict__ c_vol, const double* __restrict__ dp,
+                                      const double* __restrict__ Apr, const double* __restrict__ dPdX, double urf_p,
+                                      double* __restrict__ P, double* __restrict__ U, double* __restrict__ V,
+                                      double* __restrict__ W, double* __restrict__ red) {
+  __shared__ double wsum[kThreads / 32];
+  const int i = blk_lo[blockIdx.x] + threadIdx.x;
+  double r = 0.0;
+  if (i < blk_hi[blockIdx.x]) {
+    double ref = dp[case_pref[blk_case[blockIdx.x]]];
+    double d = dp[i] - ref;
+    double vol = c_vol[i];
+    r = fabs(dp[i] - ref) * vol;
+    P[i] += urf_p * d;
+    double coef = vol * Apr[i];
+    U[i] -= coef * dPdX[3 * (long)i];
+    V[i] -= coef * dPdX[3 * (long)i + 1];
+    W[i] -= coef * dPdX[3 * (long)i + 2];
+  }
+  for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = r;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < kThreads / 32; q++) s += wsum[q];
+    red[blockIdx.x] = s;
+  }
+}
+
 // CorrectRUFace2, constant density (navier_pressure.cpp:235-278)
 __global__ void k_correct_ruface(int nfac, const int* __restrict__ f_c1, const int* __restrict__ f_c2,
                                  const int* __restrict__ f_bnd, const double* __restrict__ f_n,
@@ -917,14 +958,15 @@ void launch_geometry(const DevMesh& m, int* d_err, cudaStream_t s) {
 }
 
 void launch_bc_velocity(const DevMesh& m, const DevFields& f, int density_model, bool set_pressure,
-                        cudaStream_t s) {
+                        cudaStream_t s, const DevBatch* b) {
   if (m.nbnd > 0)
     ++g_launch_count, k_bc_velocity<<<blocks_for(m.nbnd), kThreads, 0, s>>>(m.nbnd, m.b_face, m.b_type, m.f_c1, m.f_n, m.f_area, f.R,
                                                           f.U, f.V, f.W, f.P, f.BRo, f.BU, f.BV, f.BW, f.BPre,
                                                           set_pressure ? 1 : 0);
   if (density_model == 0 && m.n_outlet > 0)
-    ++g_launch_count, k_bc_outlet<<<1, kThreads, 0, s>>>(m.n_inlet, m.inlet_list, m.n_outlet, m.outlet_list, m.b_face, m.f_n,
-                                       m.f_area, f.BRo, f.BU, f.BV, f.BW);
+    ++g_launch_count, k_bc_outlet<<<b ? b->ncases : 1, kThreads, 0, s>>>(
+                          m.n_inlet, m.inlet_list, m.n_outlet, m.outlet_list, m.b_face, m.f_n, m.f_area, f.BRo, f.BU,
+                          f.BV, f.BW, b ? b->in0 : nullptr, b ? b->out0 : nullptr);
 }
 
 void launch_bc_deltap(const DevMesh& m, const DevFields& f, cudaStream_t s) {
@@ -1016,7 +1058,13 @@ void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s) {
 }
 
 void launch_correct_cells(const DevMesh& m, const DevFields& f, int cell_pref, double urf_p, double* red,
-                          cudaStream_t s) {
+                          cudaStream_t s, const DevBatch* b) {
+  if (b) {
+    ++g_launch_count, k_correct_cells_batch<<<b->nblk, kThreads, 0, s>>>(b->blk_lo, b->blk_hi, b->blk_case,
+                                                                          b->case_pref, m.c_vol, f.dp, f.Apr, f.dPdX,
+                                                                          urf_p, f.P, f.U, f.V, f.W, red);
+    return;
+  }
   ++g_launch_count, k_correct_cells<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.dp, f.Apr, f.dPdX, cell_pref, urf_p,
                                                           f.P, f.U, f.V, f.W, red);
 }

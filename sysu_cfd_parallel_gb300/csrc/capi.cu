@@ -105,6 +105,18 @@ struct cycas_ctx {
   std::vector<int> amg_sizes;  // rows per AMG level (fine to coarse)
   std::vector<int> amg_nnz;    // stored entries per AMG level
   std::vector<int> case_lo, case_hi;  // row ranges of the independent cases (one for a context)
+  // batch contexts: independent cases concatenated in one union mesh
+  bool is_batch = false;
+  int ncases = 1;
+  DevBatch batch;
+  std::vector<int> bnd0;              // [ncases + 1] boundary ranges of the cases
+  BatchSchedule* d_sched = nullptr;   // teams of the Krylov launches
+  int sched_grid = 0, nteams = 0;
+  unsigned* team_bar = nullptr;       // [2 * nteams]
+  KspOut* bksp = nullptr;             // [8][ncases] per-case Krylov reports
+  std::vector<double> h_res;          // [ncases][10]
+  std::vector<KspOut> h_ksp;          // [8][ncases]
+  const DevBatch* bptr() const { return is_batch ? &batch : nullptr; }
 
   template <class T>
   T* alloc(long n) {
@@ -466,8 +478,25 @@ void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const d
   c.solve_sys[slot] = sys;
   g.out = &c.st->ksp[slot];
   g.err = &c.st->err;
-  CK(cudaMemsetAsync(c.kw.bar, 0, 2 * sizeof(unsigned), c.stream));
   if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot][0], c.stream));
+  if (c.is_batch) {
+    CK(cudaMemsetAsync(c.team_bar, 0, 2 * sizeof(unsigned) * c.nteams, c.stream));
+    KrylovWork w = c.kw;
+    w.bar = c.team_bar;
+    KspOut* outs = c.bksp + (long)slot * c.ncases;
+    if (k.pc == CYCAS_PC_AMG) {
+      launch_amg_setup_values(c.amg, c.stream);
+      CK(launch_cg_amg(g, c.amg, w, c.d_sched, c.sched_grid, outs, c.stream));
+    } else {
+      require(k.type != CYCAS_KSP_CG, "batches solve CG with the AMG preconditioner only");
+      CK(launch_gmres_batch(&g, 1, w, c.d_sched, c.sched_grid, &outs, c.stream));
+    }
+    if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot][1], c.stream));
+    ++g_launch_count;
+    c.prof.krylov_launches[sys]++;
+    return;
+  }
+  CK(cudaMemsetAsync(c.kw.bar, 0, 2 * sizeof(unsigned), c.stream));
   if (k.pc == CYCAS_PC_AMG) {
     launch_amg_setup_values(c.amg, c.stream);
     CK(launch_cg_amg(g, c.amg, c.kw, nullptr, gmres_grid(g.n, c.kw.nblocks), g.out, c.stream));
@@ -487,6 +516,7 @@ void solve_velocity(cycas_ctx& c) {
   require(c.nsolve + 3 <= 8, "too many solves in one iteration");
   const KspConf& k = c.ksp[CYCAS_SYS_VELOCITY];
   if (k.type == CYCAS_KSP_CG || k.pc == CYCAS_PC_AMG) {  // non-default methods: one solve at a time
+    require(!c.is_batch, "batches solve the momentum equations with GMRES");
     solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bu, c.f.U, false);
     solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bv, c.f.V, false);
     solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bw, c.f.W, false);
@@ -513,9 +543,18 @@ void solve_velocity(cycas_ctx& c) {
     g[q].out = &c.st->ksp[slot];
     g[q].err = &c.st->err;
   }
-  CK(cudaMemsetAsync(c.kw.bar, 0, 2 * sizeof(unsigned), c.stream));
   if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot0][0], c.stream));
-  CK(launch_gmres_multi(g, 3, c.kw, c.stream));
+  if (c.is_batch) {
+    CK(cudaMemsetAsync(c.team_bar, 0, 2 * sizeof(unsigned) * c.nteams, c.stream));
+    KrylovWork w = c.kw;
+    w.bar = c.team_bar;
+    KspOut* outs[3];
+    for (int q = 0; q < 3; q++) outs[q] = c.bksp + (long)(slot0 + q) * c.ncases;
+    CK(launch_gmres_batch(g, 3, w, c.d_sched, c.sched_grid, outs, c.stream));
+  } else {
+    CK(cudaMemsetAsync(c.kw.bar, 0, 2 * sizeof(unsigned), c.stream));
+    CK(launch_gmres_multi(g, 3, c.kw, c.stream));
+  }
   if (c.profiling) {
     CK(cudaEventRecord(c.ev_solve[slot0][1], c.stream));
     // the two other slots share the launch: zero-length intervals
@@ -529,7 +568,7 @@ void solve_velocity(cycas_ctx& c) {
 }
 
 void bc_velocity(cycas_ctx& c, bool with_pressure) {
-  launch_bc_velocity(c.m, c.f, c.density, with_pressure, c.stream);
+  launch_bc_velocity(c.m, c.f, c.density, with_pressure, c.stream, c.bptr());
 }
 
 void grad_uvwp(cycas_ctx& c) {
@@ -554,12 +593,12 @@ void build_velocity(cycas_ctx& c) {
 void calculate_velocity(cycas_ctx& c) {
   build_velocity(c);
   solve_velocity(c);
-  launch_residual_uvw(c.m, c.f, c.red, c.st, c.stream);
+  launch_residual_uvw(c.m, c.f, c.red, c.st, c.stream, c.bptr());
 }
 
 void correct_cells(cycas_ctx& c) {
-  launch_correct_cells(c.m, c.f, c.cell_pref, c.urf[3], c.red, c.stream);
-  launch_finalize_residual(c.red, (c.m.ncel + 255) / 256, 3, c.st, c.stream);
+  launch_correct_cells(c.m, c.f, c.cell_pref, c.urf[3], c.red, c.stream, c.bptr());
+  launch_finalize_residual(c.red, c.is_batch ? c.batch.nblk : (c.m.ncel + 255) / 256, 3, c.st, c.stream, c.bptr());
 }
 
 // CalculatePressure (navier_pressure.cpp:9-97)
@@ -592,6 +631,10 @@ void update_keps(cycas_ctx& c) {
 
 void begin_iteration(cycas_ctx& c) {
   CK(cudaMemsetAsync(c.st, 0, sizeof(DevStatus), c.stream));
+  if (c.is_batch) {
+    CK(cudaMemsetAsync(c.batch.res, 0, sizeof(double) * 10 * c.ncases, c.stream));
+    CK(cudaMemsetAsync(c.bksp, 0, sizeof(KspOut) * 8 * c.ncases, c.stream));
+  }
   c.nsolve = 0;
   c.iter_open = true;
   if (c.profiling) CK(cudaEventRecord(c.ev_iter[0], c.stream));
@@ -696,6 +739,294 @@ void set_field(cycas_ctx& c, const char* name, const double* src, long n) {
   auto p = lookup(c, name);
   require(p.second == n, std::string("size mismatch for ") + name);
   CK(cudaMemcpyAsync(p.first, src, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+}
+
+// ---------------------------------------------------------------- batches
+// Concatenates independent cases into one mesh.  Cells, boundaries and vertices are appended
+// case by case; faces are renumbered so that the boundary faces of all cases come first (in
+// case order) followed by all interior faces (in case order).  Each case keeps the reference's
+// own numbering properties: boundary b is face b, and the faces of every cell keep their
+// relative order.
+struct UnionMesh {
+  HostCase h;                // topology + InitFlowField arrays of the union
+  std::vector<int> cell0, bnd0;
+};
+
+UnionMesh build_union(const std::vector<const HostCase*>& hs) {
+  UnionMesh u;
+  HostCase& U = u.h;
+  const int nc = (int)hs.size();
+  int NC = 0, NB = 0, NF = 0, NV = 0;
+  for (const HostCase* h : hs) {
+    NC += h->ncel;
+    NB += h->nbnd;
+    NF += h->nfac;
+    NV += h->nvrt;
+  }
+  U.ncel = NC;
+  U.nbnd = NB;
+  U.nfac = NF;
+  U.nvrt = NV;
+  U.face_cell1.resize(NF);
+  U.face_cell2.resize(NF);
+  U.face_bnd.resize(NF);
+  U.face_vertices.resize(4L * NF);
+  u.cell0.assign(nc + 1, 0);
+  u.bnd0.assign(nc + 1, 0);
+  int c0 = 0, b0 = 0, i0 = NB, v0 = 0;
+  for (int k = 0; k < nc; k++) {
+    const HostCase& h = *hs[k];
+    u.cell0[k] = c0;
+    u.bnd0[k] = b0;
+    for (int f = 0; f < h.nfac; f++)
+      if ((h.face_bnd[f] >= 0) != (f < h.nbnd) || (f < h.nbnd && h.face_bnd[f] != f))
+        throw StatusError(CYCAS_ERR_MESH, "a batched case does not number its boundary faces first");
+    auto fmap = [&](int f) { return f < h.nbnd ? b0 + f : i0 + (f - h.nbnd); };
+    for (int f = 0; f < h.nfac; f++) {
+      const int g = fmap(f);
+      U.face_cell1[g] = h.face_cell1[f] + c0;
+      U.face_cell2[g] = h.face_cell2[f] >= 0 ? h.face_cell2[f] + c0 : h.face_cell2[f];
+      U.face_bnd[g] = h.face_bnd[f] >= 0 ? h.face_bnd[f] + b0 : h.face_bnd[f];
+      for (int q = 0; q < 4; q++) U.face_vertices[4L * g + q] = h.face_vertices[4L * f + q] + v0;
+    }
+    for (int i = 0; i < h.ncel; i++) {
+      U.cell_nface.push_back(h.cell_nface[i]);
+      U.cell_rid.push_back(h.cell_rid[i]);
+      for (int j = 0; j < 6; j++) {
+        const int f = h.cell_face[6L * i + j], cc = h.cell_cell[6L * i + j];
+        U.cell_face.push_back(f >= 0 ? fmap(f) : f);
+        U.cell_cell.push_back(cc >= 0 ? cc + c0 : cc);
+      }
+      for (int q = 0; q < 8; q++) U.cell_vertices.push_back(h.cell_vertices[8L * i + q] + v0);
+    }
+    for (int b = 0; b < h.nbnd; b++) {
+      U.bnd_face.push_back(fmap(h.bnd_face[b]));
+      U.bnd_type.push_back(h.bnd_type[b]);
+      U.bnd_rid.push_back(h.bnd_rid[b]);
+    }
+    U.vert.insert(U.vert.end(), h.vert.begin(), h.vert.end());
+    auto cat = [](std::vector<double>& dst, const std::vector<double>& src) { dst.insert(dst.end(), src.begin(), src.end()); };
+    cat(U.U, h.U);
+    cat(U.V, h.V);
+    cat(U.W, h.W);
+    cat(U.P, h.P);
+    cat(U.R, h.R);
+    cat(U.T, h.T);
+    cat(U.VisLam, h.VisLam);
+    cat(U.VisTur, h.VisTur);
+    cat(U.TE, h.TE);
+    cat(U.ED, h.ED);
+    cat(U.BU, h.BU);
+    cat(U.BV, h.BV);
+    cat(U.BW, h.BW);
+    cat(U.BRo, h.BRo);
+    cat(U.BTem, h.BTem);
+    cat(U.BTE, h.BTE);
+    cat(U.BED, h.BED);
+    c0 += h.ncel;
+    b0 += h.nbnd;
+    i0 += h.nfac - h.nbnd;
+    v0 += h.nvrt;
+  }
+  u.cell0[nc] = c0;
+  u.bnd0[nc] = b0;
+  return u;
+}
+
+// Teams for the batched Krylov launches: a case with at least N/G rows (N rows in all, G CTAs)
+// gets a team of about rows*G/N CTAs of its own; the smaller cases are spread over single-CTA
+// teams, largest first onto the least loaded team.
+void build_schedule(cycas_ctx& c) {
+  const int nc = c.ncases, G = c.kw.nblocks;
+  long N = 0;
+  for (int k = 0; k < nc; k++) N += c.case_hi[k] - c.case_lo[k];
+  const double target = (double)N / G;
+  std::vector<int> k_of(nc, 0);
+  int used = 0;
+  bool small = false;
+  for (int k = 0; k < nc; k++) {
+    const int rows = c.case_hi[k] - c.case_lo[k];
+    if (rows >= target) {
+      k_of[k] = std::max(1, (int)(rows / target));
+      used += k_of[k];
+    } else {
+      small = true;
+    }
+  }
+  const int avail = G - (small ? 1 : 0);
+  while (used > avail) {
+    int big = -1;
+    for (int k = 0; k < nc; k++)
+      if (k_of[k] > 1 && (big < 0 || k_of[k] > k_of[big])) big = k;
+    if (big < 0) {  // every big case has one CTA: the smallest of them joins the small cases
+      int sm = -1;
+      for (int k = 0; k < nc; k++)
+        if (k_of[k] == 1 && (sm < 0 || c.case_hi[k] - c.case_lo[k] < c.case_hi[sm] - c.case_lo[sm])) sm = k;
+      k_of[sm] = 0;
+      small = true;
+    } else {
+      k_of[big]--;
+    }
+    used--;
+  }
+  std::vector<int> cta_team, cta_rank, team_size, team_cta0, team_case0, case_list;
+  auto add_team = [&](int size, const std::vector<int>& cases) {
+    const int t = (int)team_size.size();
+    team_cta0.push_back((int)cta_team.size());
+    team_size.push_back(size);
+    team_case0.push_back((int)case_list.size());
+    case_list.insert(case_list.end(), cases.begin(), cases.end());
+    for (int r = 0; r < size; r++) {
+      cta_team.push_back(t);
+      cta_rank.push_back(r);
+    }
+  };
+  for (int k = 0; k < nc; k++)
+    if (k_of[k] > 0) add_team(k_of[k], {k});
+  const int rest = G - (int)cta_team.size();
+  if (small) {
+    require(rest >= 1, "batch schedule left no CTA for the small cases");
+    std::vector<int> order;
+    for (int k = 0; k < nc; k++)
+      if (k_of[k] == 0) order.push_back(k);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return c.case_hi[a] - c.case_lo[a] > c.case_hi[b] - c.case_lo[b];
+    });
+    const int nteam = std::min(rest, (int)order.size());
+    std::vector<long> load(nteam, 0);
+    std::vector<std::vector<int>> lists(nteam);
+    for (int k : order) {
+      int t = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      lists[t].push_back(k);
+      load[t] += c.case_hi[k] - c.case_lo[k];
+    }
+    for (int t = 0; t < nteam; t++) {
+      std::sort(lists[t].begin(), lists[t].end());
+      add_team(1, lists[t]);
+    }
+  }
+  team_case0.push_back((int)case_list.size());
+  c.nteams = (int)team_size.size();
+  c.sched_grid = (int)cta_team.size();
+  BatchSchedule hs;
+  hs.cta_team = c.upload(cta_team.data(), (long)cta_team.size());
+  hs.cta_rank = c.upload(cta_rank.data(), (long)cta_rank.size());
+  hs.team_size = c.upload(team_size.data(), (long)team_size.size());
+  hs.team_cta0 = c.upload(team_cta0.data(), (long)team_cta0.size());
+  hs.team_case0 = c.upload(team_case0.data(), (long)team_case0.size());
+  hs.case_list = c.upload(case_list.data(), (long)case_list.size());
+  hs.case_lo = c.upload(c.case_lo.data(), nc);
+  hs.case_hi = c.upload(c.case_hi.data(), nc);
+  c.d_sched = c.upload(&hs, 1);
+  c.team_bar = c.alloc<unsigned>(2L * c.nteams);
+}
+
+// per-case metadata of a batch context
+void setup_batch(cycas_ctx& c, const UnionMesh& u, const std::vector<const HostCase*>& hs) {
+  const int nc = (int)hs.size();
+  c.is_batch = true;
+  c.ncases = nc;
+  c.case_lo.assign(u.cell0.begin(), u.cell0.end() - 1);
+  c.case_hi.assign(u.cell0.begin() + 1, u.cell0.end());
+  c.bnd0 = u.bnd0;
+  std::vector<int> blk_lo, blk_hi, blk_case, case_blk0, pref, in0(nc + 1, 0), out0(nc + 1, 0);
+  for (int k = 0; k < nc; k++) {
+    case_blk0.push_back((int)blk_lo.size());
+    for (int r = c.case_lo[k]; r < c.case_hi[k]; r += 256) {
+      blk_lo.push_back(r);
+      blk_hi.push_back(std::min(r + 256, c.case_hi[k]));
+      blk_case.push_back(k);
+    }
+    const int pr = hs[k]->cell_pressure_ref;
+    require(pr >= 0 && pr < hs[k]->ncel, "PressureRef cell out of range");
+    pref.push_back(c.case_lo[k] + pr);
+    in0[k + 1] = in0[k];
+    out0[k + 1] = out0[k];
+    for (int b = 0; b < hs[k]->nbnd; b++) {
+      if (hs[k]->bnd_type[b] == 2) in0[k + 1]++;
+      if (hs[k]->bnd_type[b] == 3) out0[k + 1]++;
+    }
+  }
+  case_blk0.push_back((int)blk_lo.size());
+  DevBatch& b = c.batch;
+  b.ncases = nc;
+  b.nblk = (int)blk_lo.size();
+  b.blk_lo = c.upload(blk_lo.data(), b.nblk);
+  b.blk_hi = c.upload(blk_hi.data(), b.nblk);
+  b.blk_case = c.upload(blk_case.data(), b.nblk);
+  b.case_blk0 = c.upload(case_blk0.data(), nc + 1);
+  b.case_pref = c.upload(pref.data(), nc);
+  b.in0 = c.upload(in0.data(), nc + 1);
+  b.out0 = c.upload(out0.data(), nc + 1);
+  b.res = c.alloc<double>(10L * nc);
+  c.red = c.alloc<double>(3L * b.nblk);
+  c.bksp = c.alloc<KspOut>(8L * nc);
+  c.h_res.assign(10L * nc, 0.0);
+  c.h_ksp.assign(8L * nc, KspOut{});
+  build_schedule(c);
+}
+
+// reads the per-case residuals and Krylov reports of a batch iteration
+int finish_batch(cycas_ctx& c, double* resmax, int32_t* its, int32_t* reasons) {
+  CK(cudaGetLastError());
+  const bool timed = c.profiling && c.iter_open;
+  c.iter_open = false;
+  if (timed) CK(cudaEventRecord(c.ev_iter[1], c.stream));
+  CK(cudaMemcpyAsync(c.st_host, c.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(c.h_res.data(), c.batch.res, sizeof(double) * 10 * c.ncases, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(c.h_ksp.data(), c.bksp, sizeof(KspOut) * 8 * c.ncases, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  const int nc = c.ncases;
+  if (timed) {
+    float total = 0.f, ksum = 0.f;
+    CK(cudaEventElapsedTime(&total, c.ev_iter[0], c.ev_iter[1]));
+    for (int k = 0; k < c.nsolve; k++) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, c.ev_solve[k][0], c.ev_solve[k][1]));
+      c.prof.krylov_ms[c.solve_sys[k]] += ms;
+      ksum += ms;
+    }
+    c.prof.assembly_ms += total - ksum;
+  }
+  int failed = -1, nan = 0;
+  for (int k = 0; k < c.nsolve; k++) {
+    int mx = 0;
+    for (int q = 0; q < nc; q++) {
+      const KspOut& o = c.h_ksp[(long)k * nc + q];
+      mx = std::max(mx, o.its);
+      if (o.reason < 0 && failed < 0) failed = q;
+      if (o.reason == CYCAS_KSP_DIVERGED_NANORINF) nan = 1;
+    }
+    c.prof.krylov_iters[c.solve_sys[k]] += mx;
+  }
+  for (int q = 0; q < nc; q++) {
+    double mx = 0.0;
+    for (int i = 0; i < 10; i++) mx = mx > c.h_res[10L * q + i] ? mx : c.h_res[10L * q + i];
+    if (resmax) resmax[q] = mx;
+    for (int k = 0; k < 8; k++) {
+      const bool on = k < c.nsolve;
+      if (its) its[8L * q + k] = on ? c.h_ksp[(long)k * nc + q].its : -1;
+      if (reasons) reasons[8L * q + k] = on ? c.h_ksp[(long)k * nc + q].reason : 0;
+    }
+  }
+  const DevStatus& s = *c.st_host;
+  if (s.err & 1) {
+    g_last_error = "a device-side barrier timed out; the solve was abandoned";
+    return CYCAS_ERR_TIMEOUT;
+  }
+  if (s.err & 4) {
+    g_last_error = "reverse flow get out of inlet (scalar transport); the reference stops here";
+    return CYCAS_ERR_INVALID;
+  }
+  if (nan) {
+    g_last_error = "NaN or Inf residual norm in a Krylov solve";
+    return CYCAS_NAN_DETECTED;
+  }
+  if (failed >= 0) {
+    g_last_error = "a Krylov solve of case " + std::to_string(failed) + " did not converge";
+    return CYCAS_NOT_CONVERGED;
+  }
+  return CYCAS_OK;
 }
 
 }  // namespace
@@ -1080,4 +1411,108 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
   });
 }
 
+int cycas_batch_create(const cycas_case* const* cases, int32_t ncases, const cycas_options* opt, cycas_ctx** out) {
+  return guard([&]() -> int {
+    require(cases && out && ncases >= 1, "bad argument");
+    *out = nullptr;
+    std::vector<const HostCase*> hs;
+    for (int k = 0; k < ncases; k++) {
+      require(cases[k] != nullptr, "null case");
+      hs.push_back(&cases[k]->hc);
+    }
+    const HostCase& h0 = *hs[0];
+    for (const HostCase* h : hs) {
+      bool same = h->turb_model == h0.turb_model && h->density_model == h0.density_model;
+      for (int i = 0; i < 8; i++) same = same && h->urf[i] == h0.urf[i];
+      for (int i = 0; i < 3; i++) same = same && h->gravity[i] == h0.gravity[i];
+      require(same, "batched cases must share the turbulence model, density model, relaxation and gravity");
+    }
+    UnionMesh u = build_union(hs);
+    cycas_mesh_view v = view_of(u.h);
+    cycas_params p;
+    std::memset(&p, 0, sizeof p);
+    p.turb_model = h0.turb_model;
+    p.density_model = h0.density_model;
+    p.cell_pressure_ref = h0.cell_pressure_ref;
+    for (int i = 0; i < 8; i++) p.urf[i] = h0.urf[i];
+    for (int i = 0; i < 3; i++) p.gravity[i] = h0.gravity[i];
+    cycas_ctx* c = new cycas_ctx();
+    try {
+      init_ctx(*c, &p, opt);
+      require(c->ksp[CYCAS_SYS_PRESSURE].pc == CYCAS_PC_AMG, "batches need the AMG pressure preconditioner");
+      build_device_mesh(*c, v);
+      alloc_fields(*c);
+      alloc_krylov(*c);
+      setup_batch(*c, u, hs);
+      setup_amg(*c);
+      const HostCase& h = u.h;
+      const long n = h.ncel, nb = h.nbnd;
+      set_field(*c, "U", h.U.data(), n);
+      set_field(*c, "V", h.V.data(), n);
+      set_field(*c, "W", h.W.data(), n);
+      set_field(*c, "P", h.P.data(), n);
+      set_field(*c, "R", h.R.data(), n);
+      set_field(*c, "T", h.T.data(), n);
+      set_field(*c, "VisLam", h.VisLam.data(), n);
+      set_field(*c, "VisTur", h.VisTur.data(), n);
+      set_field(*c, "TE", h.TE.data(), n);
+      set_field(*c, "ED", h.ED.data(), n);
+      set_field(*c, "BU", h.BU.data(), nb);
+      set_field(*c, "BV", h.BV.data(), nb);
+      set_field(*c, "BW", h.BW.data(), nb);
+      set_field(*c, "BRo", h.BRo.data(), nb);
+      set_field(*c, "BTem", h.BTem.data(), nb);
+      set_field(*c, "BTE", h.BTE.data(), nb);
+      set_field(*c, "BED", h.BED.data(), nb);
+      CK(cudaStreamSynchronize(c->stream));
+    } catch (...) {
+      delete c;
+      throw;
+    }
+    *out = c;
+    return CYCAS_OK;
+  });
+}
+
+int cycas_batch_size(cycas_ctx* c, int32_t* ncases) {
+  return guard([&]() -> int {
+    require(c && ncases, "null argument");
+    *ncases = c->is_batch ? c->ncases : 1;
+    return CYCAS_OK;
+  });
+}
+
+int cycas_batch_offsets(cycas_ctx* c, int32_t kind, int32_t* off) {
+  return guard([&]() -> int {
+    require(c && off, "null argument");
+    require(kind == 0 || kind == 1, "kind must be 0 (cells) or 1 (boundary faces)");
+    if (!c->is_batch) {
+      off[0] = 0;
+      off[1] = kind == 0 ? c->m.ncel : c->m.nbnd;
+      return CYCAS_OK;
+    }
+    for (int k = 0; k < c->ncases; k++) off[k] = kind == 0 ? c->case_lo[k] : c->bnd0[k];
+    off[c->ncases] = kind == 0 ? c->case_hi[c->ncases - 1] : c->bnd0[c->ncases];
+    return CYCAS_OK;
+  });
+}
+
+int cycas_batch_iteration(cycas_ctx* c, double* resmax, int32_t* its, int32_t* reasons) {
+  return guard([&]() -> int {
+    require(c != nullptr && c->is_batch, "not a batch context");
+    begin_iteration(*c);
+    issue_iteration(*c);
+    return finish_batch(*c, resmax, its, reasons);
+  });
+}
+
+int cycas_batch_residuals(cycas_ctx* c, double* residual) {
+  return guard([&]() -> int {
+    require(c && residual && c->is_batch, "bad argument");
+    std::memcpy(residual, c->h_res.data(), sizeof(double) * 10 * c->ncases);
+    return CYCAS_OK;
+  });
+}
+
 }  // extern "C"
+

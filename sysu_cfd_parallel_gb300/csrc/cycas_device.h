@@ -107,8 +107,23 @@ struct KspConf {
 void launch_geometry(const DevMesh& m, int* d_err, cudaStream_t s);
 
 // boundary conditions, gradients, assembly, corrections (NS/navier_*.cpp)
+// Case metadata of a batch context (several independent cases in one union mesh).
+struct DevBatch {
+  int ncases = 0;
+  int nblk = 0;                  // case-aligned blocks of at most 256 rows
+  const int* blk_lo = nullptr;   // [nblk] first row
+  const int* blk_hi = nullptr;   // [nblk] one past the last row
+  const int* blk_case = nullptr; // [nblk] case of the block
+  const int* case_blk0 = nullptr;// [ncases + 1] blocks of each case
+  const int* case_pref = nullptr;// [ncases] global pressure-reference cell
+  const int* in0 = nullptr;      // [ncases + 1] inlet boundaries of each case in inlet_list
+  const int* out0 = nullptr;     // [ncases + 1] outlet boundaries of each case in outlet_list
+  double* res = nullptr;         // [ncases][10] residuals of the iteration
+};
+
+// b: the batch metadata of a batch context, nullptr for a single case
 void launch_bc_velocity(const DevMesh& m, const DevFields& f, int density_model, bool set_pressure,
-                        cudaStream_t s);
+                        cudaStream_t s, const DevBatch* b = nullptr);
 void launch_bc_deltap(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
                      double* const* grad, cudaStream_t s);
@@ -117,7 +132,7 @@ void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, co
 void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_correct_cells(const DevMesh& m, const DevFields& f, int cell_pref, double urf_p, double* red,
-                          cudaStream_t s);
+                          cudaStream_t s, const DevBatch* b = nullptr);
 void launch_correct_ruface(const DevMesh& m, const DevFields& f, double urf_p, cudaStream_t s);
 void launch_keps_sources(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_keps_wall(const DevMesh& m, const DevFields& f, cudaStream_t s);
@@ -129,8 +144,10 @@ void launch_eps_wall_rows(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_finish_keps(const DevMesh& m, const DevFields& f, cudaStream_t s);
 
 // reductions (krylov.cu)
-void launch_residual_uvw(const DevMesh& m, const DevFields& f, double* red, DevStatus* st, cudaStream_t s);
-void launch_finalize_residual(const double* red, int nparts, int slot, DevStatus* st, cudaStream_t s);
+void launch_residual_uvw(const DevMesh& m, const DevFields& f, double* red, DevStatus* st, cudaStream_t s,
+                         const DevBatch* b = nullptr);
+void launch_finalize_residual(const double* red, int nparts, int slot, DevStatus* st, cudaStream_t s,
+                              const DevBatch* b = nullptr);
 int residual_blocks(int n);
 
 // Krylov
@@ -169,6 +186,10 @@ cudaError_t launch_gmres(const GmresCall& c, KrylovWork& w, cudaStream_t s);
 // nsys (1 or 3) systems sharing rowptr/col/val/dinv/tolerances, solved in lockstep; the
 // Krylov basis of system k starts at w.V + k*(restart+1)*w.ldv
 cudaError_t launch_gmres_multi(const GmresCall* calls, int nsys, KrylovWork& w, cudaStream_t s);
+// the same solves for every case of a batch: the teams of sched (device pointer) over `grid`
+// CTAs; system q of case c reports to outs[q][c]
+cudaError_t launch_gmres_batch(const GmresCall* calls, int nsys, KrylovWork& w, const BatchSchedule* sched, int grid,
+                               KspOut* const* outs, cudaStream_t s);
 // PETSc-style CG; needs at least four work vectors in w.V
 cudaError_t launch_cg(const GmresCall& c, KrylovWork& w, cudaStream_t s);
 

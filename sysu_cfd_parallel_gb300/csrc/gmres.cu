@@ -441,19 +441,20 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
 }
 
 template <int NS>
-cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s) {
+cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, const BatchSchedule* sched = nullptr,
+                      int grid = 0, KspOut* const* outs = nullptr) {
   GmMsArgs<NS> a;
   const GmresCall& c = calls[0];
   // workspace bounds: basis NS*(m+1) vectors, partials nb*NS*stride
-  const int nb = gmres_grid(c.n, w.nblocks);
+  const int nb = sched ? grid : gmres_grid(c.n, w.nblocks);
   if (c.restart < 1 || c.restart > kMaxRestart || (long)NS * (c.restart + 1) * w.ldv > w.v_len ||
       (long)nb * NS * kPartStride > w.part_len || w.ldv < c.n)
     return cudaErrorInvalidValue;
   a.n = c.n;
   a.m = c.restart;
   a.maxit = c.maxit;
-  a.nb = gmres_grid(c.n, w.nblocks);
-  a.sched = nullptr;
+  a.nb = nb;
+  a.sched = sched;
   a.rowptr = c.rowptr;
   a.col = c.col;
   a.val = c.val;
@@ -461,7 +462,7 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s) {
   for (int k = 0; k < NS; k++) {
     a.b[k] = calls[k].b;
     a.x[k] = calls[k].x;
-    a.out[k] = calls[k].out;
+    a.out[k] = outs ? outs[k] : calls[k].out;
   }
   a.guess_zero = c.guess_zero;
   a.V = w.V;
@@ -474,10 +475,18 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s) {
   a.dtol = 1e4;
   a.haptol = 1e-30;
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)k_gmres_ms<NS>, dim3(a.nb), dim3(kGmThreads), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)k_gmres_ms<NS>, dim3(nb), dim3(kGmThreads), args, 0, s);
 }
 
 }  // namespace
+
+cudaError_t launch_gmres_batch(const GmresCall* calls, int nsys, KrylovWork& w, const BatchSchedule* sched, int grid,
+                               KspOut* const* outs, cudaStream_t s) {
+  if (!sched || grid < 1 || grid > w.nblocks) return cudaErrorInvalidValue;
+  if (nsys == 1) return launch_ms<1>(calls, w, s, sched, grid, outs);
+  if (nsys == 3) return launch_ms<3>(calls, w, s, sched, grid, outs);
+  return cudaErrorInvalidValue;
+}
 
 cudaError_t launch_gmres_multi(const GmresCall* calls, int nsys, KrylovWork& w, cudaStream_t s) {
   if (nsys == 1) return launch_ms<1>(calls, w, s);

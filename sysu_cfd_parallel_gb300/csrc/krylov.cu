@@ -237,6 +237,53 @@ __global__ void k_finalize(const double* __restrict__ red, int nparts, int nslot
   }
 }
 
+// per-case residual sums for batches: block b covers rows [blk_lo[b], blk_hi[b]) of one case
+__global__ void k_residual_uvw_batch(const int* __restrict__ blk_lo, const int* __restrict__ blk_hi, int nblk,
+                                     const double* __restrict__ vol, const double* __restrict__ old, long n,
+                                     const double* __restrict__ U, const double* __restrict__ V,
+                                     const double* __restrict__ W, double* __restrict__ red) {
+  __shared__ double sw[kRedThreads / 32][3];
+  double r[3] = {0.0, 0.0, 0.0};
+  const int i = blk_lo[blockIdx.x] + threadIdx.x;
+  if (i < blk_hi[blockIdx.x]) {
+    double v = vol[i];
+    r[0] = fabs(old[i] - U[i]) * v;
+    r[1] = fabs(old[n + i] - V[i]) * v;
+    r[2] = fabs(old[2 * n + i] - W[i]) * v;
+  }
+  for (int k = 0; k < 3; k++) {
+    double t = r[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5][k] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double s = 0.0;
+    for (int w = 0; w < kRedThreads / 32; w++) s += sw[w][threadIdx.x];
+    red[(long)threadIdx.x * nblk + blockIdx.x] = s;
+  }
+}
+
+// case c (block c) adds the partials of its blocks [case_blk0[c], case_blk0[c+1]) to res[c][slot]
+__global__ void k_finalize_cases(const double* __restrict__ red, int nblk, const int* __restrict__ case_blk0,
+                                 int nslots, int slot0, double* __restrict__ res) {
+  __shared__ double sw[kRedThreads / 32];
+  const int b0 = case_blk0[blockIdx.x], b1 = case_blk0[blockIdx.x + 1];
+  for (int q = 0; q < nslots; q++) {
+    double s = 0.0;
+    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += red[(long)q * nblk + i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kRedThreads / 32; w++) t += sw[w];
+      res[(long)blockIdx.x * 10 + slot0 + q] += t;
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 int residual_blocks(int n) {
@@ -244,14 +291,26 @@ int residual_blocks(int n) {
   return b < 1 ? 1 : b;
 }
 
-void launch_residual_uvw(const DevMesh& m, const DevFields& f, double* red, DevStatus* st, cudaStream_t s) {
+void launch_residual_uvw(const DevMesh& m, const DevFields& f, double* red, DevStatus* st, cudaStream_t s,
+                         const DevBatch* b) {
+  if (b) {
+    ++g_launch_count, k_residual_uvw_batch<<<b->nblk, kRedThreads, 0, s>>>(b->blk_lo, b->blk_hi, b->nblk, m.c_vol,
+                                                                            f.old, m.ncel, f.U, f.V, f.W, red);
+    ++g_launch_count, k_finalize_cases<<<b->ncases, kRedThreads, 0, s>>>(red, b->nblk, b->case_blk0, 3, 0, b->res);
+    return;
+  }
   int nb = residual_blocks(m.ncel);
   if (nb > 1024) nb = 1024;
   ++g_launch_count, k_residual_uvw<<<nb, kRedThreads, 0, s>>>(m.ncel, m.c_vol, f.old, f.U, f.V, f.W, red);
   ++g_launch_count, k_finalize<<<1, kRedThreads, 0, s>>>(red, nb, 3, 0, st);
 }
 
-void launch_finalize_residual(const double* red, int nparts, int slot, DevStatus* st, cudaStream_t s) {
+void launch_finalize_residual(const double* red, int nparts, int slot, DevStatus* st, cudaStream_t s,
+                              const DevBatch* b) {
+  if (b) {
+    ++g_launch_count, k_finalize_cases<<<b->ncases, kRedThreads, 0, s>>>(red, b->nblk, b->case_blk0, 1, slot, b->res);
+    return;
+  }
   ++g_launch_count, k_finalize<<<1, kRedThreads, 0, s>>>(red, nparts, 1, slot, st);
 }
 

@@ -228,3 +228,72 @@ def csr_solve(rowptr, col, val, b, x0=None, pc=capi.PC_JACOBI, restart=30, rtol=
     if rc not in (capi.CYCAS_OK, capi.CYCAS_NOT_CONVERGED):
         capi.check(rc)
     return x, st.its, st.reason, st.rnorm
+
+
+class _UnionSizes:
+    """Sizes of the concatenated mesh of a batch (what NavierStokesSolver reads off a Case)."""
+
+    def __init__(self, cases):
+        self.ncel = sum(c.ncel for c in cases)
+        self.nfac = sum(c.nfac for c in cases)
+        self.nbnd = sum(c.nbnd for c in cases)
+        self.nnz = sum(c.nnz for c in cases)
+        self.turb_model = cases[0].turb_model
+        self.max_step = max(c.max_step for c in cases)
+        self.residual_steady = cases[0].residual_steady
+
+
+def batch_options(pc=capi.PC_JACOBI, restart=30, device=0) -> capi.Options:
+    """The reference's Krylov methods and tolerances, AMG for the pressure correction (required
+    by batches)."""
+    o = capi.default_options(pc=pc, restart=restart, device=device)
+    o.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
+    return o
+
+
+class Batch(NavierStokesSolver):
+    """Independent cases advanced together on one device (cycas_batch_*).
+
+    Fields are the cases' fields concatenated; ``case_field(name, c)`` slices one case.
+    """
+
+    def __init__(self, cases, options: capi.Options | None = None):
+        L = capi.load()
+        self.cases = list(cases)
+        self.case = _UnionSizes(self.cases)
+        self.options = options or batch_options()
+        handles = (C.c_void_p * len(self.cases))(*[c._h.value for c in self.cases])
+        h = C.c_void_p()
+        capi.check(L.cycas_batch_create(handles, len(self.cases), C.byref(self.options), C.byref(h)))
+        self._h = h
+        n = C.c_int32()
+        capi.check(L.cycas_batch_size(h, C.byref(n)))
+        self.ncases = n.value
+        self.cell0 = np.zeros(self.ncases + 1, dtype=np.int32)
+        self.bnd0 = np.zeros(self.ncases + 1, dtype=np.int32)
+        capi.check(L.cycas_batch_offsets(h, 0, capi.ptr(self.cell0)))
+        capi.check(L.cycas_batch_offsets(h, 1, capi.ptr(self.bnd0)))
+        self.step = 0
+        self.last_stats = None
+
+    def case_field(self, name: str, c: int) -> np.ndarray:
+        a = self.get(name)
+        bnd = {"BRo", "BU", "BV", "BW", "BPre", "BTE", "BED", "BTem", "bnd_distance"}
+        off = self.bnd0 if name in bnd else self.cell0
+        return a[off[c]:off[c + 1]].copy()
+
+    def iterate(self, n: int):
+        """n iterations of every case; returns dict(resmax [n, ncases], ksp_its [n, ncases, 8],
+        ksp_reason [n, ncases, 8], residual [n, ncases, 10])."""
+        L = capi.load()
+        nc = self.ncases
+        rm = np.zeros((n, nc))
+        its = np.zeros((n, nc, 8), dtype=np.int32)
+        rs = np.zeros((n, nc, 8), dtype=np.int32)
+        res = np.zeros((n, nc, 10))
+        for k in range(n):
+            rc = L.cycas_batch_iteration(self._h, capi.ptr(rm[k]), capi.ptr(its[k]), capi.ptr(rs[k]))
+            capi.check(rc)
+            capi.check(L.cycas_batch_residuals(self._h, capi.ptr(res[k])))
+            self.step += 1
+        return {"resmax": rm, "ksp_its": its, "ksp_reason": rs, "residual": res}

@@ -141,7 +141,13 @@ typedef struct {
 typedef struct {
   cycas_ksp_options ksp[3]; /* indexed by CYCAS_SYS_* */
   int32_t device;           /* CUDA device ordinal */
-  int32_t reserved[7];
+  int32_t mixed;            /* 0: FP64 Krylov (the reference's arithmetic).  1: mixed precision
+                               for the GMRES systems (momentum, k, epsilon): FP32 Arnoldi cycles
+                               wrapped in FP64 iterative refinement, each cycle ending at a
+                               relative drop of inner_rtol, convergence tested on the FP64 true
+                               residual to the system's rtol (no counterpart in the reference) */
+  double inner_rtol;        /* <= 0: 1e-4 */
+  int32_t reserved[4];
 } cycas_options;
 
 /* fills defaults: the reference's Krylov methods (GMRES(30); CG for pressure), Jacobi,

@@ -51,7 +51,8 @@ class KspOptions(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("ksp", KspOptions * 3), ("device", C.c_int32), ("reserved", C.c_int32 * 7)]
+    _fields_ = [("ksp", KspOptions * 3), ("device", C.c_int32), ("mixed", C.c_int32), ("inner_rtol", C.c_double),
+                ("reserved", C.c_int32 * 4)]
 
 
 class IterStats(C.Structure):

@@ -105,6 +105,11 @@ struct cycas_ctx {
   std::vector<int> amg_sizes;  // rows per AMG level (fine to coarse)
   std::vector<int> amg_nnz;    // stored entries per AMG level
   std::vector<int> case_lo, case_hi;  // row ranges of the independent cases (one for a context)
+  // mixed precision (GMRES systems): FP32 copies of the system being solved
+  bool mixed = false;
+  double inner_rtol = 1e-4;
+  float* val32 = nullptr;   // [nnz]
+  float* dinv32 = nullptr;  // [ncel]
   // batch contexts: independent cases concatenated in one union mesh
   bool is_batch = false;
   int ncases = 1;
@@ -387,6 +392,10 @@ void alloc_krylov(cycas_ctx& c) {
   w.part_len = 3L * w.nblocks * kGmresPartStride;
   w.part = c.alloc<double>(w.part_len);
   w.bar = c.alloc<unsigned>(2);
+  if (c.mixed) {
+    c.val32 = c.alloc<float>(c.m.nnz);
+    c.dinv32 = c.alloc<float>(c.m.ncel);
+  }
   c.red_parts = std::min(residual_blocks(c.m.ncel), 1024);
   int cells_blocks = (c.m.ncel + 255) / 256;
   c.red = c.alloc<double>(3L * std::max(c.red_parts, cells_blocks));
@@ -452,6 +461,8 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
     c.ksp[s].rtol = k.rtol > 0 ? k.rtol : kRefRtol[s];
     c.ksp[s].maxit = k.maxit > 0 ? k.maxit : kRefMaxit[s];
   }
+  c.mixed = o->mixed != 0;
+  c.inner_rtol = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
   c.d_geom_err = c.alloc<int>(1);
   c.st = c.alloc<DevStatus>(1);
   CK(cudaMallocHost((void**)&c.st_host, sizeof(DevStatus)));
@@ -459,6 +470,15 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
 }
 
 // ---------------------------------------------------------------- iteration schedule
+// mixed precision: FP32 copies of the operator and Jacobi inverse for the Arnoldi cycles
+void set_mixed(cycas_ctx& c, GmresCall& g) {
+  launch_to_float(g.val, c.val32, c.m.nnz, c.stream);
+  if (g.dinv) launch_to_float(g.dinv, c.dinv32, c.m.ncel, c.stream);
+  g.val32 = c.val32;
+  g.dinv32 = g.dinv ? c.dinv32 : nullptr;
+  g.inner_rtol = c.inner_rtol;
+}
+
 void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const double* b, double* x, bool guess_zero) {
   require(c.nsolve < 8, "too many solves in one iteration");
   const KspConf& k = c.ksp[sys];
@@ -478,6 +498,8 @@ void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const d
   c.solve_sys[slot] = sys;
   g.out = &c.st->ksp[slot];
   g.err = &c.st->err;
+  const bool gm = k.pc != CYCAS_PC_AMG && k.type != CYCAS_KSP_CG;
+  if (c.mixed && gm) set_mixed(c, g);
   if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot][0], c.stream));
   if (c.is_batch) {
     CK(cudaMemsetAsync(c.team_bar, 0, 2 * sizeof(unsigned) * c.nteams, c.stream));
@@ -542,6 +564,14 @@ void solve_velocity(cycas_ctx& c) {
     c.solve_sys[slot] = CYCAS_SYS_VELOCITY;
     g[q].out = &c.st->ksp[slot];
     g[q].err = &c.st->err;
+  }
+  if (c.mixed) {
+    set_mixed(c, g[0]);
+    for (int q = 1; q < 3; q++) {
+      g[q].val32 = g[0].val32;
+      g[q].dinv32 = g[0].dinv32;
+      g[q].inner_rtol = g[0].inner_rtol;
+    }
   }
   if (c.profiling) CK(cudaEventRecord(c.ev_solve[slot0][0], c.stream));
   if (c.is_batch) {

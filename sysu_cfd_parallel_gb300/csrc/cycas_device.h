@@ -149,6 +149,7 @@ void launch_residual_uvw(const DevMesh& m, const DevFields& f, double* red, DevS
 void launch_finalize_residual(const double* red, int nparts, int slot, DevStatus* st, cudaStream_t s,
                               const DevBatch* b = nullptr);
 int residual_blocks(int n);
+void launch_to_float(const double* src, float* dst, long n, cudaStream_t s);
 
 // Krylov
 // Batched Krylov solves: the CTAs of one cooperative launch are split into teams; each team
@@ -178,6 +179,13 @@ struct GmresCall {
   int restart;
   KspOut* out;
   int* err;
+  // mixed precision (GMRES only): FP32 copies of the matrix values and of the Jacobi inverse
+  // set => the Arnoldi cycles run in FP32 and each ends when its own residual estimate has
+  // dropped by inner_rtol; every restart recomputes the true residual in FP64 (iterative
+  // refinement), and convergence is tested on that FP64 residual
+  const float* val32 = nullptr;
+  const float* dinv32 = nullptr;
+  double inner_rtol = 0.0;
 };
 int gmres_grid(int n, int device_blocks);
 int gmres_max_blocks(int device);

@@ -14,6 +14,14 @@
 // system, and each system keeps its own Krylov basis, Hessenberg matrix and control state,
 // so its arithmetic is the same as a solve on its own.
 //
+// Mixed precision (T = float): the Krylov basis, the Arnoldi SpMV (FP32 matrix copy), the
+// Jacobi scaling, the Gram-Schmidt products and the basis updates are FP32, while the
+// Hessenberg matrix, the Givens least squares, the cross-CTA sums, x, and every restart's true
+// residual z = D^-1 (b - A x) are FP64.  A cycle ends when its residual estimate has dropped
+// by inner_rtol (or at the restart length); the restart that follows is the refinement step,
+// and the outer convergence test is made on its FP64 residual only.  GB300 runs FP64 at 1/64
+// of the FP32 rate, so this moves the arithmetic-bound part of every Arnoldi step to FP32.
+//
 // Each step is two grid barriers.  Per system the step is one of
 //   START / RESTART: (x update of the finished cycle) | residual z = D^-1 (b - A x) | beta, tests
 //   ARNOLDI:         w = D^-1 A v_j, partial <w, v_i> | h, w -= sum h_i v_i, ||w|| | Givens, tests
@@ -32,17 +40,20 @@ using namespace kry;
 
 enum Mode { M_START = 0, M_ARNOLDI = 1, M_RESTART = 2, M_FINAL = 3, M_DONE = 4 };
 
-template <int NS>
+template <int NS, class T>
 struct GmMsArgs {
   int n, m, maxit, nb;
   const int* __restrict__ rowptr;
   const int* __restrict__ col;
   const double* __restrict__ val;
   const double* __restrict__ dinv;
+  const T* __restrict__ valT;   // matrix and Jacobi inverse in the Arnoldi precision
+  const T* __restrict__ dinvT;
+  double inner_rtol;            // > 0: cycles end at this relative drop (refinement)
   const double* b[NS];
   double* x[NS];
   int guess_zero;
-  double* V;   // system s, vector q at (s*(m+1)+q)*ldv
+  T* V;   // system s, vector q at (s*(m+1)+q)*ldv
   long ldv;
   double* part;  // [nb][NS][kPartStride]
   unsigned* bar;
@@ -63,27 +74,27 @@ struct Team {
 
 // sum over CSR row r of val[k] * vec_s[col[k]] for every system s in mask, column order; W
 // entries per batch (a tetrahedral row, 5 entries, is one batch for a single system)
-template <int NS>
+template <int NS, class T>
 __device__ __forceinline__ void row_gather_ms(const int* __restrict__ rowptr, const int* __restrict__ col,
-                                              const double* __restrict__ val, int r, const double* const* vec,
-                                              unsigned mask, double* out) {
+                                              const T* __restrict__ val, int r, const T* const* vec,
+                                              unsigned mask, T* out) {
   constexpr int W = NS == 1 ? 5 : 3;
   const int k0 = __ldg(rowptr + r), k1 = __ldg(rowptr + r + 1);
 #pragma unroll
-  for (int s = 0; s < NS; s++) out[s] = 0.0;
+  for (int s = 0; s < NS; s++) out[s] = T(0);
   for (int b = k0; b < k1; b += W) {
     int c[W];
-    double v[W], xv[NS][W];
+    T v[W], xv[NS][W];
 #pragma unroll
     for (int q = 0; q < W; q++) {
       const bool ok = b + q < k1;
       c[q] = ok ? __ldg(col + b + q) : 0;
-      v[q] = ok ? __ldg(val + b + q) : 0.0;
+      v[q] = ok ? __ldg(val + b + q) : T(0);
     }
 #pragma unroll
     for (int s = 0; s < NS; s++)
 #pragma unroll
-      for (int q = 0; q < W; q++) xv[s][q] = ((mask >> s) & 1u) && b + q < k1 ? ldcg(vec[s] + c[q]) : 0.0;
+      for (int q = 0; q < W; q++) xv[s][q] = ((mask >> s) & 1u) && b + q < k1 ? __ldcg(vec[s] + c[q]) : T(0);
 #pragma unroll
     for (int s = 0; s < NS; s++)
 #pragma unroll
@@ -92,8 +103,22 @@ __device__ __forceinline__ void row_gather_ms(const int* __restrict__ rowptr, co
   }
 }
 
-template <int NS>
-__device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T, int lo, int hi, KspOut* const* out) {
+// w + sum_{q < cnt} coef[q] * V[q*ldv + r] in the basis precision, ascending q
+template <class T>
+__device__ __forceinline__ T basis_axpy(T w, const T* V, long ldv, int r, const double* coef, int cnt) {
+  for (int q0 = 0; q0 < cnt; q0 += 8) {
+    T v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = (q0 + k < cnt) ? __ldcg(V + (long)(q0 + k) * ldv + r) : T(0);
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (q0 + k < cnt) w = fma((T)coef[q0 + k], v[k], w);
+  }
+  return w;
+}
+
+template <int NS, class Tv>
+__device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team& T, int lo, int hi, KspOut* const* out) {
   constexpr int M = kMaxRestart;
   constexpr int MAXP = NS * (M + 1);
   __shared__ double s_hh[NS][(M + 1) * M];
@@ -101,7 +126,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
   __shared__ double s_scale[NS][M + 1], s_h[NS][M + 1], s_coef[NS][M + 1];
   __shared__ double s_pair[MAXP > 32 ? MAXP : 32];
   __shared__ double s_red[kDotGroup], s_warp[kGmWarps * kDotGroup];
-  __shared__ double s_rnorm0[NS], s_ttol[NS], s_rnorm[NS];
+  __shared__ double s_rnorm0[NS], s_ttol[NS], s_rnorm[NS], s_cyc[NS];
   __shared__ int s_mode[NS], s_it[NS], s_its[NS], s_reason[NS], s_first[NS], s_nupd[NS];
   __shared__ unsigned char s_ps[MAXP], s_pq[MAXP];
   __shared__ int s_npairs;
@@ -113,6 +138,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
   const int kNorm = M + 1, kInit = M + 2;
   auto part_of = [&](int blk, int s) { return T.part + ((long)blk * NS + s) * kPartStride; };
   auto Vv = [&](int s, int q) { return a.V + ((long)s * (m + 1) + q) * a.ldv; };
+  const bool mixed = a.inner_rtol > 0.0;
 
   if (tid < NS) {
     s_mode[tid] = M_START;
@@ -143,8 +169,8 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
       if (mode[s] == M_RESTART || mode[s] == M_FINAL) {
         const int cnt = s_nupd[s];
         for (int r = r0 + tid; r < r1; r += kGmThreads) {
-          double t = vec_axpy(0.0, Vv(s, 0), a.ldv, r, s_coef[s], cnt);
-          a.x[s][r] += t;
+          const Tv t = basis_axpy<Tv>(Tv(0), Vv(s, 0), a.ldv, r, s_coef[s], cnt);
+          a.x[s][r] += (double)t;
         }
       } else if (mode[s] == M_START && a.guess_zero) {
         for (int r = r0 + tid; r < r1; r += kGmThreads) a.x[s][r] = 0.0;
@@ -152,17 +178,17 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
       if (mode[s] == M_ARNOLDI) arn |= 1u << s;
     }
     if (arn) {
-      const double* vj[NS];
-      double sj[NS];
+      const Tv* vj[NS];
+      Tv sj[NS];
 #pragma unroll
       for (int s = 0; s < NS; s++) {
         vj[s] = Vv(s, itv[s]);
-        sj[s] = s_scale[s][itv[s]];
+        sj[s] = (Tv)s_scale[s][itv[s]];
       }
       for (int r = r0 + tid; r < r1; r += kGmThreads) {
-        double acc[NS];
-        row_gather_ms<NS>(a.rowptr, a.col, a.val, r, vj, arn, acc);
-        const double d = a.dinv ? a.dinv[r] : 1.0;
+        Tv acc[NS];
+        row_gather_ms<NS, Tv>(a.rowptr, a.col, a.valT, r, vj, arn, acc);
+        const Tv d = a.dinvT ? a.dinvT[r] : Tv(1);
 #pragma unroll
         for (int s = 0; s < NS; s++)
           if ((arn >> s) & 1u) Vv(s, itv[s] + 1)[r] = (acc[s] * sj[s]) * d;
@@ -187,21 +213,22 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
         const int sub = wid % wpp;
         if (wid / wpp >= (kGmWarps / wpp)) break;
         const int s = s_ps[pb], q = s_pq[pb];
-        const double* vq = Vv(s, q);
-        const double* w = Vv(s, itv[s] + 1);
+        const Tv* vq = Vv(s, q);
+        const Tv* w = Vv(s, itv[s] + 1);
         const int step = wpp * 32;
-        double acc = 0.0;
+        Tv acct = Tv(0);
         for (int base = r0 + sub * 32 + lane; base < r1; base += 8 * step) {
-          double wv[8], vv[8];
+          Tv wv[8], vv[8];
 #pragma unroll
           for (int k = 0; k < 8; k++) {
             const int r = base + k * step;
-            wv[k] = r < r1 ? ldcg(w + r) : 0.0;
-            vv[k] = r < r1 ? ldcg(vq + r) : 0.0;
+            wv[k] = r < r1 ? __ldcg(w + r) : Tv(0);
+            vv[k] = r < r1 ? __ldcg(vq + r) : Tv(0);
           }
 #pragma unroll
-          for (int k = 0; k < 8; k++) acc += wv[k] * vv[k];
+          for (int k = 0; k < 8; k++) acct += wv[k] * vv[k];
         }
+        double acc = (double)acct;  // lanes, warps and CTAs reduce in FP64
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) s_pair[pb * wpp + sub < (MAXP > 32 ? MAXP : 32) ? pb * wpp + sub : 0] = acc;
       }
@@ -236,16 +263,17 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
       __syncthreads();
       double nrm[NS];
 #pragma unroll
-      for (int s = 0; s < NS; s++) nrm[s] = 0.0;
-#pragma unroll
       for (int s = 0; s < NS; s++) {
+        nrm[s] = 0.0;
         if (!((arn >> s) & 1u)) continue;
-        double* w = Vv(s, itv[s] + 1);
+        Tv* w = Vv(s, itv[s] + 1);
+        Tv nt = Tv(0);
         for (int r = r0 + tid; r < r1; r += kGmThreads) {
-          const double wr = vec_axpy(ldcg(w + r), Vv(s, 0), a.ldv, r, s_coef[s], itv[s] + 1);
+          const Tv wr = basis_axpy<Tv>(__ldcg(w + r), Vv(s, 0), a.ldv, r, s_coef[s], itv[s] + 1);
           w[r] = wr;
-          nrm[s] += wr * wr;
+          nt += wr * wr;
         }
+        nrm[s] = (double)nt;
       }
       block_reduce<NS>(nrm, s_warp, s_red);
       if (tid < NS && ((arn >> tid) & 1u)) part_of(T.rank, tid)[kNorm] = s_red[tid];
@@ -265,7 +293,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
             if (mode[s] == M_START) gmask &= ~(1u << s);  // x = 0: residual is b
         }
         double ax[NS];
-        if (gmask) row_gather_ms<NS>(a.rowptr, a.col, a.val, r, xs, gmask, ax);
+        if (gmask) row_gather_ms<NS, double>(a.rowptr, a.col, a.val, r, xs, gmask, ax);
         const double d = a.dinv ? a.dinv[r] : 1.0;
 #pragma unroll
         for (int s = 0; s < NS; s++) {
@@ -273,7 +301,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
           const double br = a.b[s][r];
           const double t = ((gmask >> s) & 1u) ? br - ax[s] : br;
           const double z = t * d;
-          Vv(s, 0)[r] = z;
+          Vv(s, 0)[r] = (Tv)z;
           acc[2 * s] += z * z;
           if (mode[s] == M_START && !a.guess_zero) {
             const double zb = br * d;
@@ -328,17 +356,22 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
           } else {
             res = 0.0;
           }
+          bool inner_done = false;
           if (!brk) {
             used = it + 1;
             s_its[s]++;
             s_rnorm[s] = res;
             if (isnan(res) || isinf(res)) rs = -9;
-            else if (res <= s_ttol[s]) rs = res < a.abstol ? 3 : 2;
+            else if (mixed) {
+              // refinement: the cycle ends at its own relative drop; convergence is decided on
+              // the FP64 residual of the restart that follows
+              inner_done = res <= fmax(s_ttol[s], a.inner_rtol * s_cyc[s]) || hapend;
+            } else if (res <= s_ttol[s]) rs = res < a.abstol ? 3 : 2;
             else if (res >= a.dtol * s_rnorm0[s]) rs = -4;
-            if (hapend && !rs) rs = -5;
+            if (hapend && !rs && !mixed) rs = -5;
           }
           s_reason[s] = rs;
-          const bool end_cycle = brk || rs != 0 || used == m || s_its[s] >= a.maxit;
+          const bool end_cycle = brk || rs != 0 || inner_done || used == m || s_its[s] >= a.maxit;
           if (!end_cycle) {
             s_it[s] = used;
           } else {
@@ -363,9 +396,13 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
               }
             }
             s_nupd[s] = nup;
-            if (s_reason[s] == 0 && s_its[s] >= a.maxit) s_reason[s] = -3;
-            const bool finished = s_reason[s] != 0;
-            s_mode[s] = finished ? (nup > 0 ? M_FINAL : M_DONE) : (nup > 0 ? M_RESTART : M_START);
+            if (mixed && s_reason[s] == 0 && nup > 0) {
+              s_mode[s] = M_RESTART;  // x update and the FP64 residual decide
+            } else {
+              if (s_reason[s] == 0 && s_its[s] >= a.maxit) s_reason[s] = -3;
+              const bool finished = s_reason[s] != 0;
+              s_mode[s] = finished ? (nup > 0 ? M_FINAL : M_DONE) : (nup > 0 ? M_RESTART : M_START);
+            }
             s_it[s] = 0;
           }
         }
@@ -391,6 +428,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
           s_grs[s][0] = beta;
           s_scale[s][0] = 1.0 / beta;
           s_rnorm[s] = beta;
+          s_cyc[s] = beta;
           int rs = 0;
           if (beta == 0.0) {
             rs = 3;
@@ -399,6 +437,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
             if (isnan(beta) || isinf(beta)) rs = -9;
             else if (beta <= s_ttol[s]) rs = beta < a.abstol ? 3 : 2;
             else if (beta >= a.dtol * s_rnorm0[s]) rs = -4;
+            else if (mixed && s_its[s] >= a.maxit) rs = -3;
           }
           s_reason[s] = rs;
           s_first[s] = 0;
@@ -419,11 +458,11 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS>& a, const Team& T,
   __syncthreads();
 }
 
-template <int NS>
-__global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
+template <int NS, class Tv>
+__global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS, Tv> a) {
   if (!a.sched) {
     const Team T{(int)blockIdx.x, a.nb, a.bar, a.part};
-    gmres_team<NS>(a, T, 0, a.n, a.out);
+    gmres_team<NS, Tv>(a, T, 0, a.n, a.out);
     return;
   }
   const BatchSchedule& S = *a.sched;
@@ -435,15 +474,15 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS> a) {
     KspOut* out[NS];
 #pragma unroll
     for (int s = 0; s < NS; s++) out[s] = a.out[s] + c;
-    gmres_team<NS>(a, T, S.case_lo[c], S.case_hi[c], out);
+    gmres_team<NS, Tv>(a, T, S.case_lo[c], S.case_hi[c], out);
     if (*(volatile int*)a.err) return;
   }
 }
 
-template <int NS>
+template <int NS, class Tv>
 cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, const BatchSchedule* sched = nullptr,
                       int grid = 0, KspOut* const* outs = nullptr) {
-  GmMsArgs<NS> a;
+  GmMsArgs<NS, Tv> a;
   const GmresCall& c = calls[0];
   // workspace bounds: basis NS*(m+1) vectors, partials nb*NS*stride
   const int nb = sched ? grid : gmres_grid(c.n, w.nblocks);
@@ -459,13 +498,23 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
   a.col = c.col;
   a.val = c.val;
   a.dinv = c.dinv;
+  if constexpr (sizeof(Tv) == sizeof(double)) {
+    a.valT = c.val;
+    a.dinvT = c.dinv;
+    a.inner_rtol = 0.0;
+  } else {
+    if (!c.val32 || (c.dinv && !c.dinv32) || !(c.inner_rtol > 0.0)) return cudaErrorInvalidValue;
+    a.valT = c.val32;
+    a.dinvT = c.dinv ? c.dinv32 : nullptr;
+    a.inner_rtol = c.inner_rtol;
+  }
   for (int k = 0; k < NS; k++) {
     a.b[k] = calls[k].b;
     a.x[k] = calls[k].x;
     a.out[k] = outs ? outs[k] : calls[k].out;
   }
   a.guess_zero = c.guess_zero;
-  a.V = w.V;
+  a.V = reinterpret_cast<Tv*>(w.V);
   a.ldv = w.ldv;
   a.part = w.part;
   a.bar = w.bar;
@@ -475,7 +524,7 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
   a.dtol = 1e4;
   a.haptol = 1e-30;
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)k_gmres_ms<NS>, dim3(nb), dim3(kGmThreads), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)k_gmres_ms<NS, Tv>, dim3(nb), dim3(kGmThreads), args, 0, s);
 }
 
 }  // namespace
@@ -483,14 +532,16 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
 cudaError_t launch_gmres_batch(const GmresCall* calls, int nsys, KrylovWork& w, const BatchSchedule* sched, int grid,
                                KspOut* const* outs, cudaStream_t s) {
   if (!sched || grid < 1 || grid > w.nblocks) return cudaErrorInvalidValue;
-  if (nsys == 1) return launch_ms<1>(calls, w, s, sched, grid, outs);
-  if (nsys == 3) return launch_ms<3>(calls, w, s, sched, grid, outs);
+  const bool mx = calls[0].val32 != nullptr;
+  if (nsys == 1) return mx ? launch_ms<1, float>(calls, w, s, sched, grid, outs) : launch_ms<1, double>(calls, w, s, sched, grid, outs);
+  if (nsys == 3) return mx ? launch_ms<3, float>(calls, w, s, sched, grid, outs) : launch_ms<3, double>(calls, w, s, sched, grid, outs);
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_gmres_multi(const GmresCall* calls, int nsys, KrylovWork& w, cudaStream_t s) {
-  if (nsys == 1) return launch_ms<1>(calls, w, s);
-  if (nsys == 3) return launch_ms<3>(calls, w, s);
+  const bool mx = calls[0].val32 != nullptr;
+  if (nsys == 1) return mx ? launch_ms<1, float>(calls, w, s) : launch_ms<1, double>(calls, w, s);
+  if (nsys == 3) return mx ? launch_ms<3, float>(calls, w, s) : launch_ms<3, double>(calls, w, s);
   return cudaErrorInvalidValue;
 }
 

@@ -284,7 +284,16 @@ __global__ void k_finalize_cases(const double* __restrict__ red, int nblk, const
   }
 }
 
+__global__ void k_to_float(long n, const double* __restrict__ src, float* __restrict__ dst) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+
 }  // namespace
+
+void launch_to_float(const double* src, float* dst, long n, cudaStream_t s) {
+  if (n > 0) ++g_launch_count, k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, src, dst);
+}
 
 int residual_blocks(int n) {
   int b = (n + kRedThreads - 1) / kRedThreads;

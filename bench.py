@@ -54,6 +54,98 @@ def make_case() -> str:
     return param
 
 
+BATCH_SAMPLE = 32      # cavities of the batched sample (the 256-case workload is --workload batch256)
+BATCH_SEED = 4
+
+
+def batch_cases(count: int) -> list:
+    """Lid-driven cavities drawn as in the batched workload: n^3 hexes with n uniform in
+    {8..40}, node jitter 0.1h, Re log-uniform in [10, 1000] (mu = 1/Re), lid speed 1; cached
+    on disk like the channel."""
+    import numpy as np
+    from sysu_cfd_parallel_gb300 import meshgen
+    rng = np.random.default_rng(BATCH_SEED)
+    ns = rng.integers(8, 41, size=count)
+    res = 10.0 ** rng.uniform(1.0, 3.0, size=count)
+    base = os.environ.get("CYCAS_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "cycas_bench_cases"))
+    out = []
+    for k in range(count):
+        d = os.path.join(base, "cavity_batch_s%d_%03d_n%d" % (BATCH_SEED, k, ns[k]))
+        param = os.path.join(d, "param.in")
+        if not os.path.exists(os.path.join(d, "complete")):
+            meshgen.write_case(d, "cavity", n=int(ns[k]), jitter=0.1, seed=1000 + k, steps=2000,
+                               mu=float(1.0 / res[k]))
+            open(os.path.join(d, "complete"), "w").close()
+        out.append(param)
+    return out
+
+
+def timed_iterations(solver, steps: int, stream):
+    """CUDA-event time of `steps` iterations on the solver's stream (ms)."""
+    import torch
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.iterate(steps)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def measure_mixed(param, local, warmup, steps, ref_fields, fp64_ms):
+    """The same workload with mixed-precision GMRES: throughput and the field error against the
+    FP64 run after the same iterations."""
+    import numpy as np
+    import torch
+    from sysu_cfd_parallel_gb300 import capi
+    from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
+    case = Case(param)
+    opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+    opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
+    opt.mixed = 1
+    s = NavierStokesSolver(case, opt)
+    stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
+    if warmup > 0:
+        s.iterate(warmup)
+    ms = timed_iterations(s, steps, stream)
+    err = {}
+    for nm, ref in ref_fields.items():
+        err[nm] = float(np.linalg.norm(s.get(nm) - ref) / np.linalg.norm(ref))
+    s.close()
+    return {"value": case.ncel * steps / (ms / 1e3), "ms_per_step": ms / steps,
+            "speedup_vs_fp64": fp64_ms / ms,
+            "krylov": "GMRES systems: FP32 Arnoldi cycles (inner rtol 1e-4) in FP64 iterative refinement",
+            "field_rel_l2_vs_fp64": err}
+
+
+def measure_batched(local, count, steps, mixed=False):
+    """The batched sample against the same cases run one after another as single contexts."""
+    import torch
+    from sysu_cfd_parallel_gb300.solver import Batch, Case, NavierStokesSolver, batch_options
+    params = batch_cases(count)
+    opt = batch_options(device=local)
+    opt.mixed = 1 if mixed else 0
+    cases = [Case(p) for p in params]
+    cells = sum(c.ncel for c in cases)
+    b = Batch(cases, opt)
+    stream = torch.cuda.ExternalStream(b.stream_handle(), device=local)
+    b.iterate(2)
+    ms_b = timed_iterations(b, steps, stream)
+    b.close()
+    ms_s = 0.0
+    for c in cases:
+        s = NavierStokesSolver(c, opt)
+        st = torch.cuda.ExternalStream(s.stream_handle(), device=local)
+        s.iterate(2)
+        ms_s += timed_iterations(s, steps, st)
+        s.close()
+    return {"cases": count, "cells": cells, "value": cells * steps / (ms_b / 1e3), "ms_per_step": ms_b / steps,
+            "one_case_at_a_time": {"value": cells * steps / (ms_s / 1e3), "ms_per_step": ms_s / steps},
+            "speedup_vs_one_at_a_time": ms_s / ms_b, "mixed": bool(mixed),
+            "workload": f"{count} cavities n~U{{8..40}}^3 hexes, jitter 0.1h, Re~logU[10,1000], FP64 SIMPLE-C"}
+
+
 # ---------------------------------------------------------------- clocks
 class Clocks:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -310,6 +402,7 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     prof = s.profile()
+    ref_fields = {nm: s.get(nm) for nm in (["U", "V", "W", "P"] + (["TE", "ED"] if turb else []))}
     ms = reduce_max(ms, device="cuda")
     value = whole_job_rate(n, args.steps, world, ms)
 
@@ -364,6 +457,11 @@ def run_gpu(args):
     e2e_ms = reduce_max(e2e_ms, device="cuda")
     e2e_value = whole_job_rate(n, e2e_steps, world, e2e_ms)
 
+    mixed = batched = None
+    if not args.no_variants:
+        mixed = measure_mixed(param, local, args.warmup, args.steps, ref_fields, ms)
+        batched = measure_batched(local, BATCH_SAMPLE, args.steps)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt, setup, _ = cpu_sample(param, args.cpu_iters)
@@ -390,6 +488,8 @@ def run_gpu(args):
                          "frac": achieved / peak, "traffic": traffic,
                          "share_of_step": sys_ms[dom] / ms},
             "cpu_baseline": cpu,
+            "mixed": mixed,
+            "batched": batched,
             "gpu_launches": int(prof["kernel_launches"]),
             "profile": {"krylov_ms": sys_ms, "assembly_ms": prof["assembly_ms"],
                         "krylov_iters": prof["krylov_iters"]},
@@ -409,6 +509,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision and batched lines")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -252,6 +252,45 @@ int cycas_batch_iteration(cycas_ctx* ctx, double* resmax, int32_t* its, int32_t*
 /* residual[c*10 + i] = localRes[i] of case c in the last iteration */
 int cycas_batch_residuals(cycas_ctx* ctx, double* residual);
 
+/* Moves the state of case sc of batch src (fields, boundary values, face fluxes) into case dc
+ * of batch dst; the two cases must be the same mesh.  Used when a batch is re-formed. */
+int cycas_batch_copy_case(cycas_ctx* dst, int32_t dc, cycas_ctx* src, int32_t sc);
+/* the slice of a per-cell or per-boundary field belonging to case k of a batch */
+int cycas_batch_case_field(cycas_ctx* ctx, int32_t k, const char* name, double* dst, int64_t n);
+
+/* ---- serving (no counterpart in the reference) ------------------------------------------
+ * A request loop with continuous batching: submitted cases queue in arrival order; each step
+ * admits queued cases while the estimated device footprint of the active ones stays within
+ * the HBM budget, re-forms the batch of every physics class (turbulence model) whose
+ * membership changed (the state of continuing cases is moved on the device), advances every
+ * active case by one SIMPLE-C iteration, and retires each case whose residual, the reference's
+ * ResMax divided by the case's volume, is at or below the tolerance (or that reached the
+ * iteration cap).  Times are seconds of a monotonic clock (cycas_server_clock). */
+typedef struct cycas_server cycas_server;
+enum { CYCAS_REQ_CONVERGED = 1, CYCAS_REQ_FAILED = 2, CYCAS_REQ_MAX_ITERS = 3 };
+typedef struct {
+  int64_t id;
+  int32_t status;      /* CYCAS_REQ_* */
+  int32_t iterations;  /* SIMPLE-C iterations done */
+  int32_t ncel;
+  int32_t pad;
+  double t_arrival, t_admit, t_done;
+  double resmax;       /* normalised residual at retirement */
+} cycas_request_result;
+/* estimated device bytes of a case in a batch (what admission counts against the budget) */
+double cycas_footprint_estimate(const cycas_case* c);
+int cycas_server_create(const cycas_options* opt, double hbm_budget_bytes, double residual_tol, int32_t max_iters,
+                        int32_t keep_fields, cycas_server** out);
+void cycas_server_destroy(cycas_server* s);
+double cycas_server_clock(void);
+int cycas_server_submit(cycas_server* s, const char* param_path, int64_t* id);
+int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued);
+/* results of requests finished since the last poll (at most max) */
+int cycas_server_poll(cycas_server* s, cycas_request_result* out, int32_t max, int32_t* n);
+/* final U V W P TE ED of a finished request (server created with keep_fields) */
+int cycas_server_result_field(cycas_server* s, int64_t id, const char* name, double* dst, int64_t n);
+const char* cycas_server_last_error(cycas_server* s);
+
 /* No counterpart in the reference: the GMRES solve of cycas_csr_solve for callers that cannot
  * allocate device memory (their HBM is pre-reserved by another allocator, or they must not add
  * the device-wide synchronisation of cudaMalloc/cudaFree between their kernels).  rowptr, col,

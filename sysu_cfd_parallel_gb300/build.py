@@ -35,6 +35,7 @@ UNITS = [
     ("amg_setup.cpp", "cxx", []),
     ("capi.cu", "nvcc", []),
     ("noalloc.cu", "nvcc", []),
+    ("server.cpp", "cxx", []),
 ]
 
 

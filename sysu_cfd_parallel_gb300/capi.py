@@ -55,6 +55,15 @@ class Options(C.Structure):
                 ("reserved", C.c_int32 * 4)]
 
 
+class RequestResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("iterations", C.c_int32), ("ncel", C.c_int32),
+                ("pad", C.c_int32), ("t_arrival", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("resmax", C.c_double)]
+
+
+REQ_CONVERGED, REQ_FAILED, REQ_MAX_ITERS = 1, 2, 3
+
+
 class IterStats(C.Structure):
     _fields_ = [("its", C.c_int32 * 8), ("reason", C.c_int32 * 8), ("rnorm", C.c_double * 8),
                 ("nsolves", C.c_int32), ("failed_solve", C.c_int32)]
@@ -77,6 +86,9 @@ EXPORTS = (
     "cycas_run_stage", "cycas_csr_solve", "cycas_get_stream", "cycas_set_profiling", "cycas_get_profile",
     "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels", "cycas_batch_create",
     "cycas_batch_size", "cycas_batch_offsets", "cycas_batch_iteration", "cycas_batch_residuals",
+    "cycas_batch_copy_case", "cycas_batch_case_field", "cycas_server_create", "cycas_server_destroy",
+    "cycas_server_clock", "cycas_server_submit", "cycas_server_step", "cycas_server_poll",
+    "cycas_server_result_field", "cycas_server_last_error", "cycas_footprint_estimate",
 )
 
 _lib = None
@@ -134,6 +146,21 @@ def load(build_if_missing: bool = True):
     L.cycas_batch_offsets.argtypes = [_P, C.c_int32, _P]
     L.cycas_batch_iteration.argtypes = [_P, _P, _P, _P]
     L.cycas_batch_residuals.argtypes = [_P, _P]
+    L.cycas_batch_copy_case.argtypes = [_P, C.c_int32, _P, C.c_int32]
+    L.cycas_batch_case_field.argtypes = [_P, C.c_int32, C.c_char_p, _P, C.c_int64]
+    L.cycas_server_create.argtypes = [C.POINTER(Options), C.c_double, C.c_double, C.c_int32, C.c_int32, C.POINTER(_P)]
+    L.cycas_server_destroy.argtypes = [_P]
+    L.cycas_server_destroy.restype = None
+    L.cycas_server_clock.argtypes = []
+    L.cycas_server_clock.restype = C.c_double
+    L.cycas_server_submit.argtypes = [_P, C.c_char_p, C.POINTER(C.c_int64)]
+    L.cycas_server_step.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.cycas_server_poll.argtypes = [_P, C.POINTER(RequestResult), C.c_int32, C.POINTER(C.c_int32)]
+    L.cycas_server_result_field.argtypes = [_P, C.c_int64, C.c_char_p, _P, C.c_int64]
+    L.cycas_footprint_estimate.argtypes = [_P]
+    L.cycas_footprint_estimate.restype = C.c_double
+    L.cycas_server_last_error.argtypes = [_P]
+    L.cycas_server_last_error.restype = C.c_char_p
     L.cycas_csr_solve_noalloc.argtypes = [C.c_int32, _P, _P, _P, _P, _P, C.POINTER(KspOptions), C.c_double,
                                           C.c_int32, C.c_int32, _P, C.POINTER(SolveStats)]
     _lib = L

@@ -115,6 +115,7 @@ struct cycas_ctx {
   int ncases = 1;
   DevBatch batch;
   std::vector<int> bnd0;              // [ncases + 1] boundary ranges of the cases
+  std::vector<int> iface0;            // [ncases + 1] interior-face ranges of the cases
   BatchSchedule* d_sched = nullptr;   // teams of the Krylov launches
   int sched_grid = 0, nteams = 0;
   unsigned* team_bar = nullptr;       // [2 * nteams]
@@ -779,7 +780,7 @@ void set_field(cycas_ctx& c, const char* name, const double* src, long n) {
 // relative order.
 struct UnionMesh {
   HostCase h;                // topology + InitFlowField arrays of the union
-  std::vector<int> cell0, bnd0;
+  std::vector<int> cell0, bnd0, iface0;  // iface0: first interior face of each case (union index)
 };
 
 UnionMesh build_union(const std::vector<const HostCase*>& hs) {
@@ -803,11 +804,13 @@ UnionMesh build_union(const std::vector<const HostCase*>& hs) {
   U.face_vertices.resize(4L * NF);
   u.cell0.assign(nc + 1, 0);
   u.bnd0.assign(nc + 1, 0);
+  u.iface0.assign(nc + 1, 0);
   int c0 = 0, b0 = 0, i0 = NB, v0 = 0;
   for (int k = 0; k < nc; k++) {
     const HostCase& h = *hs[k];
     u.cell0[k] = c0;
     u.bnd0[k] = b0;
+    u.iface0[k] = i0;
     for (int f = 0; f < h.nfac; f++)
       if ((h.face_bnd[f] >= 0) != (f < h.nbnd) || (f < h.nbnd && h.face_bnd[f] != f))
         throw StatusError(CYCAS_ERR_MESH, "a batched case does not number its boundary faces first");
@@ -860,6 +863,7 @@ UnionMesh build_union(const std::vector<const HostCase*>& hs) {
   }
   u.cell0[nc] = c0;
   u.bnd0[nc] = b0;
+  u.iface0[nc] = i0;
   return u;
 }
 
@@ -959,6 +963,7 @@ void setup_batch(cycas_ctx& c, const UnionMesh& u, const std::vector<const HostC
   c.case_lo.assign(u.cell0.begin(), u.cell0.end() - 1);
   c.case_hi.assign(u.cell0.begin() + 1, u.cell0.end());
   c.bnd0 = u.bnd0;
+  c.iface0 = u.iface0;
   std::vector<int> blk_lo, blk_hi, blk_case, case_blk0, pref, in0(nc + 1, 0), out0(nc + 1, 0);
   for (int k = 0; k < nc; k++) {
     case_blk0.push_back((int)blk_lo.size());
@@ -1544,5 +1549,59 @@ int cycas_batch_residuals(cycas_ctx* c, double* residual) {
   });
 }
 
+int cycas_batch_copy_case(cycas_ctx* dst, int32_t dc, cycas_ctx* src, int32_t sc) {
+  return guard([&]() -> int {
+    require(dst && src && dst->is_batch && src->is_batch, "not batch contexts");
+    require(dc >= 0 && dc < dst->ncases && sc >= 0 && sc < src->ncases, "case index out of range");
+    const long nc = src->case_hi[sc] - src->case_lo[sc], nb = src->bnd0[sc + 1] - src->bnd0[sc];
+    const long ni = src->iface0[sc + 1] - src->iface0[sc];
+    require(nc == dst->case_hi[dc] - dst->case_lo[dc] && nb == dst->bnd0[dc + 1] - dst->bnd0[dc] &&
+                ni == dst->iface0[dc + 1] - dst->iface0[dc],
+            "the two cases differ in size");
+    CK(cudaStreamSynchronize(src->stream));
+    static const char* cells[] = {"U", "V", "W", "P", "R", "T", "TE", "ED", "VisLam", "VisTur", "deltaP"};
+    static const char* bnds[] = {"BU", "BV", "BW", "BRo", "BPre", "BTE", "BED", "BTem"};
+    for (const char* nm : cells) {
+      auto a = lookup(*src, nm), b = lookup(*dst, nm);
+      CK(cudaMemcpyAsync(b.first + dst->case_lo[dc], a.first + src->case_lo[sc], sizeof(double) * nc,
+                         cudaMemcpyDeviceToDevice, dst->stream));
+    }
+    for (const char* nm : bnds) {
+      auto a = lookup(*src, nm), b = lookup(*dst, nm);
+      CK(cudaMemcpyAsync(b.first + dst->bnd0[dc], a.first + src->bnd0[sc], sizeof(double) * nb,
+                         cudaMemcpyDeviceToDevice, dst->stream));
+    }
+    auto a = lookup(*src, "RUFace"), b = lookup(*dst, "RUFace");
+    CK(cudaMemcpyAsync(b.first + dst->bnd0[dc], a.first + src->bnd0[sc], sizeof(double) * nb,
+                       cudaMemcpyDeviceToDevice, dst->stream));
+    CK(cudaMemcpyAsync(b.first + dst->iface0[dc], a.first + src->iface0[sc], sizeof(double) * ni,
+                       cudaMemcpyDeviceToDevice, dst->stream));
+    CK(cudaStreamSynchronize(dst->stream));
+    return CYCAS_OK;
+  });
+}
+
+int cycas_batch_case_field(cycas_ctx* c, int32_t k, const char* name, double* dst, int64_t n) {
+  return guard([&]() -> int {
+    require(c && name && dst && c->is_batch && k >= 0 && k < c->ncases, "bad argument");
+    auto p = lookup(*c, name);
+    long lo, cnt;
+    if (p.second == c->m.ncel) {
+      lo = c->case_lo[k];
+      cnt = c->case_hi[k] - lo;
+    } else if (p.second == c->m.nbnd) {
+      lo = c->bnd0[k];
+      cnt = c->bnd0[k + 1] - lo;
+    } else {
+      throw StatusError(CYCAS_ERR_INVALID, std::string("no per-case slice of ") + name);
+    }
+    require(n == cnt, std::string("size mismatch for ") + name);
+    CK(cudaMemcpyAsync(dst, p.first + lo, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CYCAS_OK;
+  });
+}
+
 }  // extern "C"
+
 

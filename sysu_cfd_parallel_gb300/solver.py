@@ -57,6 +57,10 @@ class Case:
         capi.check(capi.load().cycas_case_get_int(self._h, name.encode(), capi.ptr(out), out.size))
         return out
 
+    def footprint(self) -> float:
+        """Estimated device bytes of this case in a batch (cycas_footprint_estimate)."""
+        return capi.load().cycas_footprint_estimate(self._h)
+
     def close(self):
         if self._h:
             capi.load().cycas_case_free(self._h)
@@ -297,3 +301,65 @@ class Batch(NavierStokesSolver):
             capi.check(L.cycas_batch_residuals(self._h, capi.ptr(res[k])))
             self.step += 1
         return {"resmax": rm, "ksp_its": its, "ksp_reason": rs, "residual": res}
+
+
+class Server:
+    """Continuous-batching request server (cycas_server_*): submit param files, step, poll."""
+
+    def __init__(self, hbm_budget_gb: float = 150.0, residual_tol: float = 1e-6, max_iters: int = 10000,
+                 keep_fields: bool = False, options: capi.Options | None = None):
+        L = capi.load()
+        self.options = options or batch_options()
+        h = C.c_void_p()
+        capi.check(L.cycas_server_create(C.byref(self.options), hbm_budget_gb * 1e9, residual_tol, max_iters,
+                                         1 if keep_fields else 0, C.byref(h)))
+        self._h = h
+        self.results = {}
+
+    @staticmethod
+    def clock() -> float:
+        return capi.load().cycas_server_clock()
+
+    def submit(self, param_path: str) -> int:
+        i = C.c_int64()
+        rc = capi.load().cycas_server_submit(self._h, param_path.encode(), C.byref(i))
+        if rc != capi.CYCAS_OK:
+            raise capi.CycasError(rc, capi.load().cycas_server_last_error(self._h).decode())
+        return i.value
+
+    def step(self):
+        """Admit, re-form batches, one iteration of every active case, retire; returns
+        (active, queued) and records finished requests in ``results``."""
+        L = capi.load()
+        a, q = C.c_int32(), C.c_int32()
+        rc = L.cycas_server_step(self._h, C.byref(a), C.byref(q))
+        if rc != capi.CYCAS_OK:
+            raise capi.CycasError(rc, L.cycas_server_last_error(self._h).decode())
+        buf = (capi.RequestResult * 256)()
+        while True:
+            n = C.c_int32()
+            capi.check(L.cycas_server_poll(self._h, buf, 256, C.byref(n)))
+            for k in range(n.value):
+                r = buf[k]
+                self.results[r.id] = {"status": r.status, "iterations": r.iterations, "ncel": r.ncel,
+                                      "t_arrival": r.t_arrival, "t_admit": r.t_admit, "t_done": r.t_done,
+                                      "resmax": r.resmax}
+            if n.value < 256:
+                break
+        return a.value, q.value
+
+    def result_field(self, rid: int, name: str, n: int) -> np.ndarray:
+        out = np.empty(n)
+        capi.check(capi.load().cycas_server_result_field(self._h, rid, name.encode(), capi.ptr(out), n))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.load().cycas_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,56 @@
+"""Serving (cycas_server_*): continuous batching gives every request the result it gets alone.
+
+Requests join and leave the running batches while others iterate (the batch is re-formed and
+the state of continuing cases moved on the device), laminar cavities and k-epsilon channels
+run in separate batches, and the HBM budget holds requests back in arrival order.  Each
+finished request must match the same case run alone for the same number of iterations, to the
+tolerance of two runs whose Krylov inner products sum in different orders (relative L2 1e-5 at
+the reference's tolerances).
+"""
+import numpy as np
+import pytest
+
+from sysu_cfd_parallel_gb300 import capi
+from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver, Server, batch_options
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel_l2(a, b):
+    s = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / s if s > 0 else np.linalg.norm(a - b)
+
+
+def test_server_continuous_batching_matches_alone(cases):
+    names = ["cavity8", "channel_tiny", "cavity8j", "cavity4", "channel_small", "cavity12"]
+    params = {n: cases(n) for n in names}
+    # a budget for the two largest requests: the others wait in arrival order
+    fp = sorted(Case(p).footprint() for p in params.values())
+    budget_gb = (fp[-1] + fp[-2]) / 1e9
+    srv = Server(hbm_budget_gb=budget_gb, residual_tol=1e-4, max_iters=25, keep_fields=True)
+    ids = {}
+    ids[names[0]] = srv.submit(params[names[0]])
+    ids[names[1]] = srv.submit(params[names[1]])
+    max_active = 0
+    for step in range(200):
+        if step == 3:  # later arrivals join running batches
+            for n in names[2:]:
+                ids[n] = srv.submit(params[n])
+        active, queued = srv.step()
+        max_active = max(max_active, active)
+        if step > 3 and active == 0 and queued == 0:
+            break
+    assert len(srv.results) == len(names)
+    assert max_active < len(names)  # the budget held some requests back
+    for n in names:
+        r = srv.results[ids[n]]
+        assert r["status"] in (capi.REQ_CONVERGED, capi.REQ_MAX_ITERS), (n, r)
+        assert r["t_arrival"] <= r["t_admit"] <= r["t_done"]
+        s = NavierStokesSolver(Case(params[n]), batch_options())
+        s.iterate(r["iterations"])
+        fields = ["U", "V", "W", "P"] + (["TE", "ED"] if s.case.turb_model == 1 else [])
+        for nm in fields:
+            got = srv.result_field(ids[n], nm, s.case.ncel)
+            err = _rel_l2(got, s.get(nm))
+            assert err < 1e-5, f"{n} {nm}: relative L2 {err:.3e}"
+    srv.close()

@@ -146,6 +146,97 @@ def measure_batched(local, count, steps, mixed=False):
             "workload": f"{count} cavities n~U{{8..40}}^3 hexes, jitter 0.1h, Re~logU[10,1000], FP64 SIMPLE-C"}
 
 
+def serve_requests(args):
+    """Request stream of the serving workload (seeded): Poisson arrivals at args.rate per second
+    for args.duration seconds; each request a cavity (n^3 hexes, n uniform in the cavity range,
+    Re log-uniform in [10, 2000], lid speed 1) or, with equal probability, a jittered-tet k-eps
+    channel (10m x m x m x 6 tets, m uniform in the channel range, inlet U log-uniform in
+    [0.2, 5], mu 2e-5).  Meshes are shared between requests of the same size."""
+    import numpy as np
+    from sysu_cfd_parallel_gb300 import meshgen
+    rng = np.random.default_rng(args.serve_seed)
+    base = os.environ.get("CYCAS_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "cycas_bench_cases"))
+    n_lo, n_hi = [int(v) for v in args.cavity_n.split(",")]
+    m_lo, m_hi = [int(v) for v in args.channel_m.split(",")]
+    t, reqs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / args.rate)
+        if t > args.duration:
+            break
+        if rng.random() < 0.5:
+            n = int(rng.integers(n_lo, n_hi + 1))
+            re = 10.0 ** rng.uniform(1.0, np.log10(2000.0))
+            mesh_dir = os.path.join(base, "serve_cavity_n%d" % n)
+            if not os.path.exists(os.path.join(mesh_dir, "complete")):
+                meshgen.write_case(mesh_dir, "cavity", n=n, steps=10)
+                open(os.path.join(mesh_dir, "complete"), "w").close()
+            text = meshgen.cavity_param(os.path.join(mesh_dir, "case.msh"), steps=100000, mu=1.0 / re)
+        else:
+            m = int(rng.integers(m_lo, m_hi + 1))
+            u = 10.0 ** rng.uniform(np.log10(0.2), np.log10(5.0))
+            mesh_dir = os.path.join(base, "serve_channel_m%d" % m)
+            if not os.path.exists(os.path.join(mesh_dir, "complete")):
+                meshgen.write_case(mesh_dir, "channel", nx=10 * m, ny=m, nz=m, steps=10)
+                open(os.path.join(mesh_dir, "complete"), "w").close()
+            text = meshgen.channel_param(os.path.join(mesh_dir, "case.msh"), steps=100000, u_in=u)
+        pdir = os.path.join(base, "serve_req_s%d" % args.serve_seed)
+        os.makedirs(pdir, exist_ok=True)
+        param = os.path.join(pdir, "req%05d.in" % len(reqs))
+        with open(param, "w") as f:
+            f.write(text)
+        reqs.append((t, param))
+    return reqs
+
+
+def run_serve(args):
+    """Serving workload: requests submitted at their arrival times to the continuous-batching
+    server; reports time-to-converged percentiles and the aggregate cell-iterations/s."""
+    import numpy as np
+    import torch
+    from sysu_cfd_parallel_gb300.solver import Server, batch_options
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    reqs = serve_requests(args)
+    opt = batch_options(device=local)
+    opt.mixed = 1 if args.mixed else 0
+    srv = Server(hbm_budget_gb=args.budget_gb, residual_tol=args.tol, max_iters=args.max_iters, options=opt)
+    t0 = Server.clock()
+    k = 0
+    steps = 0
+    while True:
+        now = Server.clock() - t0
+        while k < len(reqs) and reqs[k][0] <= now:
+            srv.submit(reqs[k][1])
+            k += 1
+        active, queued = srv.step()
+        steps += 1
+        if k >= len(reqs) and active == 0 and queued == 0:
+            break
+        if Server.clock() - t0 > args.duration + args.drain:
+            break
+        if active == 0 and queued == 0 and k < len(reqs):
+            time.sleep(max(0.0, reqs[k][0] - (Server.clock() - t0)))
+    wall = Server.clock() - t0
+    res = list(srv.results.values())
+    lat = np.array([r["t_done"] - r["t_arrival"] for r in res]) if res else np.zeros(1)
+    conv = [r for r in res if r["status"] == 1]
+    cell_iters = sum(r["ncel"] * r["iterations"] for r in res)
+    line = {
+        "metric": "time-to-converged (serving, continuous batching)", "unit": "s", "higher_is_better": False,
+        "value": float(np.percentile(lat, 99)), "p50_s": float(np.percentile(lat, 50)),
+        "p99_s": float(np.percentile(lat, 99)), "requests": len(reqs), "finished": len(res),
+        "converged": len(conv), "server_steps": steps, "wall_s": wall,
+        "cell_iters_per_s": cell_iters / wall, "n_gpus": 1, "dtype": "f64" if not args.mixed else "mixed",
+        "data": "synthetic",
+        "config": {"workload": f"Poisson {args.rate}/s for {args.duration}s; cavities n={args.cavity_n}, "
+                               f"channels m={args.channel_m}; tol {args.tol}; cap {args.max_iters} iterations; "
+                               f"budget {args.budget_gb} GB; drain {args.drain}s",
+                   "mixed": bool(args.mixed)},
+    }
+    print(json.dumps(line), flush=True)
+    srv.close()
+
+
 # ---------------------------------------------------------------- clocks
 class Clocks:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -510,8 +601,21 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision and batched lines")
+    ap.add_argument("--workload", default="channel", choices=["channel", "serve"])
+    ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--drain", type=float, default=120.0)
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--max-iters", type=int, default=3000)
+    ap.add_argument("--cavity-n", default="16,64")
+    ap.add_argument("--channel-m", default="10,25")
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--mixed", action="store_true")
+    ap.add_argument("--serve-seed", type=int, default=5)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "serve":
+        run_serve(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

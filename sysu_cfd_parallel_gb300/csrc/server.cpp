@@ -10,11 +10,13 @@
 //      stay from the old batch to the new one on the device;
 //   3. advances every active case by one SIMPLE-C iteration (one batch iteration per class);
 //   4. retires every case whose residual, max_i localRes[i] divided by the case's volume, is
-//      at or below the tolerance (or that reached the iteration cap), recording its times.
+//      at or below the tolerance, that reached the iteration cap, or whose fields stopped being
+//      finite, recording its times.
 // A case's iterations are exactly those it would do alone; only the Krylov inner products
 // sum in another order (see the batch contexts).
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -206,16 +208,20 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
     std::vector<double> resmax(nc);
     std::vector<int32_t> its(8L * nc), reasons(8L * nc);
     int rc = cycas_batch_iteration(K.ctx, resmax.data(), its.data(), reasons.data());
-    if (rc != CYCAS_OK && rc != CYCAS_NOT_CONVERGED) return fail(s, rc);
+    // per-case outcomes are judged below; only errors of the batch itself stop the server
+    if (rc != CYCAS_OK && rc != CYCAS_NOT_CONVERGED && rc != CYCAS_NAN_DETECTED) return fail(s, rc);
     std::vector<int> retire;
     for (int k = 0; k < nc; k++) {
       Request* r = K.members[k];
       r->iterations++;
       r->resmax = resmax[k] / (r->volume > 0.0 ? r->volume : 1.0);
-      bool failed = false;
-      for (int q = 0; q < 8; q++) failed = failed || reasons[8L * k + q] < 0;
-      if (r->resmax <= s->tol) r->status = CYCAS_REQ_CONVERGED;
-      else if (failed) r->status = CYCAS_REQ_FAILED;
+      // a Krylov solve that stops short (iteration cap, breakdown near a converged field) does
+      // not end the request: the outer iteration goes on with its iterate, as long as the
+      // fields stay finite
+      bool failed = !std::isfinite(r->resmax);
+      for (int q = 0; q < 8; q++) failed = failed || reasons[8L * k + q] == CYCAS_KSP_DIVERGED_NANORINF;
+      if (failed) r->status = CYCAS_REQ_FAILED;
+      else if (r->resmax <= s->tol) r->status = CYCAS_REQ_CONVERGED;
       else if (r->iterations >= s->max_iters) r->status = CYCAS_REQ_MAX_ITERS;
       if (r->status != 0) retire.push_back(k);
     }

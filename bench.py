@@ -337,6 +337,40 @@ def krylov_bytes(its_row, turb, n, nnz, restart=30, levels=None):
     return out
 
 
+def krylov_fp64_flops(its_row, turb, n, nnz, restart=30):
+    """FP64 floating-point operations of each GMRES launch of one iteration (FP64 path): per
+    Arnoldi step j the SpMV (2 nnz), the Jacobi and basis scaling (2 n), the Gram-Schmidt dots and
+    update (4 n (j+1)) and the norm (2 n); per restart cycle the residual (2 nnz + 4 n) and the
+    solution update (2 n m_used).  CG slots are left out (their V-cycle is FP32)."""
+    kinds = ["gmres", "gmres", "gmres", "cg"] + (["gmres", "gmres"] if turb else [])
+    out = []
+    for slot, kind in enumerate(kinds):
+        its = int(its_row[slot])
+        if its < 0 or kind == "cg":
+            continue
+        f, left = 0, its
+        while True:
+            m = min(left, restart)
+            f += 2 * nnz + 4 * n
+            for j in range(m):
+                f += 2 * nnz + 2 * n + 4 * n * (j + 1) + 2 * n
+            f += 2 * n * m
+            left -= m
+            if left <= 0:
+                break
+        out.append((slot, f))
+    return out
+
+
+def measure_fp_rates():
+    """FP64 / FP32 FMA throughput of this GPU in TFLOP/s (cycas_measure_fp_rates)."""
+    import ctypes as C
+    from sysu_cfd_parallel_gb300 import capi
+    a, b = C.c_double(), C.c_double()
+    capi.check(capi.load().cycas_measure_fp_rates(C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -466,6 +500,7 @@ def run_gpu(args):
     from sysu_cfd_parallel_gb300 import capi
     from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
 
+    fp64_peak, fp32_peak = measure_fp_rates()
     param = make_case()
     case = Case(param)
     opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
@@ -511,6 +546,13 @@ def run_gpu(args):
     peak, peak_kind = measured_peak()
     launches = max(1, per_sys_launch[dom])
     achieved = (per_sys_bytes[dom] / launches) / (sys_ms[dom] / launches / 1e3) / 1e9 if sys_ms[dom] > 0 else 0.0
+    fp64 = None
+    if dom != "cg":
+        flops = sum(f for row in hist["ksp_its"] for slot, f in krylov_fp64_flops(row, turb, n, nnz)
+                    if (slot < 3) == (dom == "gmres_vel"))
+        ach = flops / (sys_ms[dom] / 1e3) / 1e12 if sys_ms[dom] > 0 else 0.0
+        fp64 = {"kernel": dom, "achieved_tflops": ach, "peak_tflops": fp64_peak, "peak_kind": "measured live",
+                "frac": ach / fp64_peak if fp64_peak > 0 else None, "fp32_peak_tflops": fp32_peak}
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
@@ -578,6 +620,7 @@ def run_gpu(args):
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "share_of_step": sys_ms[dom] / ms},
+            "fp64_roofline": fp64,
             "cpu_baseline": cpu,
             "mixed": mixed,
             "batched": batched,

@@ -220,6 +220,9 @@ typedef struct {
 int cycas_set_profiling(cycas_ctx* ctx, int32_t on);
 int cycas_get_profile(cycas_ctx* ctx, cycas_profile* out);
 int cycas_reset_profile(cycas_ctx* ctx);
+/* FP64 and FP32 FMA throughput of the current device in TFLOP/s (one CTA of 1024 threads per
+ * SM, eight independent FMA chains per thread); the bench's FP64 ceiling. */
+int cycas_measure_fp_rates(double* fp64_tflops, double* fp32_tflops);
 /* Sizes of the pressure AMG hierarchy (0 levels unless CYCAS_PC_AMG is in use): *nlev levels,
  * rows[l] and stored entries nnz[l] for the first max_levels of them, fine to coarse. */
 int cycas_get_amg_levels(cycas_ctx* ctx, int32_t max_levels, int32_t* nlev, int32_t* rows, int32_t* nnz);

@@ -36,6 +36,7 @@ UNITS = [
     ("capi.cu", "nvcc", []),
     ("noalloc.cu", "nvcc", []),
     ("server.cpp", "cxx", []),
+    ("rate_probe.cu", "nvcc", []),
 ]
 
 

@@ -556,8 +556,15 @@ def run_gpu(args):
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
+        # DRAM bytes of one captured launch (ncu), scaled to this run's mean Krylov iterations
+        # per launch of the same system (the traffic grows with the iterations)
         try:
-            traffic = json.load(open(tpath)).get(dom)
+            t = json.load(open(tpath)).get(dom)
+            if t:
+                its = [x[2] for row in hist["ksp_its"] for x in krylov_bytes(row, turb, n, nnz, levels=levels)
+                       if {"cg": x[0] == "cg", "gmres_vel": x[0] == "gmres" and x[1] < 3,
+                           "gmres_scalar": x[0] == "gmres" and x[1] >= 3}[dom]]
+                traffic = t["bytes"] * (sum(its) / len(its)) / t["its"] if its else None
         except Exception:
             traffic = None
 

@@ -216,6 +216,10 @@ typedef struct {
   double krylov_ms[3];       /* CUDA-event time of those launches per system (profiling on) */
   double assembly_ms;        /* CUDA-event time outside the Krylov launches (profiling on) */
 } cycas_profile;
+/* Graph replay: with on = 1 the next iteration is captured as one CUDA graph (every launch of
+ * the iteration, cooperative Krylov launches included) and later iterations replay it with a
+ * single launch; exclusive with per-solve profiling.  No counterpart in the reference. */
+int cycas_set_graph(cycas_ctx* ctx, int32_t on);
 /* Profiling records CUDA events around every Krylov launch on the context's stream. */
 int cycas_set_profiling(cycas_ctx* ctx, int32_t on);
 int cycas_get_profile(cycas_ctx* ctx, cycas_profile* out);
@@ -252,6 +256,12 @@ int cycas_batch_offsets(cycas_ctx* ctx, int32_t kind, int32_t* off);
 /* One SIMPLE-C iteration of every case: resmax[c] = vec_max of case c's localRes;
  * its/reasons[c*8 + k] = Krylov report of solve k of case c (-1 / 0 when not run). */
 int cycas_batch_iteration(cycas_ctx* ctx, double* resmax, int32_t* its, int32_t* reasons);
+/* Picks the team schedule of the batch's Krylov launches: for every CTA count G in {all, 3/4,
+ * 1/2 of the co-resident maximum} and every row-share factor f in {0.5, 1, 2} (a case gets a
+ * team of its own when it holds at least f*N/G of the N rows) it times `iters` SIMPLE
+ * iterations and keeps the fastest.  These are real iterations of every case (they advance
+ * the solution).  Reports the choice and its time per iteration. */
+int cycas_batch_autotune(cycas_ctx* ctx, int32_t iters, int32_t* best_grid, double* best_factor, double* best_ms);
 /* residual[c*10 + i] = localRes[i] of case c in the last iteration */
 int cycas_batch_residuals(cycas_ctx* ctx, double* residual);
 

@@ -619,7 +619,7 @@ cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& 
   cudaError_t e = cudaFuncSetAttribute((const void*)k_cg_amg, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)k_cg_amg, dim3(grid), dim3(kGmThreads), args, smem, s);
+  return launch_cooperative((const void*)k_cg_amg, grid, kGmThreads, args, smem, s);
 }
 
 }  // namespace cycas

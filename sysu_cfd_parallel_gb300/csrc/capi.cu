@@ -105,6 +105,10 @@ struct cycas_ctx {
   std::vector<int> amg_sizes;  // rows per AMG level (fine to coarse)
   std::vector<int> amg_nnz;    // stored entries per AMG level
   std::vector<int> case_lo, case_hi;  // row ranges of the independent cases (one for a context)
+  // CUDA graph of one iteration, captured on first use and replayed
+  bool use_graph = false;
+  cudaGraphExec_t gexec = nullptr;
+  long long graph_launches = 0;  // kernels of one replay
   // mixed precision (GMRES systems): FP32 copies of the system being solved
   bool mixed = false;
   double inner_rtol = 1e-4;
@@ -119,6 +123,8 @@ struct cycas_ctx {
   BatchSchedule* d_sched = nullptr;   // teams of the Krylov launches
   int sched_grid = 0, nteams = 0;
   unsigned* team_bar = nullptr;       // [2 * nteams]
+  int sched_G = 0;                    // schedule parameters in use
+  double sched_factor = 1.0;
   KspOut* bksp = nullptr;             // [8][ncases] per-case Krylov reports
   std::vector<double> h_res;          // [ncases][10]
   std::vector<KspOut> h_ksp;          // [8][ncases]
@@ -147,6 +153,7 @@ struct cycas_ctx {
   }
   ~cycas_ctx() {
     if (stream) cudaStreamSynchronize(stream);
+    if (gexec) cudaGraphExecDestroy(gexec);
     for (auto& e : ev_iter)
       if (e) cudaEventDestroy(e);
     for (auto& pr : ev_solve)
@@ -677,6 +684,39 @@ void issue_iteration(cycas_ctx& c) {
   if (c.turb == 1) update_keps(c);
 }
 
+// One iteration's device work.  In graph mode the first call captures begin + issue into a
+// CUDA graph (the launches of an iteration do not depend on device results, so the sequence
+// is the same every iteration) and every call replays it with one launch.
+void run_iteration(cycas_ctx& c) {
+  if (!c.use_graph) {
+    begin_iteration(c);
+    issue_iteration(c);
+    return;
+  }
+  if (!c.gexec) {
+    const long long l0 = g_launch_count;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed));
+    cudaGraph_t g = nullptr;
+    try {
+      begin_iteration(c);
+      issue_iteration(c);
+    } catch (...) {
+      cudaStreamEndCapture(c.stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    CK(cudaStreamEndCapture(c.stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&c.gexec, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    c.graph_launches = g_launch_count - l0;
+    g_launch_count = l0;
+  }
+  c.iter_open = false;
+  CK(cudaGraphLaunch(c.gexec, c.stream));
+  g_launch_count += c.graph_launches;
+}
+
 // reads the status block; returns the C status of the iteration
 int finish_iteration(cycas_ctx& c, double* residual, double* resmax, cycas_iter_stats* stats) {
   CK(cudaGetLastError());
@@ -870,11 +910,14 @@ UnionMesh build_union(const std::vector<const HostCase*>& hs) {
 // Teams for the batched Krylov launches: a case with at least N/G rows (N rows in all, G CTAs)
 // gets a team of about rows*G/N CTAs of its own; the smaller cases are spread over single-CTA
 // teams, largest first onto the least loaded team.
-void build_schedule(cycas_ctx& c) {
-  const int nc = c.ncases, G = c.kw.nblocks;
+// G: CTAs of the Krylov launches (at most the co-resident maximum); factor scales the row
+// share that earns a case its own team.
+void build_schedule(cycas_ctx& c, int G, double factor) {
+  const int nc = c.ncases;
+  G = std::max(1, std::min(G, c.kw.nblocks));
   long N = 0;
   for (int k = 0; k < nc; k++) N += c.case_hi[k] - c.case_lo[k];
-  const double target = (double)N / G;
+  const double target = factor * (double)N / G;
   std::vector<int> k_of(nc, 0);
   int used = 0;
   bool small = false;
@@ -952,7 +995,9 @@ void build_schedule(cycas_ctx& c) {
   hs.case_lo = c.upload(c.case_lo.data(), nc);
   hs.case_hi = c.upload(c.case_hi.data(), nc);
   c.d_sched = c.upload(&hs, 1);
-  c.team_bar = c.alloc<unsigned>(2L * c.nteams);
+  if (!c.team_bar) c.team_bar = c.alloc<unsigned>(2L * c.kw.nblocks);
+  c.sched_G = G;
+  c.sched_factor = factor;
 }
 
 // per-case metadata of a batch context
@@ -998,7 +1043,7 @@ void setup_batch(cycas_ctx& c, const UnionMesh& u, const std::vector<const HostC
   c.bksp = c.alloc<KspOut>(8L * nc);
   c.h_res.assign(10L * nc, 0.0);
   c.h_ksp.assign(8L * nc, KspOut{});
-  build_schedule(c);
+  build_schedule(c, c.kw.nblocks, 1.0);
 }
 
 // reads the per-case residuals and Krylov reports of a batch iteration
@@ -1265,8 +1310,7 @@ int cycas_get_int(cycas_ctx* c, const char* name, int32_t* dst, int64_t n) {
 int cycas_simple_iteration(cycas_ctx* c, double residual[10], double* resmax, cycas_iter_stats* stats) {
   return guard([&]() -> int {
     require(c != nullptr, "null context");
-    begin_iteration(*c);
-    issue_iteration(*c);
+    run_iteration(*c);
     return finish_iteration(*c, residual, resmax, stats);
   });
 }
@@ -1278,8 +1322,7 @@ int cycas_simple_iterations(cycas_ctx* c, int32_t n, double* res_hist, double* r
     for (int s = 0; s < n; s++) {
       cycas_iter_stats st;
       double res[10], rm;
-      begin_iteration(*c);
-      issue_iteration(*c);
+      run_iteration(*c);
       int rc = finish_iteration(*c, res, &rm, &st);
       if (res_hist) std::memcpy(res_hist + 10L * s, res, sizeof res);
       if (resmax) resmax[s] = rm;
@@ -1330,9 +1373,24 @@ int cycas_get_stream(cycas_ctx* c, void** stream) {
   });
 }
 
+int cycas_set_graph(cycas_ctx* c, int32_t on) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    require(!(on && c->profiling), "per-solve profiling and graph replay are exclusive");
+    if (c->gexec) {
+      CK(cudaStreamSynchronize(c->stream));
+      CK(cudaGraphExecDestroy(c->gexec));
+      c->gexec = nullptr;
+    }
+    c->use_graph = on != 0;
+    return CYCAS_OK;
+  });
+}
+
 int cycas_set_profiling(cycas_ctx* c, int32_t on) {
   return guard([&]() -> int {
     require(c != nullptr, "null context");
+    require(!(on && c->use_graph), "per-solve profiling and graph replay are exclusive");
     if (on && !c->ev_iter[0]) {
       for (auto& e : c->ev_iter) CK(cudaEventCreate(&e));
       for (auto& pr : c->ev_solve)
@@ -1535,8 +1593,7 @@ int cycas_batch_offsets(cycas_ctx* c, int32_t kind, int32_t* off) {
 int cycas_batch_iteration(cycas_ctx* c, double* resmax, int32_t* its, int32_t* reasons) {
   return guard([&]() -> int {
     require(c != nullptr && c->is_batch, "not a batch context");
-    begin_iteration(*c);
-    issue_iteration(*c);
+    run_iteration(*c);
     return finish_batch(*c, resmax, its, reasons);
   });
 }
@@ -1602,6 +1659,60 @@ int cycas_batch_case_field(cycas_ctx* c, int32_t k, const char* name, double* ds
   });
 }
 
+int cycas_batch_autotune(cycas_ctx* c, int32_t iters, int32_t* best_grid, double* best_factor, double* best_ms) {
+  return guard([&]() -> int {
+    require(c != nullptr && c->is_batch && iters >= 1, "bad argument");
+    const int G0 = c->kw.nblocks;
+    const int grids[3] = {G0, std::max(1, (3 * G0) / 4), std::max(1, G0 / 2)};
+    const double factors[3] = {0.5, 1.0, 2.0};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const bool graph = c->use_graph;
+    int bg = G0;
+    double bf = 1.0, bms = 1e300;
+    int rc = CYCAS_OK;
+    for (int gi = 0; gi < 3 && rc == CYCAS_OK; gi++)
+      for (int fi = 0; fi < 3 && rc == CYCAS_OK; fi++) {
+        build_schedule(*c, grids[gi], factors[fi]);
+        if (c->gexec) {
+          CK(cudaStreamSynchronize(c->stream));
+          CK(cudaGraphExecDestroy(c->gexec));
+          c->gexec = nullptr;
+        }
+        if (graph) run_iteration(*c), rc = finish_batch(*c, nullptr, nullptr, nullptr);  // capture outside the timing
+        CK(cudaEventRecord(e0, c->stream));
+        for (int k = 0; k < iters && (rc == CYCAS_OK || rc == CYCAS_NOT_CONVERGED); k++) {
+          run_iteration(*c);
+          rc = finish_batch(*c, nullptr, nullptr, nullptr);
+        }
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (rc == CYCAS_NOT_CONVERGED) rc = CYCAS_OK;
+        if (ms < bms) {
+          bms = ms;
+          bg = grids[gi];
+          bf = factors[fi];
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    build_schedule(*c, bg, bf);
+    if (c->gexec) {
+      CK(cudaStreamSynchronize(c->stream));
+      CK(cudaGraphExecDestroy(c->gexec));
+      c->gexec = nullptr;
+    }
+    if (best_grid) *best_grid = bg;
+    if (best_factor) *best_factor = bf;
+    if (best_ms) *best_ms = bms / iters;
+    return rc;
+  });
+}
+
 }  // extern "C"
+
 
 

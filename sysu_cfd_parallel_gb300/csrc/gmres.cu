@@ -524,7 +524,7 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
   a.dtol = 1e4;
   a.haptol = 1e-30;
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)k_gmres_ms<NS, Tv>, dim3(nb), dim3(kGmThreads), args, 0, s);
+  return launch_cooperative((const void*)k_gmres_ms<NS, Tv>, nb, kGmThreads, args, 0, s);
 }
 
 }  // namespace

@@ -361,7 +361,7 @@ cudaError_t launch_cg(const GmresCall& c, KrylovWork& w, cudaStream_t s) {
   a.abstol = 1e-50;
   a.dtol = 1e4;
   void* args[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)k_cg, dim3(a.nb), dim3(kGmThreads), args, 0, s);
+  return launch_cooperative((const void*)k_cg, a.nb, kGmThreads, args, 0, s);
 }
 
 int gmres_max_blocks(int device) {

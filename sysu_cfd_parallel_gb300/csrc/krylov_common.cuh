@@ -18,6 +18,22 @@ constexpr int kPartStride = kMaxRestart + 4;
 
 __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
 
+// cooperative launch (all CTAs co-resident) through the extensible launch API, which stream
+// capture records into a CUDA graph
+inline cudaError_t launch_cooperative(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
 // bounded grid barrier for a cooperative launch
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nb, int* err) {
   __shared__ int s_ok;

@@ -186,6 +186,10 @@ class NavierStokesSolver:
     def set_profiling(self, on: bool) -> None:
         capi.check(capi.load().cycas_set_profiling(self._h, 1 if on else 0))
 
+    def set_graph(self, on: bool) -> None:
+        """Replay each iteration as one captured CUDA graph (exclusive with profiling)."""
+        capi.check(capi.load().cycas_set_graph(self._h, 1 if on else 0))
+
     def amg_levels(self):
         """(rows, nnz) per level of the pressure AMG hierarchy, fine to coarse."""
         nl = C.c_int32()
@@ -279,6 +283,14 @@ class Batch(NavierStokesSolver):
         capi.check(L.cycas_batch_offsets(h, 1, capi.ptr(self.bnd0)))
         self.step = 0
         self.last_stats = None
+
+    def autotune(self, iters: int = 1):
+        """Times the team schedules (CTA count x row-share factor) over `iters` real iterations
+        each and keeps the fastest; returns (grid, factor, ms per iteration)."""
+        g, f, ms = C.c_int32(), C.c_double(), C.c_double()
+        capi.check(capi.load().cycas_batch_autotune(self._h, iters, C.byref(g), C.byref(f), C.byref(ms)))
+        self.step += 9 * iters
+        return g.value, f.value, ms.value
 
     def case_field(self, name: str, c: int) -> np.ndarray:
         a = self.get(name)

@@ -132,7 +132,20 @@ def measure_batched(local, count, steps, mixed=False):
     stream = torch.cuda.ExternalStream(b.stream_handle(), device=local)
     b.iterate(2)
     ms_b = timed_iterations(b, steps, stream)
+    # the autotuned team schedule, replayed as one CUDA graph per iteration
+    grid, factor, _ = b.autotune(1)
+    b.set_graph(True)
+    b.iterate(1)
+    ms_bg = timed_iterations(b, steps, stream)
     b.close()
+    # the same batch with mixed-precision GMRES
+    opt_m = batch_options(device=local)
+    opt_m.mixed = 1
+    bm = Batch(cases, opt_m)
+    stream_m = torch.cuda.ExternalStream(bm.stream_handle(), device=local)
+    bm.iterate(2)
+    ms_bm = timed_iterations(bm, steps, stream_m)
+    bm.close()
     ms_s = 0.0
     for c in cases:
         s = NavierStokesSolver(c, opt)
@@ -142,7 +155,12 @@ def measure_batched(local, count, steps, mixed=False):
         s.close()
     return {"cases": count, "cells": cells, "value": cells * steps / (ms_b / 1e3), "ms_per_step": ms_b / steps,
             "one_case_at_a_time": {"value": cells * steps / (ms_s / 1e3), "ms_per_step": ms_s / steps},
-            "speedup_vs_one_at_a_time": ms_s / ms_b, "mixed": bool(mixed),
+            "speedup_vs_one_at_a_time": ms_s / ms_b,
+            "autotuned_graph": {"value": cells * steps / (ms_bg / 1e3), "ms_per_step": ms_bg / steps,
+                                "team_ctas": grid, "row_share_factor": factor},
+            "batched_mixed": {"value": cells * steps / (ms_bm / 1e3), "ms_per_step": ms_bm / steps,
+                              "speedup_vs_plain_fp64_one_at_a_time": ms_s / ms_bm},
+            "mixed": bool(mixed),
             "workload": f"{count} cavities n~U{{8..40}}^3 hexes, jitter 0.1h, Re~logU[10,1000], FP64 SIMPLE-C"}
 
 
@@ -186,6 +204,50 @@ def serve_requests(args):
             f.write(text)
         reqs.append((t, param))
     return reqs
+
+
+def run_precision(args):
+    """Precision workload: the 400x40x40x6 channel (3.84M tets, seed 2027), plain FP64 against
+    mixed-precision GMRES from the same initial state for the same iterations; throughput of
+    both and the relative-L2 error of every field of the mixed run against the FP64 run."""
+    import numpy as np
+    import torch
+    from sysu_cfd_parallel_gb300 import capi, meshgen
+    from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    base = os.environ.get("CYCAS_BENCH_CACHE", os.path.join(tempfile.gettempdir(), "cycas_bench_cases"))
+    d = os.path.join(base, "channel_400x40x40_s2027")
+    param = os.path.join(d, "param.in")
+    if not os.path.exists(os.path.join(d, "complete")):
+        meshgen.write_case(d, "channel", nx=400, ny=40, nz=40, jitter=0.15, seed=2027, steps=500)
+        open(os.path.join(d, "complete"), "w").close()
+    out = {}
+    fields = {}
+    for mixed in (0, 1):
+        case = Case(param)
+        opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+        opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
+        opt.mixed = mixed
+        s = NavierStokesSolver(case, opt)
+        stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
+        if args.warmup > 0:
+            s.iterate(args.warmup)
+        ms = timed_iterations(s, args.steps, stream)
+        fields[mixed] = {nm: s.get(nm) for nm in ("U", "V", "W", "P", "TE", "ED")}
+        out["mixed" if mixed else "fp64"] = {"value": case.ncel * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps}
+        s.close()
+    err = {nm: float(np.linalg.norm(fields[1][nm] - fields[0][nm]) / np.linalg.norm(fields[0][nm]))
+           for nm in fields[0]}
+    line = {"metric": "cell-iters/s (steady SIMPLE-C, k-eps channel 3.84M tets)", "unit": "cell-iters/s",
+            "higher_is_better": True, "value": out["mixed"]["value"], "fp64": out["fp64"],
+            "mixed": out["mixed"], "speedup_mixed_vs_fp64": out["mixed"]["value"] / out["fp64"]["value"],
+            "field_rel_l2_mixed_vs_fp64": err, "steps": args.steps, "warmup": args.warmup, "n_gpus": 1,
+            "dtype": "mixed", "data": "synthetic",
+            "config": {"workload": "kepsilon channel 400x40x40x6 jittered tets (3840000 cells), seed 2027",
+                       "krylov": "GMRES systems: FP32 Arnoldi cycles (inner rtol 1e-4) in FP64 iterative "
+                                 "refinement to the reference rtol; CG + FP32 AMG V-cycle (p')"}}
+    print(json.dumps(line), flush=True)
 
 
 def run_serve(args):
@@ -651,7 +713,7 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision and batched lines")
-    ap.add_argument("--workload", default="channel", choices=["channel", "serve"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "serve", "precision"])
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--drain", type=float, default=120.0)
@@ -665,6 +727,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "serve":
         run_serve(args)
+    elif args.workload == "precision":
+        run_precision(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -228,6 +228,9 @@ def run_precision(args):
         case = Case(param)
         opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
         opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
+        for k in range(3):  # the precision workload's outer tolerance, for both runs
+            opt.ksp[k].rtol = args.outer_rtol
+            opt.ksp[k].maxit = 5000
         opt.mixed = mixed
         s = NavierStokesSolver(case, opt)
         stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
@@ -246,7 +249,8 @@ def run_precision(args):
             "dtype": "mixed", "data": "synthetic",
             "config": {"workload": "kepsilon channel 400x40x40x6 jittered tets (3840000 cells), seed 2027",
                        "krylov": "GMRES systems: FP32 Arnoldi cycles (inner rtol 1e-4) in FP64 iterative "
-                                 "refinement to the reference rtol; CG + FP32 AMG V-cycle (p')"}}
+                                 "refinement; CG + FP32 AMG V-cycle (p'); every system to the outer rtol "
+                                 "in both runs", "outer_rtol": args.outer_rtol}}
     print(json.dumps(line), flush=True)
 
 
@@ -724,6 +728,7 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--mixed", action="store_true")
     ap.add_argument("--serve-seed", type=int, default=5)
+    ap.add_argument("--outer-rtol", type=float, default=1e-10, help="precision workload: rtol of every system")
     args = ap.parse_args()
     if args.workload == "serve":
         run_serve(args)

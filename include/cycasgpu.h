@@ -91,6 +91,19 @@ int cycas_case_params(const cycas_case* c, double* residual_steady, double urf[8
 /* integer topology arrays by name (face_cell1, face_cell2, face_bnd, face_vertices, cell_nface,
  * cell_face, cell_cell, cell_vertices, cell_rid, bnd_face, bnd_rid, bnd_type, bnd_vertices) */
 int cycas_case_get_int(const cycas_case* c, const char* name, int32_t* dst, int64_t n);
+/* output cadence (the "output" key, noutput; NS/readparamfile.cpp:317-319) and the "restart"
+ * key (IfReadBackup, readparamfile.cpp:168-178).  With restart yes the initial cell fields are
+ * read from res.sav in the directory of param_path (ReadBackupFile, NS/navierIO.cpp:389-404,
+ * which reads it from the working directory). */
+int cycas_case_output(const cycas_case* c, int32_t* noutput, int32_t* restart);
+/* host arrays of a loaded case: vert [3*Nvrt] and the initial cell fields U V W P R T VisLam
+ * VisTur TE ED [Ncel] */
+int cycas_case_get_field(const cycas_case* c, const char* name, double* dst, int64_t n);
+/* Grid files of one partition holding the whole mesh: binary = 0 writes the ASCII Tecplot grid
+ * (tec/grid.dat of OutputGrid, NS/navierIO.cpp:58-128), binary = 1 the binary geometry
+ * (tec/geo of OutputGridBinary, navierIO.cpp:29-55: int32 {rank 0, 1 partition, Ncel, Nvrt},
+ * Nvrt x 3 doubles, Ncel x 8 one-based int32 vertex numbers). */
+int cycas_write_grid(const cycas_case* c, const char* path, int32_t binary);
 
 /* ---- mesh view for callers that already hold the reference's Face/Cell/Bnd arrays --- */
 typedef struct {
@@ -230,6 +243,22 @@ int cycas_measure_fp_rates(double* fp64_tflops, double* fp32_tflops);
 /* Sizes of the pressure AMG hierarchy (0 levels unless CYCAS_PC_AMG is in use): *nlev levels,
  * rows[l] and stored entries nnz[l] for the first max_levels of them, fine to coarse. */
 int cycas_get_amg_levels(cycas_ctx* ctx, int32_t max_levels, int32_t* nlev, int32_t* rows, int32_t* nnz);
+
+/* ---- result files of case k of a context (k = 0 for a single-case context; a batch's case
+ * index otherwise); each call copies the case's fields off the device and writes one file.
+ * Output2Tecplot (NS/navierIO.cpp:161-283): the ASCII Tecplot result (tec/res0000.dat),
+ * FEBRICK zone in BLOCK packing, x y z at the vertices, p u v w ro T Ma mu [te ed] at the cells,
+ * "%19.5f " numbers five to a line; c is the loaded case (vertices, connectivity). */
+int cycas_write_tecplot(cycas_ctx* ctx, int32_t k, const cycas_case* c, const char* path);
+/* Output2TecplotBinary (navierIO.cpp:132-159): tec/data, int32 {rank 0, nVar} then the cell
+ * fields P U V W R T [TE ED] as doubles, nVar = 6 (8 with k-epsilon). */
+int cycas_write_data(cycas_ctx* ctx, int32_t k, const char* path);
+/* WriteBackupFile (navierIO.cpp:370-387): res.sav, one line "R U V W P T R VisLam" per cell
+ * (plus "VisTur TE ED" with k-epsilon) in printf %g. */
+int cycas_write_backup(cycas_ctx* ctx, int32_t k, const char* path);
+/* ReadBackupFile (navierIO.cpp:389-404): sets R U V W P T VisLam [VisTur TE ED] of case k from
+ * a backup file. */
+int cycas_read_backup(cycas_ctx* ctx, int32_t k, const char* path);
 
 /* Standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
  * col[nnz], double val[nnz]); b and x are host arrays, x holds the initial guess unless

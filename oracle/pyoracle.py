@@ -162,3 +162,102 @@ def csr_solve(rowptr, col, val, b, x0=None, pc=PC_JACOBI, restart=30, rtol=1e-8,
     if rc != 0:
         raise RuntimeError(lib().orc_last_error().decode())
     return x, its.value, reason.value, rn.value
+
+
+# ---------------------------------------------------------------- result files (restatement)
+# Pure-Python renderings of the reference's writers, used by the tests as the checker of the
+# library's files.  Python's own float formatting (not the C library's printf) renders each
+# number, so agreement is a check of both.
+
+def _c_float_text(fmt, x):
+    """printf conversion of one double as glibc prints it (a NaN with the sign bit set is "-nan")."""
+    x = float(x)
+    if x != x:
+        neg = np.signbit(x)
+        w = fmt[1:].split(".")[0].rstrip("fg")
+        s = ("-nan" if neg else "nan")
+        return s.rjust(int(w)) if w else s
+    return fmt % x
+
+
+def _block(vals):
+    """OutArray2File (NS/navierIO.cpp:2-17): "%19.5f " on a 20-character stride, "\\n" after
+    every fifth value and after the block."""
+    out = []
+    n = len(vals)
+    for i, v in enumerate(vals):
+        s = _c_float_text("%19.5f", v) + " "
+        fifth = i % 5 == 4
+        if len(s) > 20 and (i != n - 1 or fifth):
+            s = s[:20]
+        out.append(s)
+        if fifth:
+            out.append("\n")
+    out.append("\n")
+    return "".join(out)
+
+
+def tecplot_text(vert, cell_vertices, f, turb):
+    """Output2Tecplot (NS/navierIO.cpp:161-283) at one rank: ``vert`` [nvrt, 3] or flat,
+    ``cell_vertices`` zero-based [ncel * 8], ``f`` a dict of cell fields P U V W R T VisLam VisTur
+    [TE ED]."""
+    vert = np.asarray(vert, dtype=np.float64).reshape(-1, 3)
+    cv = np.asarray(cell_vertices).reshape(-1, 8)
+    n = cv.shape[0]
+    nvar = 8 if turb == 1 else 6
+    head = 'variables= "x", "y", "z", "p", "u", "v", "w", "ro", "T","Ma","mu" '
+    if turb == 1:
+        head += '"te", "ed"'
+    parts = [head + "\n",
+             "ZONE N=%d, E=%d, VARLOCATION=([1-3]=NODAL,[4-%d]=CELLCENTERED) DATAPACKING=BLOCK, ZONETYPE=FEBRICK\n"
+             % (vert.shape[0], n, 3 + nvar + 2)]
+    for d in range(3):
+        parts.append(_block(vert[:, d]))
+    for nm in ("P", "U", "V", "W", "R", "T"):
+        parts.append(_block(f[nm]))
+    U, V, W = (np.asarray(f[k], dtype=np.float64) for k in ("U", "V", "W"))
+    parts.append(_block(np.sqrt(U * U + V * V + W * W)))
+    parts.append(_block(np.asarray(f["VisLam"]) + np.asarray(f["VisTur"])))
+    if turb == 1:
+        parts.append(_block(f["TE"]))
+        parts.append(_block(f["ED"]))
+    parts.append("".join("%d %d %d %d %d %d %d %d\n " % tuple(int(v) + 1 for v in row) for row in cv))
+    return "".join(parts)
+
+
+def grid_text(vert, cell_vertices):
+    """OutputGrid (NS/navierIO.cpp:58-128) at one rank: no interface vertices."""
+    vert = np.asarray(vert, dtype=np.float64).reshape(-1, 3)
+    cv = np.asarray(cell_vertices).reshape(-1, 8)
+    parts = ['title = "cycas partition grid"\nvariables="x","y","z","p"\n',
+             "zone n=%d, e=%d, f=fepoint, et=BRICK\n" % (vert.shape[0], cv.shape[0])]
+    parts += ["%f %f %f %f\n" % (x, y, z, 0.0) for x, y, z in vert]
+    parts += ["%8d %8d %8d %8d %8d %8d %8d %8d\n" % tuple(int(v) + 1 for v in row) for row in cv]
+    return "".join(parts)
+
+
+def geo_bytes(vert, cell_vertices):
+    """OutputGridBinary (NS/navierIO.cpp:29-55) at rank 0 of one partition."""
+    vert = np.asarray(vert, dtype="<f8").reshape(-1, 3)
+    cv = np.asarray(cell_vertices, dtype="<i4").reshape(-1, 8)
+    return (np.array([0, 1, cv.shape[0], vert.shape[0]], dtype="<i4").tobytes() + vert.tobytes()
+            + (cv + 1).astype("<i4").tobytes())
+
+
+def data_bytes(f, turb):
+    """Output2TecplotBinary (NS/navierIO.cpp:132-159)."""
+    names = ["P", "U", "V", "W", "R", "T"] + (["TE", "ED"] if turb == 1 else [])
+    return (np.array([0, len(names)], dtype="<i4").tobytes()
+            + b"".join(np.asarray(f[k], dtype="<f8").tobytes() for k in names))
+
+
+def backup_text(f, turb):
+    """WriteBackupFile (NS/navierIO.cpp:370-387): ostream's default conversion is %g."""
+    g = lambda x: _c_float_text("%g", x)
+    n = len(f["U"])
+    out = []
+    for i in range(n):
+        out.append(" ".join(g(f[k][i]) for k in ("R", "U", "V", "W", "P", "T", "R", "VisLam")) + "\n")
+        if turb == 1:
+            out.append(" ".join(g(f[k][i]) for k in ("VisTur", "TE", "ED")) + "\n")
+    return "".join(out)

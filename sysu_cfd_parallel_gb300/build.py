@@ -6,6 +6,7 @@ Translation units:
                  reference's source orders each product and sum
   krylov.cu      nvcc -- persistent GMRES, reductions
   capi.cu        nvcc -- C ABI and iteration schedule
+  result_io.cpp  g++ -ffp-contract=off -- result files in the reference's formats
 Objects are compiled in parallel and linked with nvcc into
 ``sysu_cfd_parallel_gb300/_build/libcycasgpu.so``.
 """
@@ -36,6 +37,7 @@ UNITS = [
     ("capi.cu", "nvcc", []),
     ("noalloc.cu", "nvcc", []),
     ("server.cpp", "cxx", []),
+    ("result_io.cpp", "cxx", ["-ffp-contract=off"]),
     ("rate_probe.cu", "nvcc", []),
 ]
 
@@ -79,7 +81,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(obj)
         path = os.path.join(CSRC, src)
         if kind == "cxx":
-            cmd = [CXX, "-O2", "-std=c++17", "-fPIC", "-Wall", "-c", path, "-o", obj, "-I", INCLUDE,
+            cmd = [CXX, "-O2", "-std=c++17", "-fPIC", "-Wall", *extra, "-c", path, "-o", obj, "-I", INCLUDE,
                    "-I", os.path.join(_cuda_home(), "include")]
         else:
             cmd = [NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",

@@ -81,7 +81,8 @@ class SolveStats(C.Structure):
 # every exported symbol declared in include/cycasgpu.h
 EXPORTS = (
     "cycas_last_error", "cycas_options_default", "cycas_case_load", "cycas_case_free", "cycas_case_dims",
-    "cycas_case_params", "cycas_case_get_int", "cycas_create", "cycas_create_from_case", "cycas_destroy",
+    "cycas_case_params", "cycas_case_get_int", "cycas_case_output", "cycas_case_get_field", "cycas_write_grid",
+    "cycas_write_tecplot", "cycas_write_data", "cycas_write_backup", "cycas_read_backup", "cycas_create", "cycas_create_from_case", "cycas_destroy",
     "cycas_get_field", "cycas_set_field", "cycas_get_int", "cycas_simple_iteration", "cycas_simple_iterations",
     "cycas_run_stage", "cycas_csr_solve", "cycas_get_stream", "cycas_set_profiling", "cycas_get_profile",
     "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels", "cycas_batch_create",
@@ -125,6 +126,13 @@ def load(build_if_missing: bool = True):
     L.cycas_case_dims.argtypes = [_P, C.POINTER(C.c_int64)]
     L.cycas_case_params.argtypes = [_P, _F64P, _F64P, _F64P]
     L.cycas_case_get_int.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.cycas_case_output.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.cycas_case_get_field.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.cycas_write_grid.argtypes = [_P, C.c_char_p, C.c_int32]
+    L.cycas_write_tecplot.argtypes = [_P, C.c_int32, _P, C.c_char_p]
+    L.cycas_write_data.argtypes = [_P, C.c_int32, C.c_char_p]
+    L.cycas_write_backup.argtypes = [_P, C.c_int32, C.c_char_p]
+    L.cycas_read_backup.argtypes = [_P, C.c_int32, C.c_char_p]
     L.cycas_create.argtypes = [C.POINTER(MeshView), C.POINTER(Params), C.POINTER(Options), C.POINTER(_P)]
     L.cycas_create_from_case.argtypes = [_P, C.POINTER(Options), C.POINTER(_P)]
     L.cycas_destroy.argtypes = [_P]

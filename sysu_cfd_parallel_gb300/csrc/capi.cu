@@ -1109,6 +1109,31 @@ int finish_batch(cycas_ctx& c, double* resmax, int32_t* its, int32_t* reasons) {
   return CYCAS_OK;
 }
 
+// ---------------------------------------------------------------- result files
+// The cell fields of case k (the context's only case when it is not a batch), copied to the host.
+struct CaseFields {
+  std::vector<double> a[10];  // P U V W R T VisLam VisTur TE ED
+  CellFieldsView view;
+};
+
+void fetch_case_fields(cycas_ctx& c, int k, CaseFields& out) {
+  require(k >= 0 && k < c.ncases, "case index out of range");
+  static const char* names[10] = {"P", "U", "V", "W", "R", "T", "VisLam", "VisTur", "TE", "ED"};
+  const long lo = c.case_lo[k], n = c.case_hi[k] - lo;
+  for (int i = 0; i < 10; i++) {
+    out.a[i].resize((size_t)n);
+    auto p = lookup(c, names[i]);
+    CK(cudaMemcpyAsync(out.a[i].data(), p.first + lo, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+  }
+  CK(cudaStreamSynchronize(c.stream));
+  CellFieldsView& v = out.view;
+  v.ncel = n;
+  v.turb = c.turb;
+  v.P = out.a[0].data(), v.U = out.a[1].data(), v.V = out.a[2].data(), v.W = out.a[3].data();
+  v.R = out.a[4].data(), v.T = out.a[5].data(), v.VisLam = out.a[6].data(), v.VisTur = out.a[7].data();
+  v.TE = out.a[8].data(), v.ED = out.a[9].data();
+}
+
 }  // namespace
 
 // ==================================================================== C ABI
@@ -1709,6 +1734,99 @@ int cycas_batch_autotune(cycas_ctx* c, int32_t iters, int32_t* best_grid, double
     if (best_factor) *best_factor = bf;
     if (best_ms) *best_ms = bms / iters;
     return rc;
+  });
+}
+
+// ---------------------------------------------------------------- result files
+int cycas_case_output(const cycas_case* c, int32_t* noutput, int32_t* restart) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null case");
+    if (noutput) *noutput = c->hc.noutput;
+    if (restart) *restart = c->hc.restart;
+    return CYCAS_OK;
+  });
+}
+
+int cycas_case_get_field(const cycas_case* c, const char* name, double* dst, int64_t n) {
+  return guard([&]() -> int {
+    require(c && name && dst, "null argument");
+    const HostCase& h = c->hc;
+    std::string s(name);
+    const std::vector<double>* v = nullptr;
+    if (s == "vert") v = &h.vert;
+    else if (s == "U") v = &h.U;
+    else if (s == "V") v = &h.V;
+    else if (s == "W") v = &h.W;
+    else if (s == "P") v = &h.P;
+    else if (s == "R") v = &h.R;
+    else if (s == "T") v = &h.T;
+    else if (s == "VisLam") v = &h.VisLam;
+    else if (s == "VisTur") v = &h.VisTur;
+    else if (s == "TE") v = &h.TE;
+    else if (s == "ED") v = &h.ED;
+    require(v != nullptr, "unknown case field " + s);
+    require((int64_t)v->size() == n, "size mismatch for " + s);
+    std::memcpy(dst, v->data(), sizeof(double) * (size_t)n);
+    return CYCAS_OK;
+  });
+}
+
+int cycas_write_grid(const cycas_case* c, const char* path, int32_t binary) {
+  return guard([&]() -> int {
+    require(c && path, "null argument");
+    write_file(path, binary ? geo_bytes(c->hc) : grid_text(c->hc));
+    return CYCAS_OK;
+  });
+}
+
+int cycas_write_tecplot(cycas_ctx* c, int32_t k, const cycas_case* cs, const char* path) {
+  return guard([&]() -> int {
+    require(c && cs && path, "null argument");
+    CaseFields f;
+    fetch_case_fields(*c, k, f);
+    require(cs->hc.ncel == f.view.ncel && cs->hc.turb_model == c->turb, "the case does not match the context's case");
+    write_file(path, tecplot_text(cs->hc.vert.data(), cs->hc.nvrt, cs->hc.cell_vertices.data(), f.view));
+    return CYCAS_OK;
+  });
+}
+
+int cycas_write_data(cycas_ctx* c, int32_t k, const char* path) {
+  return guard([&]() -> int {
+    require(c && path, "null argument");
+    CaseFields f;
+    fetch_case_fields(*c, k, f);
+    write_file(path, data_bytes(f.view));
+    return CYCAS_OK;
+  });
+}
+
+int cycas_write_backup(cycas_ctx* c, int32_t k, const char* path) {
+  return guard([&]() -> int {
+    require(c && path, "null argument");
+    CaseFields f;
+    fetch_case_fields(*c, k, f);
+    write_file(path, backup_text(f.view));
+    return CYCAS_OK;
+  });
+}
+
+int cycas_read_backup(cycas_ctx* c, int32_t k, const char* path) {
+  return guard([&]() -> int {
+    require(c && path, "null argument");
+    require(k >= 0 && k < c->ncases, "case index out of range");
+    const long lo = c->case_lo[k], n = c->case_hi[k] - lo;
+    std::vector<double> a[10];
+    double* dst[10];
+    for (int i = 0; i < 10; i++) a[i].assign((size_t)n, 0.0), dst[i] = a[i].data();
+    read_backup(path, n, c->turb, dst);
+    static const char* names[10] = {"R", "U", "V", "W", "P", "T", "VisLam", "VisTur", "TE", "ED"};
+    const int nread = c->turb == 1 ? 10 : 7;
+    for (int i = 0; i < nread; i++) {
+      auto p = lookup(*c, names[i]);
+      CK(cudaMemcpyAsync(p.first + lo, a[i].data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return CYCAS_OK;
   });
 }
 

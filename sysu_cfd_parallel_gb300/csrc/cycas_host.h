@@ -30,6 +30,7 @@ struct HostCase {
   double urf[8] = {0.6, 0.6, 0.6, 0.5, 0.8, 0.8, 0.8, 0.8};
   double gravity[3] = {0, 0, 0};
   std::string gridfile;
+  std::string backup_path;  // res.sav read when restart is "yes" (beside param.in)
   std::map<int, Region> regions;
 
   int ncel = 0, nfac = 0, nbnd = 0, nvrt = 0;
@@ -48,5 +49,24 @@ void load_gmsh(HostCase& hc, const std::string& path);
 void build_faces(HostCase& hc);
 void init_fields(HostCase& hc);
 void load_case(HostCase& hc, const std::string& paramPath);
+
+// ---------------------------------------------------------------- result files (result_io.cpp)
+// The cell fields one case writes, each [ncel] on the host (TE and ED only read with k-epsilon).
+struct CellFieldsView {
+  long ncel = 0;
+  int turb = 0;
+  const double *P = nullptr, *U = nullptr, *V = nullptr, *W = nullptr, *R = nullptr, *T = nullptr;
+  const double *VisLam = nullptr, *VisTur = nullptr, *TE = nullptr, *ED = nullptr;
+};
+
+std::string tecplot_text(const double* vert, long nvrt, const int32_t* cell_vertices, const CellFieldsView& f);
+std::string grid_text(const HostCase& hc);
+std::string geo_bytes(const HostCase& hc);
+std::string data_bytes(const CellFieldsView& f);
+std::string backup_text(const CellFieldsView& f);
+// parses a backup file into out[0..10) = R U V W P T VisLam VisTur TE ED (each [ncel]; the last
+// three only with k-epsilon)
+void read_backup(const std::string& path, long ncel, int turb, double* const out[10]);
+void write_file(const std::string& path, const std::string& bytes);
 
 }  // namespace cycas

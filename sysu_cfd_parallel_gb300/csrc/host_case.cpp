@@ -10,7 +10,8 @@
 //   element -> Cell/Bnd      NS/geometry.cpp:47-218 (hex-form vertex lists)
 //   face discovery order     NS/geometry.cpp:222-358 (CreateFaces / FindFace)
 //   neighbours               NS/geometry.cpp:461-473
-//   initial fields           NS/navier.cpp:588-697 (InitFlowField, steady, no restart)
+//   initial fields           NS/navier.cpp:588-697 (InitFlowField, steady; restart yes reads
+//                            res.sav beside param.in, ReadBackupFile navierIO.cpp:389-404)
 //
 // The face list is built by sorting (vertex-set key, discovery rank) records instead of the
 // reference's per-vertex std::set search and per-face realloc; it reproduces the same face
@@ -493,7 +494,6 @@ void init_fields(HostCase& hc) {
   for (auto* v : {&hc.U, &hc.V, &hc.W, &hc.R, &hc.T, &hc.P, &hc.VisLam, &hc.VisTur, &hc.TE, &hc.ED})
     v->assign(n, 0.0);
   for (auto* v : {&hc.BU, &hc.BV, &hc.BW, &hc.BRo, &hc.BTem, &hc.BTE, &hc.BED}) v->assign(nb, 0.0);
-  if (hc.restart) throw ParamError("restart from res.sav is outside the measured path");
   auto apply = [&](int i, const double* iv) {
     hc.U[i] = iv[0];
     hc.V[i] = iv[1];
@@ -509,13 +509,20 @@ void init_fields(HostCase& hc) {
       hc.VisTur[i] = hc.R[i] * Cmu * hc.TE[i] * hc.TE[i] / (hc.ED[i] + 1.e-16);
     }
   };
-  auto r0 = hc.regions.find(0);
-  if (r0 != hc.regions.end())
-    for (int i = 0; i < n; i++) apply(i, r0->second.init);
-  for (int i = 0; i < n; i++) {
-    auto it = hc.regions.find(hc.cell_rid[i]);
-    if (it == hc.regions.end()) throw ParamError("cell region " + std::to_string(hc.cell_rid[i]) + " not defined");
-    apply(i, it->second.init);
+  if (hc.restart) {
+    // restart yes: the cell fields come from the backup file alone (navier.cpp:590-591)
+    double* const dst[10] = {hc.R.data(), hc.U.data(), hc.V.data(), hc.W.data(), hc.P.data(),
+                             hc.T.data(), hc.VisLam.data(), hc.VisTur.data(), hc.TE.data(), hc.ED.data()};
+    read_backup(hc.backup_path, n, hc.turb_model, dst);
+  } else {
+    auto r0 = hc.regions.find(0);
+    if (r0 != hc.regions.end())
+      for (int i = 0; i < n; i++) apply(i, r0->second.init);
+    for (int i = 0; i < n; i++) {
+      auto it = hc.regions.find(hc.cell_rid[i]);
+      if (it == hc.regions.end()) throw ParamError("cell region " + std::to_string(hc.cell_rid[i]) + " not defined");
+      apply(i, it->second.init);
+    }
   }
   hc.bnd_type.assign(nb, 0);
   for (int i = 0; i < nb; i++) {
@@ -550,6 +557,8 @@ void load_case(HostCase& hc, const std::string& paramPath) {
   }
   load_gmsh(hc, grid);
   build_faces(hc);
+  size_t sl = paramPath.find_last_of('/');
+  hc.backup_path = (sl == std::string::npos ? std::string() : paramPath.substr(0, sl + 1)) + "res.sav";
   init_fields(hc);
 }
 

@@ -47,6 +47,25 @@ class Case:
         self.residual_steady = rs.value
         self.urf = list(urf)
         self.gravity = list(g)
+        no, rst = C.c_int32(), C.c_int32()
+        capi.check(L.cycas_case_output(h, C.byref(no), C.byref(rst)))
+        self.noutput = no.value
+        self.restart = bool(rst.value)
+        self.param_path = param_path
+
+    def get_field(self, name: str) -> np.ndarray:
+        """Host arrays of the loaded case: ``vert`` [3*nvrt] or an initial cell field."""
+        out = np.empty(3 * self.nvrt if name == "vert" else self.ncel, dtype=np.float64)
+        capi.check(capi.load().cycas_case_get_field(self._h, name.encode(), capi.ptr(out), out.size))
+        return out
+
+    def OutputGrid(self, path: str = "tec/grid.dat") -> None:
+        """ASCII Tecplot grid (NS/navierIO.cpp:58-128)."""
+        capi.check(capi.load().cycas_write_grid(self._h, path.encode(), 0))
+
+    def OutputGridBinary(self, path: str = "tec/geo") -> None:
+        """Binary geometry (NS/navierIO.cpp:29-55)."""
+        capi.check(capi.load().cycas_write_grid(self._h, path.encode(), 1))
 
     def get_int(self, name: str) -> np.ndarray:
         sizes = {"face_cell1": self.nfac, "face_cell2": self.nfac, "face_bnd": self.nfac,
@@ -164,17 +183,67 @@ class NavierStokesSolver:
         self.step += n
         return {"residual": res, "resmax": rm, "ksp_its": its, "ksp_reason": rs}
 
-    def NSSolve(self, max_step: int | None = None, residual_steady: float | None = None, callback=None):
-        """Steady outer loop (NS/navier.cpp:52-141): stop when ResMax < ResidualSteady."""
+    # ---- result files (NS/navierIO.cpp); k is the case of a batch, 0 otherwise
+    def _case_handle(self, k: int):
+        if k != 0:
+            raise IndexError("a single-case solver has case 0 only")
+        return self.case._h
+
+    def Output2Tecplot(self, path: str = "tec/res0000.dat", k: int = 0) -> None:
+        """ASCII Tecplot result of the current fields (NS/navierIO.cpp:161-283)."""
+        capi.check(capi.load().cycas_write_tecplot(self._h, k, self._case_handle(k), path.encode()))
+
+    def Output2TecplotBinary(self, path: str = "tec/data", k: int = 0) -> None:
+        """Binary cell fields P U V W R T [TE ED] (NS/navierIO.cpp:132-159)."""
+        capi.check(capi.load().cycas_write_data(self._h, k, path.encode()))
+
+    def WriteBackupFile(self, path: str = "localGeometryBackup_0/res.sav", k: int = 0) -> None:
+        """Restart file (NS/navierIO.cpp:370-387)."""
+        capi.check(capi.load().cycas_write_backup(self._h, k, path.encode()))
+
+    def ReadBackupFile(self, path: str = "res.sav", k: int = 0) -> None:
+        """Sets the cell fields from a restart file (NS/navierIO.cpp:389-404)."""
+        capi.check(capi.load().cycas_read_backup(self._h, k, path.encode()))
+
+    def NSSolve(self, max_step: int | None = None, residual_steady: float | None = None, callback=None,
+                output_dir: str | None = None, out_binary: bool = False, noutput: int | None = None):
+        """Steady outer loop (NS/navier.cpp:52-141): stop when ResMax < ResidualSteady.
+
+        With ``output_dir`` the reference's files are written under it at the reference's
+        cadence: the grid before the loop (tec/geo with ``out_binary``, else tec/grid.dat;
+        geometry.cpp:209-213); after step s (1-based) with (s - 1) % noutput == 0 the backup
+        localGeometryBackup_0/res.sav and tec/data (``out_binary``) or tec/res0000.dat
+        (navier.cpp:113-122, 161-199); after the loop tec/res0000.dat (navier.cpp:149).
+        """
+        import os
+
         max_step = self.case.max_step if max_step is None else max_step
         tol = self.case.residual_steady if residual_steady is None else residual_steady
+        nout = max(1, (self.case.noutput if noutput is None else noutput))
+        if output_dir is not None:
+            tec = os.path.join(output_dir, "tec")
+            bak = os.path.join(output_dir, "localGeometryBackup_0")
+            os.makedirs(tec, exist_ok=True)
+            os.makedirs(bak, exist_ok=True)
+            if out_binary:
+                self.case.OutputGridBinary(os.path.join(tec, "geo"))
+            else:
+                self.case.OutputGrid(os.path.join(tec, "grid.dat"))
         rm = None
-        for _ in range(max_step):
+        for step in range(1, max_step + 1):
             rm = self.simple_iteration()
             if callback:
                 callback(self.step, rm, self.Residual)
+            if output_dir is not None and (step - 1) % nout == 0:
+                self.WriteBackupFile(os.path.join(bak, "res.sav"))
+                if out_binary:
+                    self.Output2TecplotBinary(os.path.join(tec, "data"))
+                else:
+                    self.Output2Tecplot(os.path.join(tec, "res0000.dat"))
             if rm < tol:
                 break
+        if output_dir is not None:
+            self.Output2Tecplot(os.path.join(tec, "res0000.dat"))
         return rm
 
     # ---- measurement hooks
@@ -283,6 +352,9 @@ class Batch(NavierStokesSolver):
         capi.check(L.cycas_batch_offsets(h, 1, capi.ptr(self.bnd0)))
         self.step = 0
         self.last_stats = None
+
+    def _case_handle(self, k: int):
+        return self.cases[k]._h
 
     def autotune(self, iters: int = 1):
         """Times the team schedules (CTA count x row-share factor) over `iters` real iterations

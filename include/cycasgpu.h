@@ -83,6 +83,12 @@ typedef struct cycas_case cycas_case;
  * (InitFlowField, NS/navier.cpp:588-697).  A relative gridfile is resolved against the
  * directory of param_path. */
 int cycas_case_load(const char* param_path, cycas_case** out);
+/* Same with flags: CYCAS_LOAD_MSH_BINARY reads the gridfile as the compressed binary gmsh form
+ * (RootProcess::readBin, NS/RootStructure.cpp:61-116; the -mshBinary switch, NS/main.cpp:27,48):
+ * uint64 vertex count, {int32 id, 3 doubles} per vertex, uint64 element count, {int32 id, int32
+ * type, int32 ntag, ntag int32 tags, one-based int32 vertex ids} per element. */
+#define CYCAS_LOAD_MSH_BINARY 1
+int cycas_case_load_ex(const char* param_path, int32_t flags, cycas_case** out);
 void cycas_case_free(cycas_case* c);
 /* dims: [0] Ncel [1] Nfac [2] Nbnd [3] Nvrt [4] TurModel [5] MaxStep [6] cellPressureRef [7] nnz */
 int cycas_case_dims(const cycas_case* c, int64_t dims[8]);
@@ -259,6 +265,20 @@ int cycas_write_backup(cycas_ctx* ctx, int32_t k, const char* path);
 /* ReadBackupFile (navierIO.cpp:389-404): sets R U V W P T VisLam [VisTur TE ED] of case k from
  * a backup file. */
 int cycas_read_backup(cycas_ctx* ctx, int32_t k, const char* path);
+
+/* Asynchronous dump of case k (no counterpart in the reference, whose writers stop the solve
+ * while they gather and format): the cell fields are snapshotted on the context's stream (a
+ * device-to-device copy), copied to pinned host memory on a side stream while later iterations
+ * run, and formatted and written by a host thread, to the same bytes as the writers above.
+ * kinds is a set of CYCAS_DUMP_* bits; c (Tecplot only) must stay loaded until the dump ends.
+ * One dump is in flight per context: a second begin waits for the first; cycas_dump_wait waits
+ * and returns the dump's status (a failure not yet collected is returned by the next begin). */
+#define CYCAS_DUMP_TECPLOT 1
+#define CYCAS_DUMP_DATA 2
+#define CYCAS_DUMP_BACKUP 4
+int cycas_dump_begin(cycas_ctx* ctx, int32_t k, const cycas_case* c, int32_t kinds, const char* tecplot_path,
+                     const char* data_path, const char* backup_path);
+int cycas_dump_wait(cycas_ctx* ctx);
 
 /* Standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
  * col[nnz], double val[nnz]); b and x are host arrays, x holds the initial guess unless

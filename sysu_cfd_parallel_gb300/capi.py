@@ -24,6 +24,8 @@ CYCAS_ERR_MESH = 8
 CYCAS_ERR_UNSUPPORTED = 9
 
 PC_NONE, PC_JACOBI, PC_ILU0, PC_AMG = 0, 1, 2, 3
+LOAD_MSH_BINARY = 1
+DUMP_TECPLOT, DUMP_DATA, DUMP_BACKUP = 1, 2, 4
 KSP_DEFAULT, KSP_GMRES, KSP_CG = 0, 1, 2
 SYS_VELOCITY, SYS_PRESSURE, SYS_SCALAR = 0, 1, 2
 
@@ -80,9 +82,11 @@ class SolveStats(C.Structure):
 
 # every exported symbol declared in include/cycasgpu.h
 EXPORTS = (
-    "cycas_last_error", "cycas_options_default", "cycas_case_load", "cycas_case_free", "cycas_case_dims",
-    "cycas_case_params", "cycas_case_get_int", "cycas_case_output", "cycas_case_get_field", "cycas_write_grid",
-    "cycas_write_tecplot", "cycas_write_data", "cycas_write_backup", "cycas_read_backup", "cycas_create", "cycas_create_from_case", "cycas_destroy",
+    "cycas_last_error", "cycas_options_default", "cycas_case_load", "cycas_case_load_ex", "cycas_case_free",
+    "cycas_case_dims", "cycas_case_params", "cycas_case_get_int", "cycas_case_output", "cycas_case_get_field",
+    "cycas_write_grid", "cycas_write_tecplot", "cycas_write_data", "cycas_write_backup", "cycas_read_backup",
+    "cycas_dump_begin", "cycas_dump_wait",
+    "cycas_create", "cycas_create_from_case", "cycas_destroy",
     "cycas_get_field", "cycas_set_field", "cycas_get_int", "cycas_simple_iteration", "cycas_simple_iterations",
     "cycas_run_stage", "cycas_csr_solve", "cycas_get_stream", "cycas_set_profiling", "cycas_get_profile",
     "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels", "cycas_batch_create",
@@ -121,6 +125,7 @@ def load(build_if_missing: bool = True):
     L.cycas_options_default.argtypes = [C.POINTER(Options)]
     L.cycas_options_default.restype = None
     L.cycas_case_load.argtypes = [C.c_char_p, C.POINTER(_P)]
+    L.cycas_case_load_ex.argtypes = [C.c_char_p, C.c_int32, C.POINTER(_P)]
     L.cycas_case_free.argtypes = [_P]
     L.cycas_case_free.restype = None
     L.cycas_case_dims.argtypes = [_P, C.POINTER(C.c_int64)]
@@ -133,6 +138,8 @@ def load(build_if_missing: bool = True):
     L.cycas_write_data.argtypes = [_P, C.c_int32, C.c_char_p]
     L.cycas_write_backup.argtypes = [_P, C.c_int32, C.c_char_p]
     L.cycas_read_backup.argtypes = [_P, C.c_int32, C.c_char_p]
+    L.cycas_dump_begin.argtypes = [_P, C.c_int32, _P, C.c_int32, C.c_char_p, C.c_char_p, C.c_char_p]
+    L.cycas_dump_wait.argtypes = [_P]
     L.cycas_create.argtypes = [C.POINTER(MeshView), C.POINTER(Params), C.POINTER(Options), C.POINTER(_P)]
     L.cycas_create_from_case.argtypes = [_P, C.POINTER(Options), C.POINTER(_P)]
     L.cycas_destroy.argtypes = [_P]

@@ -11,6 +11,7 @@
 #include <exception>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/cycasgpu.h"
@@ -70,6 +71,20 @@ int guard(F&& f) {
     return CYCAS_ERR_INVALID;
   }
 }
+
+// Asynchronous result dump of one context: the cell fields are snapshotted on the compute
+// stream (device-to-device, a few microseconds), copied out on a side stream while the next
+// iterations run, and formatted and written by a host thread.
+struct DumpState {
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_snap = nullptr, ev_host = nullptr;
+  double* snap = nullptr;  // device [10 * cap]
+  double* host = nullptr;  // pinned [10 * cap]
+  long cap = 0;
+  std::thread worker;
+  int rc = 0;
+  std::string err;
+};
 
 }  // namespace cycas
 
@@ -151,7 +166,14 @@ struct cycas_ctx {
     dfields[name] = {p, n};
     return p;
   }
+  DumpState dump;
   ~cycas_ctx() {
+    if (dump.worker.joinable()) dump.worker.join();
+    if (dump.side) cudaStreamSynchronize(dump.side);
+    if (dump.ev_snap) cudaEventDestroy(dump.ev_snap);
+    if (dump.ev_host) cudaEventDestroy(dump.ev_host);
+    if (dump.host) cudaFreeHost(dump.host);
+    if (dump.side) cudaStreamDestroy(dump.side);
     if (stream) cudaStreamSynchronize(stream);
     if (gexec) cudaGraphExecDestroy(gexec);
     for (auto& e : ev_iter)
@@ -1153,13 +1175,16 @@ void cycas_options_default(cycas_options* o) {
   o->device = 0;
 }
 
-int cycas_case_load(const char* param_path, cycas_case** out) {
+int cycas_case_load(const char* param_path, cycas_case** out) { return cycas_case_load_ex(param_path, 0, out); }
+
+int cycas_case_load_ex(const char* param_path, int32_t flags, cycas_case** out) {
   return guard([&]() -> int {
     require(param_path && out, "null argument");
+    require((flags & ~CYCAS_LOAD_MSH_BINARY) == 0, "unknown load flags");
     *out = nullptr;
     cycas_case* c = new cycas_case();
     try {
-      load_case(c->hc, param_path);
+      load_case(c->hc, param_path, (flags & CYCAS_LOAD_MSH_BINARY) != 0);
     } catch (...) {
       delete c;
       throw;
@@ -1826,6 +1851,94 @@ int cycas_read_backup(cycas_ctx* c, int32_t k, const char* path) {
       CK(cudaMemcpyAsync(p.first + lo, a[i].data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
+    return CYCAS_OK;
+  });
+}
+
+// ---------------------------------------------------------------- asynchronous dumps
+int cycas_dump_begin(cycas_ctx* c, int32_t k, const cycas_case* cs, int32_t kinds, const char* tecplot_path,
+                     const char* data_path, const char* backup_path) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    require(k >= 0 && k < c->ncases, "case index out of range");
+    require(kinds != 0 && (kinds & ~(CYCAS_DUMP_TECPLOT | CYCAS_DUMP_DATA | CYCAS_DUMP_BACKUP)) == 0,
+            "kinds must be a non-empty set of CYCAS_DUMP_* bits");
+    require(!(kinds & CYCAS_DUMP_TECPLOT) || (cs && tecplot_path), "the Tecplot dump needs the case and a path");
+    require(!(kinds & CYCAS_DUMP_DATA) || data_path, "the data dump needs a path");
+    require(!(kinds & CYCAS_DUMP_BACKUP) || backup_path, "the backup dump needs a path");
+    const long lo = c->case_lo[k], n = c->case_hi[k] - lo;
+    if (kinds & CYCAS_DUMP_TECPLOT)
+      require(cs->hc.ncel == n && cs->hc.turb_model == c->turb, "the case does not match the context's case");
+    DumpState& d = c->dump;
+    // one dump in flight: the previous one must have finished with the snapshot and host buffers
+    if (d.worker.joinable()) d.worker.join();
+    if (d.rc != CYCAS_OK) {
+      int rc = d.rc;
+      d.rc = CYCAS_OK;
+      throw StatusError(rc, "previous dump failed: " + d.err);
+    }
+    if (!d.side) {
+      long cap = 0;
+      for (int q = 0; q < c->ncases; q++) cap = std::max(cap, (long)(c->case_hi[q] - c->case_lo[q]));
+      CK(cudaStreamCreateWithFlags(&d.side, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&d.ev_snap, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&d.ev_host, cudaEventDisableTiming));
+      d.snap = c->alloc<double>(10 * cap);
+      void* h = nullptr;
+      if (cudaMallocHost(&h, sizeof(double) * 10 * (size_t)std::max(cap, 1L)) != cudaSuccess)
+        throw StatusError(CYCAS_ERR_ALLOC, "pinned host buffer of the dump");
+      d.host = (double*)h;
+      d.cap = cap;
+    }
+    static const char* names[10] = {"P", "U", "V", "W", "R", "T", "VisLam", "VisTur", "TE", "ED"};
+    for (int i = 0; i < 10; i++) {
+      auto p = lookup(*c, names[i]);
+      CK(cudaMemcpyAsync(d.snap + i * n, p.first + lo, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    CK(cudaEventRecord(d.ev_snap, c->stream));
+    CK(cudaStreamWaitEvent(d.side, d.ev_snap, 0));
+    CK(cudaMemcpyAsync(d.host, d.snap, sizeof(double) * 10 * n, cudaMemcpyDeviceToHost, d.side));
+    CK(cudaEventRecord(d.ev_host, d.side));
+    const std::string tp = tecplot_path ? tecplot_path : "", dp = data_path ? data_path : "",
+                      bp = backup_path ? backup_path : "";
+    const HostCase* hc = (kinds & CYCAS_DUMP_TECPLOT) ? &cs->hc : nullptr;
+    const int turb = c->turb, device = c->device;
+    d.worker = std::thread([&d, hc, kinds, tp, dp, bp, n, turb, device]() {
+      try {
+        cudaSetDevice(device);
+        cudaError_t e = cudaEventSynchronize(d.ev_host);
+        if (e != cudaSuccess) throw CudaError(std::string("dump copy: ") + cudaGetErrorString(e));
+        CellFieldsView v;
+        v.ncel = n;
+        v.turb = turb;
+        const double* b = d.host;
+        v.P = b, v.U = b + n, v.V = b + 2 * n, v.W = b + 3 * n, v.R = b + 4 * n, v.T = b + 5 * n;
+        v.VisLam = b + 6 * n, v.VisTur = b + 7 * n, v.TE = b + 8 * n, v.ED = b + 9 * n;
+        if (kinds & CYCAS_DUMP_BACKUP) write_file(bp, backup_text(v));
+        if (kinds & CYCAS_DUMP_DATA) write_file(dp, data_bytes(v));
+        if (kinds & CYCAS_DUMP_TECPLOT)
+          write_file(tp, tecplot_text(hc->vert.data(), hc->nvrt, hc->cell_vertices.data(), v));
+        d.rc = CYCAS_OK;
+      } catch (CudaError& e) {
+        d.rc = CYCAS_ERR_CUDA, d.err = e.what();
+      } catch (IoError& e) {
+        d.rc = CYCAS_ERR_IO, d.err = e.what();
+      } catch (std::exception& e) {
+        d.rc = CYCAS_ERR_INVALID, d.err = e.what();
+      }
+    });
+    return CYCAS_OK;
+  });
+}
+
+int cycas_dump_wait(cycas_ctx* c) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    DumpState& d = c->dump;
+    if (d.worker.joinable()) d.worker.join();
+    int rc = d.rc;
+    d.rc = CYCAS_OK;
+    if (rc != CYCAS_OK) throw StatusError(rc, d.err);
     return CYCAS_OK;
   });
 }

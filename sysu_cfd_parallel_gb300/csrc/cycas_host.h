@@ -45,10 +45,10 @@ struct HostCase {
 };
 
 void load_params(HostCase& hc, const std::string& path);
-void load_gmsh(HostCase& hc, const std::string& path);
+void load_gmsh(HostCase& hc, const std::string& path, bool binary);
 void build_faces(HostCase& hc);
 void init_fields(HostCase& hc);
-void load_case(HostCase& hc, const std::string& paramPath);
+void load_case(HostCase& hc, const std::string& paramPath, bool msh_binary = false);
 
 // ---------------------------------------------------------------- result files (result_io.cpp)
 // The cell fields one case writes, each [ncel] on the host (TE and ED only read with k-epsilon).

@@ -4,7 +4,8 @@
 //
 // Reference behaviour mirrored here:
 //   param.in keys            NS/readparamfile.cpp:10-344
-//   gmsh reader              NS/RootStructure.cpp:428-487
+//   gmsh reader              NS/RootStructure.cpp:428-487 (ASCII), 61-116 (compressed binary,
+//                            the -mshBinary switch of main.cpp:27,48)
 //   one-rank numbering       NS/RootStructure.cpp:797-816 (std::sort by part id) and the
 //                            vertex pool of getVertexSendBuffer, RootStructure.cpp:930-968
 //   element -> Cell/Bnd      NS/geometry.cpp:47-218 (hex-form vertex lists)
@@ -209,13 +210,27 @@ struct Tokenizer {
   }
 };
 
+// little-endian fixed-size records of the compressed mesh, bounds-checked
+struct ByteReader {
+  const char* p;
+  const char* end;
+  template <class T>
+  T take() {
+    if (end - p < (long)sizeof(T)) throw MeshError("truncated binary mesh file");
+    T v;
+    std::memcpy(&v, p, sizeof(T));
+    p += sizeof(T);
+    return v;
+  }
+};
+
 struct RawElem {
   int type, tag0;
   int v[8];
 };
 }  // namespace
 
-void load_gmsh(HostCase& hc, const std::string& path) {
+void load_gmsh(HostCase& hc, const std::string& path, bool binary) {
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) throw IoError("cant find grid file " + path);
   std::fseek(f, 0, SEEK_END);
@@ -227,40 +242,79 @@ void load_gmsh(HostCase& hc, const std::string& path) {
     throw IoError("short read on " + path);
   }
   std::fclose(f);
-  Tokenizer tk{data.data(), data.data() + sz};
-  std::string w;
-  do {
-    if (!tk.word(w)) throw MeshError("no $Nodes section");
-  } while (w != "$Nodes");
-  long nv = tk.integer();
-  if (nv <= 0) throw MeshError("vertex less than 0");
-  std::vector<double> raw(3 * (size_t)nv);
-  for (long i = 0; i < nv; i++) {
-    tk.integer();
-    raw[3 * i] = tk.real();
-    raw[3 * i + 1] = tk.real();
-    raw[3 * i + 2] = tk.real();
-  }
-  tk.word(w);
-  tk.word(w);
-  long ne = tk.integer();
-  if (ne <= 0) throw MeshError("elements of the mesh file less than 0");
-  std::vector<RawElem> el((size_t)ne);
-  for (long i = 0; i < ne; i++) {
-    tk.integer();
-    RawElem& e = el[i];
-    e.type = (int)tk.integer();
-    int ntag = (int)tk.integer();
+  long nv = 0, ne = 0;
+  std::vector<double> raw;
+  std::vector<RawElem> el;
+  auto check_elem = [&](RawElem& e, int ntag) {
     if (e.type < 0 || e.type > 7 || ntag < 0 || ntag > 10) throw MeshError("bad element record");
     if (ntag != 2 && ntag != 3) throw MeshError("element with neither 2 nor 3 tags");
-    for (int t = 0; t < ntag; t++) {
-      long tg = tk.integer();
-      if (t == 0) e.tag0 = (int)tg;
+  };
+  if (binary) {
+    // compressed gmsh (RootProcess::readBin, RootStructure.cpp:61-116): size_t vertex count,
+    // per vertex {int32 id, 3 doubles}; size_t element count, per element {int32 id, int32
+    // type, int32 ntag, ntag int32 tags, the type's int32 one-based vertex ids}
+    ByteReader br{data.data(), data.data() + sz};
+    nv = (long)br.take<uint64_t>();
+    if (nv <= 0 || nv > (sz / 28)) throw MeshError("vertex less than 0");
+    raw.resize(3 * (size_t)nv);
+    for (long i = 0; i < nv; i++) {
+      br.take<int32_t>();
+      for (int d = 0; d < 3; d++) raw[3 * i + d] = br.take<double>();
     }
-    for (int k = 0; k < kNodes[e.type]; k++) {
-      long v = tk.integer() - 1;
-      if (v < 0 || v >= nv) throw MeshError("vertex id out of range");
-      e.v[k] = (int)v;
+    ne = (long)br.take<uint64_t>();
+    if (ne <= 0 || ne > (sz / 12)) throw MeshError("elements of the mesh file less than 0");
+    el.resize((size_t)ne);
+    for (long i = 0; i < ne; i++) {
+      br.take<int32_t>();
+      RawElem& e = el[i];
+      e.type = br.take<int32_t>();
+      int ntag = br.take<int32_t>();
+      check_elem(e, ntag);
+      for (int t = 0; t < ntag; t++) {
+        int32_t tg = br.take<int32_t>();
+        if (t == 0) e.tag0 = tg;
+      }
+      for (int k = 0; k < kNodes[e.type]; k++) {
+        long v = (long)br.take<int32_t>() - 1;
+        if (v < 0 || v >= nv) throw MeshError("vertex id out of range");
+        e.v[k] = (int)v;
+      }
+    }
+  } else {
+    Tokenizer tk{data.data(), data.data() + sz};
+    std::string w;
+    do {
+      if (!tk.word(w)) throw MeshError("no $Nodes section");
+    } while (w != "$Nodes");
+    nv = tk.integer();
+    if (nv <= 0) throw MeshError("vertex less than 0");
+    raw.resize(3 * (size_t)nv);
+    for (long i = 0; i < nv; i++) {
+      tk.integer();
+      raw[3 * i] = tk.real();
+      raw[3 * i + 1] = tk.real();
+      raw[3 * i + 2] = tk.real();
+    }
+    tk.word(w);
+    tk.word(w);
+    ne = tk.integer();
+    if (ne <= 0) throw MeshError("elements of the mesh file less than 0");
+    el.resize((size_t)ne);
+    for (long i = 0; i < ne; i++) {
+      tk.integer();
+      RawElem& e = el[i];
+      e.type = (int)tk.integer();
+      int ntag = (int)tk.integer();
+      check_elem(e, ntag);
+      for (int t = 0; t < ntag; t++) {
+        long tg = tk.integer();
+        if (t == 0) e.tag0 = (int)tg;
+      }
+      for (int k = 0; k < kNodes[e.type]; k++) {
+        long v = tk.integer() - 1;
+        if (v < 0 || v >= nv) throw MeshError("vertex id out of range");
+        e.v[k] = (int)v;
+      }
     }
   }
 
@@ -547,7 +601,7 @@ void init_fields(HostCase& hc) {
   }
 }
 
-void load_case(HostCase& hc, const std::string& paramPath) {
+void load_case(HostCase& hc, const std::string& paramPath, bool msh_binary) {
   load_params(hc, paramPath);
   std::string grid = hc.gridfile;
   if (grid.empty()) throw ParamError("no gridfile line in " + paramPath);
@@ -555,7 +609,7 @@ void load_case(HostCase& hc, const std::string& paramPath) {
     size_t sl = paramPath.find_last_of('/');
     if (sl != std::string::npos) grid = paramPath.substr(0, sl + 1) + grid;
   }
-  load_gmsh(hc, grid);
+  load_gmsh(hc, grid, msh_binary);
   build_faces(hc);
   size_t sl = paramPath.find_last_of('/');
   hc.backup_path = (sl == std::string::npos ? std::string() : paramPath.substr(0, sl + 1)) + "res.sav";

@@ -210,3 +210,33 @@ def write_case(directory, kind, **kw):
     with open(param, "w") as f:
         f.write(text)
     return param
+
+
+def compress_msh(src, dst):
+    """Writes the compressed binary form of a gmsh v2 ASCII file, line by line as the reference's
+    converter does (postCycas.py:compressIn): nothing before ``$Nodes``; a line with one number
+    becomes an int64 (the node and element counts); a node line becomes int32 id + three doubles;
+    an element line becomes its numbers as int32; section markers are dropped.  The result is
+    what ``Case(param, msh_binary=True)`` (RootProcess::readBin) reads."""
+    import struct
+
+    found_node = found_elem = False
+    with open(src) as f, open(dst, "wb") as out:
+        for line in f:
+            if line.startswith("$Nodes"):
+                found_node = True
+                continue
+            if line.startswith("$Elements"):
+                found_elem = True
+                continue
+            if line.startswith("$EndNodes") or line.startswith("$EndElements"):
+                continue
+            nums = line.split()
+            if not found_node or not nums:
+                continue
+            if len(nums) == 1:
+                out.write(struct.pack("<q", int(nums[0])))
+            elif found_elem:
+                out.write(struct.pack("<%di" % len(nums), *[int(x) for x in nums]))
+            else:
+                out.write(struct.pack("<i3d", int(nums[0]), float(nums[1]), float(nums[2]), float(nums[3])))

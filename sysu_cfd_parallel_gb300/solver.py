@@ -29,12 +29,14 @@ _SOLVE_NAMES = ("Un", "Vn", "Wn", "Pn", "Tn", "ED", "?", "?")
 
 
 class Case:
-    """param.in + mesh loaded by the library's host code (no GPU needed)."""
+    """param.in + mesh loaded by the library's host code (no GPU needed); ``msh_binary`` reads
+    the gridfile as the compressed binary gmsh form (the reference's -mshBinary switch)."""
 
-    def __init__(self, param_path: str):
+    def __init__(self, param_path: str, msh_binary: bool = False):
         L = capi.load()
         h = C.c_void_p()
-        capi.check(L.cycas_case_load(param_path.encode(), C.byref(h)))
+        flags = capi.LOAD_MSH_BINARY if msh_binary else 0
+        capi.check(L.cycas_case_load_ex(param_path.encode(), flags, C.byref(h)))
         self._h = h
         d = (C.c_int64 * 8)()
         capi.check(L.cycas_case_dims(h, d))
@@ -205,15 +207,31 @@ class NavierStokesSolver:
         """Sets the cell fields from a restart file (NS/navierIO.cpp:389-404)."""
         capi.check(capi.load().cycas_read_backup(self._h, k, path.encode()))
 
+    def dump_begin(self, tecplot: str | None = None, data: str | None = None, backup: str | None = None,
+                   k: int = 0) -> None:
+        """Starts an asynchronous dump of the current fields to the given files (cycas_dump_begin):
+        the solve may continue at once; ``dump_wait`` collects the status."""
+        kinds = ((capi.DUMP_TECPLOT if tecplot else 0) | (capi.DUMP_DATA if data else 0)
+                 | (capi.DUMP_BACKUP if backup else 0))
+        enc = lambda x: x.encode() if x else None
+        capi.check(capi.load().cycas_dump_begin(self._h, k, self._case_handle(k) if tecplot else None, kinds,
+                                                enc(tecplot), enc(data), enc(backup)))
+
+    def dump_wait(self) -> None:
+        capi.check(capi.load().cycas_dump_wait(self._h))
+
     def NSSolve(self, max_step: int | None = None, residual_steady: float | None = None, callback=None,
-                output_dir: str | None = None, out_binary: bool = False, noutput: int | None = None):
+                output_dir: str | None = None, out_binary: bool = False, noutput: int | None = None,
+                async_output: bool = True):
         """Steady outer loop (NS/navier.cpp:52-141): stop when ResMax < ResidualSteady.
 
         With ``output_dir`` the reference's files are written under it at the reference's
         cadence: the grid before the loop (tec/geo with ``out_binary``, else tec/grid.dat;
         geometry.cpp:209-213); after step s (1-based) with (s - 1) % noutput == 0 the backup
         localGeometryBackup_0/res.sav and tec/data (``out_binary``) or tec/res0000.dat
-        (navier.cpp:113-122, 161-199); after the loop tec/res0000.dat (navier.cpp:149).
+        (navier.cpp:113-122, 161-199); after the loop tec/res0000.dat (navier.cpp:149).  With
+        ``async_output`` the in-loop files are written by asynchronous dumps of the step's fields
+        (same bytes) while the next iterations run.
         """
         import os
 
@@ -235,14 +253,22 @@ class NavierStokesSolver:
             if callback:
                 callback(self.step, rm, self.Residual)
             if output_dir is not None and (step - 1) % nout == 0:
-                self.WriteBackupFile(os.path.join(bak, "res.sav"))
-                if out_binary:
-                    self.Output2TecplotBinary(os.path.join(tec, "data"))
+                backup = os.path.join(bak, "res.sav")
+                data = os.path.join(tec, "data") if out_binary else None
+                res = None if out_binary else os.path.join(tec, "res0000.dat")
+                if async_output:
+                    self.dump_begin(tecplot=res, data=data, backup=backup)
                 else:
-                    self.Output2Tecplot(os.path.join(tec, "res0000.dat"))
+                    self.WriteBackupFile(backup)
+                    if out_binary:
+                        self.Output2TecplotBinary(data)
+                    else:
+                        self.Output2Tecplot(res)
             if rm < tol:
                 break
         if output_dir is not None:
+            if async_output:
+                self.dump_wait()
             self.Output2Tecplot(os.path.join(tec, "res0000.dat"))
         return rm
 

@@ -1,11 +1,13 @@
-"""CPU tests of the result files in the reference's formats (NS/navierIO.cpp).
+"""CPU tests of the mesh and result files in the reference's formats (NS/navierIO.cpp,
+NS/RootStructure.cpp).
 
 The block layout of the Tecplot writer is pinned by known answers written out by hand from
 OutArray2File (navierIO.cpp:2-17); the oracle's Python renderings are checked against those; the
 library's grid writers (host code, no GPU) are then compared byte for byte with the oracle's
-renderings of the oracle's own mesh, and restart files written by the oracle are read back by the
-library's case loader.
+renderings of the oracle's own mesh, restart files written by the oracle are read back by the
+library's case loader, and the compressed binary mesh loads to the same topology as the ASCII one.
 """
+import ctypes as C
 import os
 import shutil
 
@@ -119,3 +121,49 @@ def test_restart_short_backup_fails(tmp_path):
     with pytest.raises(capi.CycasError) as e:
         Case(_restart_copy(tmp_path, "cavity5j", f, 0))
     assert e.value.code == capi.CYCAS_ERR_IO
+
+
+# ---------------------------------------------------------------- compressed binary mesh
+INT_ARRAYS = ["face_cell1", "face_cell2", "face_bnd", "face_vertices", "cell_nface", "cell_face", "cell_cell",
+              "cell_vertices", "cell_rid", "bnd_face", "bnd_rid", "bnd_type", "bnd_vertices"]
+
+
+def _binary_copy(tmp_path, name):
+    from sysu_cfd_parallel_gb300 import meshgen
+
+    d = tmp_path / name
+    shutil.copytree(os.path.join(GOLDEN, name), d, ignore=shutil.ignore_patterns("*.npz"))
+    meshgen.compress_msh(str(d / "case.msh"), str(d / "case.bin"))
+    text = (d / "param.in").read_text().replace("gridfile,case.msh", "gridfile,case.bin")
+    (d / "param.in").write_text(text)
+    return d
+
+
+@pytest.mark.parametrize("name", ["cavity5j", "channel_tiny"])
+def test_binary_mesh_loads_like_ascii(tmp_path, name):
+    a = Case(os.path.join(GOLDEN, name, "param.in"))
+    d = _binary_copy(tmp_path, name)
+    b = Case(str(d / "param.in"), msh_binary=True)
+    assert (a.ncel, a.nfac, a.nbnd, a.nvrt) == (b.ncel, b.nfac, b.nbnd, b.nvrt)
+    assert np.array_equal(a.get_field("vert").view(np.int64), b.get_field("vert").view(np.int64))
+    for nm in INT_ARRAYS:
+        assert np.array_equal(a.get_int(nm), b.get_int(nm)), nm
+    # record layout: int64 count, then 28-byte vertex records
+    raw = (d / "case.bin").read_bytes()
+    assert int(np.frombuffer(raw, dtype="<i8", count=1)[0]) >= a.nvrt
+
+
+def test_binary_mesh_errors(tmp_path):
+    d = _binary_copy(tmp_path, "cavity5j")
+    raw = (d / "case.bin").read_bytes()
+    (d / "case.bin").write_bytes(raw[: len(raw) // 2])
+    with pytest.raises(capi.CycasError) as e:
+        Case(str(d / "param.in"), msh_binary=True)
+    assert e.value.code == capi.CYCAS_ERR_MESH and "truncated" in str(e.value)
+    # the ASCII file read as binary is refused, not misread
+    text = (d / "param.in").read_text().replace("gridfile,case.bin", "gridfile,case.msh")
+    (d / "param.in").write_text(text)
+    with pytest.raises(capi.CycasError):
+        Case(str(d / "param.in"), msh_binary=True)
+    with pytest.raises(capi.CycasError):
+        capi.check(capi.load().cycas_case_load_ex(str(d / "param.in").encode(), 4, C.byref(C.c_void_p())))

@@ -2,9 +2,10 @@
 
 Each file must equal, byte for byte, the oracle's rendering of the same fields read back through
 cycas_get_field: the files then say exactly what the device holds, in the reference's layout.
-NSSolve must write them at the reference's cadence, a batch's case must write the file the case
-writes alone when its fields are the same, and a backup must restart a solve at the values the
-file holds.
+NSSolve must write them at the reference's cadence, an asynchronous dump must write the fields of
+the step it was started at while later iterations run, a batch's case must write the file the
+case writes alone when its fields are the same, and a backup must restart a solve at the values
+the file holds.
 """
 import os
 
@@ -67,25 +68,52 @@ def test_backup_round_trip_restarts_at_file_values(cases, tmp_path):
     assert np.all(np.isfinite(b.get("U")))
 
 
-def test_nssolve_writes_at_the_reference_cadence(cases, tmp_path):
+@pytest.mark.parametrize("async_output", [False, True])
+def test_nssolve_writes_at_the_reference_cadence(cases, tmp_path, async_output):
     p = cases("cavity8")
     s = NavierStokesSolver(Case(p))
-    written = []
+    seen = {}
 
     def note(step, rm, res):
-        written.append((step, os.path.exists(tmp_path / "tec" / "data")))
+        seen[step] = (s.get("U"), os.path.exists(tmp_path / "tec" / "data"))
 
-    s.NSSolve(max_step=5, residual_steady=0.0, callback=note, output_dir=str(tmp_path), out_binary=True, noutput=3)
-    # binary grid before the loop; data after steps 1 and 4; the ASCII result after the loop
+    s.NSSolve(max_step=5, residual_steady=0.0, callback=note, output_dir=str(tmp_path), out_binary=True, noutput=3,
+              async_output=async_output)
+    # binary grid before the loop; data and backup after steps 1 and 4; the ASCII result after the loop
     assert (tmp_path / "tec" / "geo").exists() and not (tmp_path / "tec" / "grid.dat").exists()
-    assert [w for _, w in written] == [False, True, True, True, True]
+    if not async_output:
+        assert [seen[k][1] for k in range(1, 6)] == [False, True, True, True, True]
     f = _fields(s)
     vert, cv = _mesh(p)
     assert (tmp_path / "tec" / "res0000.dat").read_bytes() == po.tecplot_text(vert, cv, f, 0).encode()
-    # the last data and backup files are those of step 4, not of the final step 5
+    # the last data and backup files hold step 4's fields, not the final step's
     d, = results.read_data(str(tmp_path / "tec" / "data"), [s.case.ncel])
-    assert not np.array_equal(d[1], f["U"])
-    assert (tmp_path / "localGeometryBackup_0" / "res.sav").exists()
+    assert np.array_equal(d[1], seen[4][0]) and not np.array_equal(d[1], f["U"])
+    back = results.read_backup(str(tmp_path / "localGeometryBackup_0" / "res.sav"), s.case.ncel, 0)
+    assert np.array_equal(back["U"], np.array([float("%g" % x) for x in seen[4][0]]))
+
+
+def test_async_dump_snapshots_the_fields_of_its_step(cases, tmp_path):
+    p = cases("channel_small")
+    c = Case(p)
+    s = NavierStokesSolver(c)
+    s.set_graph(True)
+    s.iterate(2)
+    f = _fields(s)
+    s.dump_begin(tecplot=str(tmp_path / "a.dat"), data=str(tmp_path / "a.bin"), backup=str(tmp_path / "a.sav"))
+    s.iterate(3)  # the dump's copy-out and formatting overlap these iterations
+    s.dump_wait()
+    vert, cv = _mesh(p)
+    assert (tmp_path / "a.dat").read_bytes() == po.tecplot_text(vert, cv, f, 1).encode()
+    assert (tmp_path / "a.bin").read_bytes() == po.data_bytes(f, 1)
+    assert (tmp_path / "a.sav").read_bytes() == po.backup_text(f, 1).encode()
+    # a dump that cannot write reports it at the wait, and the context stays usable
+    s.dump_begin(data=str(tmp_path / "missing" / "b.bin"))
+    with pytest.raises(capi.CycasError) as e:
+        s.dump_wait()
+    assert e.value.code == capi.CYCAS_ERR_IO
+    s.dump_wait()
+    s.iterate(1)
 
 
 def test_batch_case_writes_what_the_case_writes_alone(cases, tmp_path):
@@ -103,5 +131,8 @@ def test_batch_case_writes_what_the_case_writes_alone(cases, tmp_path):
         alone.Output2TecplotBinary(str(tmp_path / f"alone{k}.bin"))
         assert (tmp_path / f"batch{k}.dat").read_bytes() == (tmp_path / f"alone{k}.dat").read_bytes()
         assert (tmp_path / f"batch{k}.bin").read_bytes() == (tmp_path / f"alone{k}.bin").read_bytes()
+        b.dump_begin(tecplot=str(tmp_path / f"dump{k}.dat"), k=k)
+        b.dump_wait()
+        assert (tmp_path / f"dump{k}.dat").read_bytes() == (tmp_path / f"alone{k}.dat").read_bytes()
     with pytest.raises(capi.CycasError):
         b.Output2TecplotBinary(str(tmp_path / "x.bin"), k=len(params))

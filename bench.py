@@ -119,6 +119,43 @@ def measure_mixed(param, local, warmup, steps, ref_fields, fp64_ms):
             "field_rel_l2_vs_fp64": err}
 
 
+def measure_output(s, stream, steps, plain_ms):
+    """Result files of the headline case (Tecplot ASCII + res.sav backup): the synchronous writers'
+    wall time, and the same files as an asynchronous dump started before `steps` iterations --
+    the iterations' CUDA-event time with the dump in flight against `plain_ms` without it."""
+    import shutil
+    import tempfile
+    import time
+    import torch
+    d = tempfile.mkdtemp(prefix="cycas_out_")
+    try:
+        t0 = time.perf_counter()
+        s.Output2Tecplot(os.path.join(d, "res0000.dat"))
+        s.WriteBackupFile(os.path.join(d, "res.sav"))
+        sync_s = time.perf_counter() - t0
+        nbytes = os.path.getsize(os.path.join(d, "res0000.dat")) + os.path.getsize(os.path.join(d, "res.sav"))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        t0 = time.perf_counter()
+        s.dump_begin(tecplot=os.path.join(d, "a.dat"), backup=os.path.join(d, "a.sav"))
+        begin_ms = (time.perf_counter() - t0) * 1e3
+        s.iterate(steps)
+        e1.record(stream)
+        e1.synchronize()
+        t0 = time.perf_counter()
+        s.dump_wait()
+        wait_s = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {"files": "tec/res0000.dat (Tecplot ASCII) + res.sav", "bytes": int(nbytes),
+            "sync_write_s": sync_s, "async_begin_host_ms": begin_ms,
+            "async_iterations_ms_per_step": ms / steps, "plain_ms_per_step": plain_ms / steps,
+            "async_overhead_ms_per_step": (ms - plain_ms) / steps, "wait_after_iterations_s": wait_s}
+
+
 def measure_batched(local, count, steps, mixed=False):
     """The batched sample against the same cases run one after another as single contexts."""
     import torch
@@ -663,8 +700,9 @@ def run_gpu(args):
     e2e_ms = reduce_max(e2e_ms, device="cuda")
     e2e_value = whole_job_rate(n, e2e_steps, world, e2e_ms)
 
-    mixed = batched = None
+    mixed = batched = output = None
     if not args.no_variants:
+        output = measure_output(s, stream, args.steps, ms)
         mixed = measure_mixed(param, local, args.warmup, args.steps, ref_fields, ms)
         batched = measure_batched(local, BATCH_SAMPLE, args.steps)
 
@@ -697,6 +735,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "mixed": mixed,
             "batched": batched,
+            "output": output,
             "gpu_launches": int(prof["kernel_launches"]),
             "profile": {"krylov_ms": sys_ms, "assembly_ms": prof["assembly_ms"],
                         "krylov_iters": prof["krylov_iters"]},

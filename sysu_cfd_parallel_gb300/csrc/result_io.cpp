@@ -16,7 +16,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <atomic>
+#include <functional>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cycas_host.h"
@@ -44,6 +48,28 @@ void block(std::string& out, const double* a, long n, int stride) {
   out.push_back('\n');
 }
 
+// Renders parts [0, nparts) with part(i, out_i) on up to the host's hardware threads and
+// returns them in order; the text does not depend on the thread count.
+std::vector<std::string> render_parts(int nparts, const std::function<void(int, std::string&)>& part) {
+  std::vector<std::string> out((size_t)nparts);
+  const int nt = std::max(1, std::min(nparts, (int)std::thread::hardware_concurrency()));
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int i = next++; i < nparts; i = next++) part(i, out[(size_t)i]);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  return out;
+}
+
+// cells [lo, hi) of chunk i of n cells cut into `chunks` pieces
+void chunk_range(long n, int chunks, int i, long& lo, long& hi) {
+  lo = n * i / chunks;
+  hi = n * (i + 1) / chunks;
+}
+
 void append_i32(std::string& out, int32_t v) { out.append(reinterpret_cast<const char*>(&v), sizeof v); }
 
 void append_f64(std::string& out, const double* a, long n) {
@@ -64,30 +90,42 @@ std::string tecplot_text(const double* vert, long nvrt, const int32_t* cell_vert
                 "ZONETYPE=FEBRICK\n",
                 nvrt, n, 3 + nvar + 2);
   out += line;
-  out.reserve(out.size() + (size_t)(3 * nvrt + (nvar + 2) * n) * 21 + (size_t)n * 64);
-  for (int d = 0; d < 3; d++) block(out, vert + d, nvrt, 3);
-  block(out, f.P, n, 1);
-  block(out, f.U, n, 1);
-  block(out, f.V, n, 1);
-  block(out, f.W, n, 1);
-  block(out, f.R, n, 1);
-  block(out, f.T, n, 1);
-  std::vector<double> tmp((size_t)n);
-  for (long i = 0; i < n; i++)  // velocity magnitude (constant density)
-    tmp[i] = std::sqrt((f.U[i] * f.U[i] + f.V[i] * f.V[i] + f.W[i] * f.W[i]));
-  block(out, tmp.data(), n, 1);
-  for (long i = 0; i < n; i++) tmp[i] = f.VisLam[i] + f.VisTur[i];
-  block(out, tmp.data(), n, 1);
+  // blocks x y z, P U V W R T, Ma, mu, [TE ED], then the connectivity in chunks of cells; every
+  // block is independent text, rendered in parallel and joined in order
+  std::vector<double> ma((size_t)n), mu((size_t)n);
+  for (long i = 0; i < n; i++) {  // velocity magnitude (constant density); VisLam + VisTur
+    ma[i] = std::sqrt((f.U[i] * f.U[i] + f.V[i] * f.V[i] + f.W[i] * f.W[i]));
+    mu[i] = f.VisLam[i] + f.VisTur[i];
+  }
+  std::vector<const double*> cols = {f.P, f.U, f.V, f.W, f.R, f.T, ma.data(), mu.data()};
   if (f.turb == 1) {
-    block(out, f.TE, n, 1);
-    block(out, f.ED, n, 1);
+    cols.push_back(f.TE);
+    cols.push_back(f.ED);
   }
-  for (long i = 0; i < n; i++) {
-    const int32_t* v = cell_vertices + 8 * i;
-    std::snprintf(line, sizeof line, "%d %d %d %d %d %d %d %d\n ", v[0] + 1, v[1] + 1, v[2] + 1, v[3] + 1,
-                  v[4] + 1, v[5] + 1, v[6] + 1, v[7] + 1);
-    out += line;
-  }
+  const int nblocks = 3 + (int)cols.size(), conn_chunks = 16;
+  std::vector<std::string> parts = render_parts(nblocks + conn_chunks, [&](int i, std::string& o) {
+    if (i < 3) {
+      o.reserve((size_t)nvrt * 21 + 2);
+      block(o, vert + i, nvrt, 3);
+    } else if (i < nblocks) {
+      o.reserve((size_t)n * 21 + 2);
+      block(o, cols[(size_t)(i - 3)], n, 1);
+    } else {
+      long lo, hi;
+      chunk_range(n, conn_chunks, i - nblocks, lo, hi);
+      char ln[256];
+      for (long c = lo; c < hi; c++) {
+        const int32_t* v = cell_vertices + 8 * c;
+        std::snprintf(ln, sizeof ln, "%d %d %d %d %d %d %d %d\n ", v[0] + 1, v[1] + 1, v[2] + 1, v[3] + 1,
+                      v[4] + 1, v[5] + 1, v[6] + 1, v[7] + 1);
+        o += ln;
+      }
+    }
+  });
+  size_t total = out.size();
+  for (auto& p : parts) total += p.size();
+  out.reserve(total);
+  for (auto& p : parts) out += p;
   return out;
 }
 
@@ -139,17 +177,26 @@ std::string data_bytes(const CellFieldsView& f) {
 
 // ostream's default double conversion is printf's %g (six significant digits)
 std::string backup_text(const CellFieldsView& f) {
-  std::string out;
-  char line[512];
-  for (long i = 0; i < f.ncel; i++) {
-    std::snprintf(line, sizeof line, "%g %g %g %g %g %g %g %g\n", f.R[i], f.U[i], f.V[i], f.W[i], f.P[i], f.T[i],
-                  f.R[i], f.VisLam[i]);
-    out += line;
-    if (f.turb == 1) {
-      std::snprintf(line, sizeof line, "%g %g %g\n", f.VisTur[i], f.TE[i], f.ED[i]);
+  const int chunks = 64;
+  std::vector<std::string> parts = render_parts(chunks, [&](int ch, std::string& out) {
+    long lo, hi;
+    chunk_range(f.ncel, chunks, ch, lo, hi);
+    char line[512];
+    for (long i = lo; i < hi; i++) {
+      std::snprintf(line, sizeof line, "%g %g %g %g %g %g %g %g\n", f.R[i], f.U[i], f.V[i], f.W[i], f.P[i],
+                    f.T[i], f.R[i], f.VisLam[i]);
       out += line;
+      if (f.turb == 1) {
+        std::snprintf(line, sizeof line, "%g %g %g\n", f.VisTur[i], f.TE[i], f.ED[i]);
+        out += line;
+      }
     }
-  }
+  });
+  std::string out;
+  size_t total = 0;
+  for (auto& p : parts) total += p.size();
+  out.reserve(total);
+  for (auto& p : parts) out += p;
   return out;
 }
 

@@ -94,6 +94,10 @@ void cycas_case_free(cycas_case* c);
 int cycas_case_dims(const cycas_case* c, int64_t dims[8]);
 /* residual stop value and relaxation factors of the case (dbOptions, NS/navier.cpp:777-791) */
 int cycas_case_params(const cycas_case* c, double* residual_steady, double urf[8], double gravity[3]);
+/* time and physics switches of the case: iopt = {IfSteady, TimeScheme, MaxOuterStep, SolveEnergy,
+ * DensityModel, MaxStep}, dopt = {dt, total_time, PressureReference} (the "steady"/"transient",
+ * "energy", "density" and "PressureRef" keys, NS/readparamfile.cpp:76-140) */
+int cycas_case_physics(const cycas_case* c, int32_t iopt[6], double dopt[3]);
 /* integer topology arrays by name (face_cell1, face_cell2, face_bnd, face_vertices, cell_nface,
  * cell_face, cell_cell, cell_vertices, cell_rid, bnd_face, bnd_rid, bnd_type, bnd_vertices) */
 int cycas_case_get_int(const cycas_case* c, const char* name, int32_t* dst, int64_t n);
@@ -143,10 +147,17 @@ typedef struct {
 
 typedef struct {
   int32_t turb_model;        /* TurModel: 0 laminar, 1 k-epsilon */
-  int32_t density_model;     /* must be 0 (constant density) */
+  int32_t density_model;     /* DensityModel: 0 constant density, 1 perfect gas (energy is then solved) */
   int32_t cell_pressure_ref; /* cellPressureRef */
   double urf[8];             /* URF[0..7] */
   double gravity[3];
+  /* fields below: zero selects the steady, isothermal defaults */
+  int32_t transient;          /* 0 steady (IfSteady); 1 transient (the "transient" key) */
+  int32_t time_scheme;        /* TimeScheme: 1 Euler, 2 the reference's "Dual" second-order form */
+  double dt;                  /* time step */
+  int32_t max_outer;          /* MaxOuterStep: a time step runs at most max_outer - 1 outer iterations */
+  int32_t solve_energy;       /* SolveEnergy */
+  double pressure_reference;  /* PressureReference (perfect gas; <= 0: 1.01325e5) */
 } cycas_params;
 
 typedef struct {
@@ -191,6 +202,16 @@ void cycas_destroy(cycas_ctx* ctx);
 int cycas_get_field(cycas_ctx* ctx, const char* name, double* dst, int64_t n);
 int cycas_set_field(cycas_ctx* ctx, const char* name, const double* src, int64_t n);
 int cycas_get_int(cycas_ctx* ctx, const char* name, int32_t* dst, int64_t n); /* A_rowptr, A_col */
+
+/* One physical time step of a transient context (NS/navier.cpp:52-111): SaveTransientOldData
+ * (navier.cpp:698-740), the clock advanced by dt, then outer SIMPLE iterations (momentum,
+ * pressure, k-epsilon, energy) until ResMax0 / ResMax > 100 or max_outer - 1 of them ran.
+ * For outer iteration k < cap: res_hist[10k..] its residuals, resmax[k] its ResMax,
+ * its[8k..] / reasons[8k..] its Krylov solves (unused slots -1).  *n_outer receives the number
+ * of outer iterations, *cur_time the clock after the step.  A Krylov failure ends the step with
+ * CYCAS_NOT_CONVERGED (its outer iteration recorded). */
+int cycas_time_step(cycas_ctx* ctx, int32_t cap, int32_t* n_outer, double* res_hist, double* resmax, int32_t* its,
+                    int32_t* reasons, double* cur_time);
 
 typedef struct {
   int32_t its[8];      /* Krylov iterations of each solve of the iteration, in call order */

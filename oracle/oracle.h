@@ -1,7 +1,8 @@
 // CPU ORACLE — TEST INFRASTRUCTURE ONLY.
 //
 // A single-rank C++ restatement of the Cycas2Parallel (Meiyim/SYSU_CFD_Parallel)
-// steady SIMPLE solve, written from the reference's behaviour, used only by
+// SIMPLE solve (steady and transient, constant density or perfect gas, k-epsilon and
+// energy), written from the reference's behaviour, used only by
 // tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm
 // as the checker.  Nothing in the product links or calls it.
 //
@@ -124,7 +125,14 @@ struct Case {
 
   // k-epsilon work arrays kept for inspection (navier_scalar.cpp:21-27)
   std::vector<double> Prod, TESource, EDSource, ApTE, ApED;
+  // energy work arrays kept for inspection (navier_scalar.cpp:209-217)
+  std::vector<double> kcond, ESource, ApE;
   int reverseInletWarnings = 0;
+
+  // transient runs (navier.h:136-150): previous time levels and the clock
+  std::vector<double> Rnp, Unp, Vnp, Wnp, Tnp, TEp, EDp;
+  std::vector<double> Rnp2, Unp2, Vnp2, Wnp2, Tnp2, TEp2, EDp2;
+  double cur_time = 0.;
 };
 
 // setup (mesh + params + init), following main.cpp:38-65 at one rank
@@ -135,6 +143,15 @@ void build_pattern(Case& cs);
 
 // one SIMPLE iteration of NSSolve (navier.cpp:60-111); returns ResMax
 double simple_iteration(Case& cs);
+// one physical time step of a transient run (navier.cpp:52-111): SaveTransientOldData, then
+// outer iterations until the residual has dropped by a factor 100 or MaxOuterStep - 1 of them
+// ran; resmax[k] is the ResMax of outer iteration k.  Returns the number of outer iterations.
+int time_step(Case& cs, std::vector<double>* resmax, std::vector<double>* residuals,
+              std::vector<KspResult>* ksp);
+void save_transient_old_data(Case& cs);
+void set_bc_temperature(Case& cs);
+void update_energy(Case& cs);
+void build_energy(Case& cs);
 
 // stages
 void set_bc_velocity(Case& cs);

@@ -63,6 +63,17 @@ std::vector<double>* field(Case& cs, const std::string& nm) {
   if (nm == "ApTE") return &cs.ApTE;
   if (nm == "ApED") return &cs.ApED;
   if (nm == "vert") return &cs.Vert;
+  if (nm == "BTem") return &cs.BTem;
+  if (nm == "kcond") return &cs.kcond;
+  if (nm == "ESource") return &cs.ESource;
+  if (nm == "ApE") return &cs.ApE;
+  if (nm == "Rnp") return &cs.Rnp;
+  if (nm == "Unp") return &cs.Unp;
+  if (nm == "Vnp") return &cs.Vnp;
+  if (nm == "Wnp") return &cs.Wnp;
+  if (nm == "Tnp") return &cs.Tnp;
+  if (nm == "TEp") return &cs.TEp;
+  if (nm == "EDp") return &cs.EDp;
   return nullptr;
 }
 }  // namespace
@@ -256,6 +267,9 @@ int orc_stage(void* hp, const char* name) {
     else if (s == "calculate_velocity") calculate_velocity(cs);
     else if (s == "calculate_pressure") calculate_pressure(cs);
     else if (s == "keps") update_tur_kepsilon(cs);
+    else if (s == "build_energy") build_energy(cs);
+    else if (s == "energy") update_energy(cs);
+    else if (s == "save_transient") save_transient_old_data(cs);
     else if (s == "clear_residual") {
       for (int i = 0; i < RESIDUAL_LEN; i++) cs.localRes[i] = cs.Residual[i] = 0.0;
     } else {
@@ -291,6 +305,42 @@ int orc_iterate(void* hp, int nsteps, double* res_hist, double* resmax, int* ksp
     }
   }
   return nsteps;
+}
+
+// physics switches: iopt = {IfSteady, TimeScheme, MaxOuterStep, SolveEnergy, DensityModel, MaxStep},
+// dopt = {dt, total_time, cur_time, PressureReference}
+int orc_physics(void* hp, int* iopt, double* dopt) {
+  Case& cs = ((Handle*)hp)->cs;
+  int iv[6] = {cs.IfSteady, cs.TimeScheme, cs.MaxOuterStep, cs.SolveEnergy, cs.DensityModel, cs.MaxStep};
+  double dv[4] = {cs.dt, cs.total_time, cs.cur_time, cs.PressureReference};
+  if (iopt) std::memcpy(iopt, iv, sizeof iv);
+  if (dopt) std::memcpy(dopt, dv, sizeof dv);
+  return 0;
+}
+
+// One physical time step of a transient case.  Up to `cap` outer iterations are recorded:
+// resmax[k], res_hist[10k..], ksp_its / ksp_reason [8k..].  Returns the number of outer
+// iterations, or <0 on error.
+int orc_time_step(void* hp, int cap, double* resmax, double* res_hist, int* ksp_its, int* ksp_reason) {
+  Case& cs = ((Handle*)hp)->cs;
+  try {
+    std::vector<double> rm, rh;
+    std::vector<KspResult> kl;
+    int n = time_step(cs, &rm, &rh, &kl);
+    for (int k = 0; k < n && k < cap; k++) {
+      if (resmax) resmax[k] = rm[k];
+      if (res_hist)
+        for (int i = 0; i < RESIDUAL_LEN; i++) res_hist[k * RESIDUAL_LEN + i] = rh[k * RESIDUAL_LEN + i];
+      for (int q = 0; q < 8; q++) {
+        if (ksp_its) ksp_its[k * 8 + q] = kl[k * 8 + q].its;
+        if (ksp_reason) ksp_reason[k * 8 + q] = kl[k * 8 + q].reason;
+      }
+    }
+    return n;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
 }
 
 // standalone Krylov solve on an arbitrary CSR system (for solver unit tests)

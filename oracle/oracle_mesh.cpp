@@ -78,8 +78,16 @@ void read_param_file(Case& cs, const std::string& path) {
       cs.IfSteady = 1;
       cs.MaxStep = std::atoi(k[1]);
       cs.ResidualSteady = std::atof(k[2]);
-    } else if (!std::strcmp(k[0], "transient")) {
-      fail("transient runs are not on the steady SIMPLE path");
+    } else if (!std::strcmp(k[0], "transient")) {  // readparamfile.cpp:84-101
+      if (ikey != 4) fail("transient requies 3 parameters");
+      cs.IfSteady = 0;
+      cs.dt = std::atof(k[1]);
+      cs.total_time = std::atof(k[2]);
+      cs.MaxStep = (int)(cs.total_time / cs.dt);
+      cs.MaxOuterStep = (int)std::atof(k[3]);
+      if (!std::strcmp(k[4], "Euler")) cs.TimeScheme = 1;
+      else if (!std::strcmp(k[4], "Dual")) cs.TimeScheme = 2;
+      else fail(std::string("unknown time scheme: ") + k[4]);
     } else if (!std::strcmp(k[0], "energy")) {
       if (!std::strcmp(k[1], "on")) cs.SolveEnergy = 1;
       else if (!std::strcmp(k[1], "off")) cs.SolveEnergy = 0;
@@ -477,6 +485,10 @@ void read_grid_and_build(Case& cs, const std::string& meshPath) {
     cs.TE.assign(n, 0.0);
     cs.ED.assign(n, 0.0);
   }
+  if (!cs.IfSteady)
+    for (auto* v : {&cs.Rnp, &cs.Unp, &cs.Vnp, &cs.Wnp, &cs.Tnp, &cs.TEp, &cs.EDp, &cs.Rnp2, &cs.Unp2, &cs.Vnp2,
+                    &cs.Wnp2, &cs.Tnp2, &cs.TEp2, &cs.EDp2})
+      v->assign(n, 0.0);
   for (auto* v : {&cs.dPdX, &cs.dUdX, &cs.dVdX, &cs.dWdX, &cs.dPhidX}) v->assign(3 * n, 0.0);
   for (auto* v : {&cs.BRo, &cs.BU, &cs.BV, &cs.BW, &cs.BPre, &cs.BTem, &cs.BTE, &cs.BED}) v->assign(cs.Nbnd, 0.0);
   cs.RUFace.assign(cs.Nfac, 0.0);

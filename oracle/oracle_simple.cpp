@@ -1,5 +1,6 @@
 // CPU ORACLE — TEST INFRASTRUCTURE ONLY (see oracle.h; parity unpinned at the PETSc boundary).
-// One steady SIMPLE iteration of NavierStokesSolver::NSSolve restated at one rank.
+// One SIMPLE iteration of NavierStokesSolver::NSSolve restated at one rank (steady or one outer
+// iteration of a transient step; constant density or perfect gas; k-epsilon; energy).
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
@@ -142,7 +143,7 @@ void gradient(Case& cs, const double* phi, const double* Bphif, double* g) {
     for (int d = 0; d < 3; d++) g[3 * i + d] /= cs.C[i].vol;
 }
 
-// BuildVelocityMatrix (navier_velocity.cpp:63-393), steady
+// BuildVelocityMatrix (navier_velocity.cpp:63-393)
 void build_velocity_matrix(Case& cs) {
   set_bc_velocity(cs);
   set_bc_pressure(cs);
@@ -158,6 +159,21 @@ void build_velocity_matrix(Case& cs) {
     double app = 0., su = 0., sv = 0., sw = 0., apn[6] = {0, 0, 0, 0, 0, 0};
     int ani[6], nj = 0;
     double fcs[3] = {0., 0., 0.}, fde[3], fdi[3];
+    if (!cs.IfSteady) {  // unsteady terms (navier_velocity.cpp:108-123)
+      if (cs.TimeScheme == 1) {
+        double coef = cs.Rn[i] / cs.dt * ci.vol;
+        app += coef;
+        su += coef * cs.Unp[i];
+        sv += coef * cs.Vnp[i];
+        sw += coef * cs.Wnp[i];
+      } else if (cs.TimeScheme == 2) {
+        double coef = cs.Rn[i] / cs.dt * ci.vol;
+        app += 1.5 * coef;
+        su += coef * (2 * cs.Unp[i] - 0.5 * cs.Unp2[i]);
+        sv += coef * (2 * cs.Vnp[i] - 0.5 * cs.Vnp2[i]);
+        sw += coef * (2 * cs.Wnp[i] - 0.5 * cs.Wnp2[i]);
+      }
+    }
     for (int j = 0; j < ci.nface; j++) {
       int iface = ci.face[j];
       const Face& f = cs.F[iface];
@@ -347,27 +363,63 @@ void cal_ruface2(Case& cs) {
   }
 }
 
-// BuildPressureMatrix (navier_pressure.cpp:99-232), DensityModel 0
+// BuildPressureMatrix (navier_pressure.cpp:99-232)
 void build_pressure_matrix(Case& cs) {
-  if (cs.DensityModel != 0) throw std::runtime_error("only constant density is on the measured path");
+  if (cs.DensityModel != 0 && cs.DensityModel != 1) throw std::runtime_error("unknown DensityModel found");
+  const bool gas = cs.DensityModel == 1;
   for (int i = 0; i < cs.Ncel; i++) {
     const Cell& ci = cs.C[i];
     double valcen = 0., bpv = 0., Acn[7];
     int cn[7], nj = 0;
+    if (!cs.IfSteady && gas) valcen += -ci.vol / (cs.dt * cs.Rcpcv * cs.Tn[i]);
     for (int j = 0; j < ci.nface; j++) {
       int iface = ci.face[j];
       const Face& f = cs.F[iface];
       if (i == f.cell1) bpv += cs.RUFace[iface];
       else bpv -= cs.RUFace[iface];
       int in = ci.cell[j];
-      if (in < 0) continue;
-      double lambda = (i == f.cell1) ? f.lambda : 1. - f.lambda;
+      if (in < 0) {
+        if (!gas) continue;
+        int bnd = f.bnd;
+        int t = type1Of(cs, cs.B[bnd].rid);
+        double RUnormal = cs.RUFace[iface];
+        if (t == 2) {  // inlet
+          double rof = cs.BRo[bnd], Tf = cs.Tn[i];
+          valcen += dmin(RUnormal, 0.) / (rof * cs.Rcpcv * Tf);
+        } else if (t == 3) {  // outlet
+          double rof = cs.Rn[i], Tf = cs.Tn[i];
+          valcen += (RUnormal > 0. ? RUnormal : 0.) / (rof * cs.Rcpcv * Tf);  // CYCASMAX
+        }
+        continue;
+      }
+      double lambda, RUnormal;
+      if (i == f.cell1) {
+        lambda = f.lambda;
+        RUnormal = cs.RUFace[iface];
+      } else {
+        lambda = 1. - f.lambda;
+        RUnormal = -cs.RUFace[iface];
+      }
       double lambda2 = 1. - lambda;
       double roapf = cs.Rn[i] * cs.Apr[i] * lambda + cs.Rn[in] * cs.Apr[in] * lambda2;
       double vol = ci.vol * lambda + cs.C[in].vol * lambda2;
       double tmp = roapf * vol * f.rlencos;
       valcen += -tmp;
-      Acn[nj] = tmp;
+      if (!gas) {
+        Acn[nj] = tmp;
+      } else {
+        double rof = lambda * cs.Rn[i] + lambda2 * cs.Rn[in];
+        if (RUnormal > 0.) {
+          double Tf = cs.Tn[i];
+          double tmp2 = -RUnormal / (rof * cs.Rcpcv * Tf);
+          valcen += tmp2;
+        }
+        Acn[nj] = tmp;
+        if (RUnormal < 0.) {
+          double Tf = cs.Tn[in];
+          Acn[nj] += -RUnormal / (rof * cs.Rcpcv * Tf);
+        }
+      }
       cn[nj] = cs.C[in].globalIdx;
       nj++;
     }
@@ -378,12 +430,17 @@ void build_pressure_matrix(Case& cs) {
   }
 }
 
-// pressure and velocity correction (navier_pressure.cpp:45-70), DensityModel 0
+// pressure (and density) and velocity correction (navier_pressure.cpp:45-70)
 void correct_cells(Case& cs) {
   double ref = cs.deltaP[cs.cellPressureRef];  // root rank value; MPI_Bcast at one rank is the identity
   for (int i = 0; i < cs.Ncel; i++) {
     cs.localRes[3] += std::fabs(cs.deltaP[i] - ref) * cs.C[i].vol;
-    cs.Pn[i] += cs.URF[3] * (cs.deltaP[i] - ref);
+    if (cs.DensityModel == 0) {
+      cs.Pn[i] += cs.URF[3] * (cs.deltaP[i] - ref);
+    } else if (cs.DensityModel == 1) {  // perfect gas
+      cs.Pn[i] += cs.URF[3] * cs.deltaP[i];
+      cs.Rn[i] += cs.deltaP[i] / (cs.Rcpcv * cs.Tn[i]);
+    }
     double coef = cs.C[i].vol * cs.Apr[i];
     cs.Un[i] -= coef * cs.dPdX[3 * i];
     cs.Vn[i] -= coef * cs.dPdX[3 * i + 1];
@@ -391,7 +448,7 @@ void correct_cells(Case& cs) {
   }
 }
 
-// CorrectRUFace2 (navier_pressure.cpp:235-278), DensityModel 0
+// CorrectRUFace2 (navier_pressure.cpp:235-278)
 void correct_ruface2(Case& cs) {
   const double* dp = cs.deltaP.data();
   for (int i = 0; i < cs.Nfac; i++) {
@@ -406,6 +463,11 @@ void correct_ruface2(Case& cs) {
     double lambda = f.lambda, lambda2 = 1. - lambda, dx1[3], dx2[3];
     vminus(dx1, f.Xpac, cs.C[c1].x);
     vminus(dx2, f.Xnac, cs.C[c2].x);
+    if (cs.DensityModel == 1) {  // ro'*u
+      double rop = dp[c1] / (cs.Rcpcv * cs.Tn[c1]) * lambda + dp[c2] / (cs.Rcpcv * cs.Tn[c2]) * lambda2;
+      double rof = cs.Rn[c1] * lambda + cs.Rn[c2] * lambda2;
+      cs.RUFace[i] += cs.RUFace[i] * rop / rof;
+    }
     double roapf = cs.Rn[c1] * cs.Apr[c1] * lambda + cs.Rn[c2] * cs.Apr[c2] * lambda2;
     double vol = cs.C[c1].vol * lambda + cs.C[c2].vol * lambda2;
     double coef = roapf * vol * f.rlencos;
@@ -416,8 +478,9 @@ void correct_ruface2(Case& cs) {
 }
 
 static void solve_or_throw(Case& cs, const Csr& A, int which, double tol, int maxit, bool guess_zero,
-                           const double* b, double* x, const char* name) {
-  const KspSettings& s = cs.ksp[which];
+                           const double* b, double* x, const char* name, int force_type = -1) {
+  KspSettings s = cs.ksp[which];
+  if (force_type >= 0) s.type = force_type;
   double rtol = s.rtol_override > 0 ? s.rtol_override : tol;
   int mi = s.maxit_override > 0 ? s.maxit_override : maxit;
   KspResult r = ksp_solve(A, s, rtol, mi, guess_zero, b, x);
@@ -449,7 +512,9 @@ int calculate_pressure(Case& cs) {
   set_bc_velocity(cs);
   cal_ruface2(cs);
   build_pressure_matrix(cs);
-  solve_or_throw(cs, cs.Ap, 1, 1.e-6, 1000, true, cs.bp.data(), cs.deltaP.data(), "Pn");
+  // CG for the symmetric constant-density system, GMRES otherwise (MPIStructure.cpp:462-467)
+  solve_or_throw(cs, cs.Ap, 1, 1.e-6, 1000, true, cs.bp.data(), cs.deltaP.data(), "Pn",
+                 cs.DensityModel == 0 ? -1 : (int)KSP_GMRES);
   cs.Ap.zero();
   set_bc_deltap(cs);
   gradient(cs, cs.deltaP.data(), cs.BPre.data(), cs.dPdX.data());
@@ -459,7 +524,7 @@ int calculate_pressure(Case& cs) {
   return 0;
 }
 
-// BuildScalarMatrix (navier_scalar.cpp:407-592), steady
+// BuildScalarMatrix (navier_scalar.cpp:407-592)
 void build_scalar_matrix(Case& cs, int iSca, double* Phi, double* BPhi, double* DiffCoef, double* source, double* App) {
   (void)iSca;
   double* dP = cs.dPhidX.data();
@@ -551,7 +616,7 @@ void build_scalar_matrix(Case& cs, int iSca, double* Phi, double* BPhi, double* 
   }
 }
 
-// UpdateTurKEpsilon (navier_scalar.cpp:11-197) with SetBCKEpsilon (navier_bc.cpp:220-345), steady
+// UpdateTurKEpsilon (navier_scalar.cpp:11-197) with SetBCKEpsilon (navier_bc.cpp:220-345)
 void update_tur_kepsilon(Case& cs) {
   const double kappa = 0.419, Cmu = 0.09, Ceps1 = 1.44, Ceps2 = 1.92, Sigma_k = 1.0, Sigma_e = 1.3;
   int n = cs.Ncel;
@@ -613,6 +678,22 @@ void update_tur_kepsilon(Case& cs) {
       cs.BED[i] = cs.ED[ic];
     }
 
+  if (!cs.IfSteady) {  // unsteady terms (navier_scalar.cpp:71-90)
+    for (int i = 0; i < n; i++) {
+      double coef = cs.Rn[i] / cs.dt * cs.C[i].vol;
+      if (cs.TimeScheme == 1) {
+        ApTE[i] += coef;
+        TES[i] += coef * cs.TEp[i];
+        ApED[i] += coef;
+        EDS[i] += coef * cs.EDp[i];
+      } else if (cs.TimeScheme == 2) {
+        ApTE[i] += 1.5 * coef;
+        TES[i] += coef * (2 * cs.TEp[i] - 0.5 * cs.TEp2[i]);
+        ApED[i] += 1.5 * coef;
+        EDS[i] += coef * (2 * cs.EDp[i] - 0.5 * cs.EDp2[i]);
+      }
+    }
+  }
   build_scalar_matrix(cs, 2, cs.TE.data(), cs.BTE.data(), VisTE.data(), TES, ApTE);
   solve_or_throw(cs, cs.As, 2, 1.e-8, 500, false, cs.bs.data(), cs.TE.data(), "Tn");
   cs.As.zero();
@@ -647,7 +728,151 @@ void update_tur_kepsilon(Case& cs) {
   }
 }
 
-// one pass of the steady outer loop (navier.cpp:60-111)
+// SetBCTemperature (navier_bc.cpp:183-213): walls and inlets keep their values
+void set_bc_temperature(Case& cs) {
+  for (int i = 0; i < cs.Nbnd; i++) {
+    int ic = cs.F[cs.B[i].face].cell1;
+    int t = type1Of(cs, cs.B[i].rid);
+    if (t == 3 || t == 4) cs.BTem[i] = cs.Tn[ic];
+    else if (t != 1 && t != 2) throw std::runtime_error("no such boundary type");
+  }
+}
+
+// UpdateEnergy (navier_scalar.cpp:204-326) up to the assembled system (As, bs)
+void build_energy(Case& cs) {
+  const int n = cs.Ncel;
+  cs.kcond.assign(n, 0.0);
+  cs.ESource.assign(n, 0.0);
+  cs.ApE.assign(n, 0.0);
+  double *kcond = cs.kcond.data(), *ES = cs.ESource.data(), *ApE = cs.ApE.data();
+  for (int i = 0; i < n; i++) kcond[i] = cs.cp * (cs.VisLam[i] / cs.prl + cs.VisTur[i] / cs.prte) / cs.cp;
+  if (cs.DensityModel == 1) {  // work of the viscous stresses, face by face
+    const double* dU = cs.dUdX.data();
+    const double* dV = cs.dVdX.data();
+    const double* dW = cs.dWdX.data();
+    for (int i = 0; i < cs.Nfac; i++) {
+      const Face& f = cs.F[i];
+      int c1 = f.cell1, c2 = f.cell2;
+      double VisL, VisT, dudx, dudy, dudz, dvdx, dvdy, dvdz, dwdx, dwdy, dwdz, vxg, vyg, vzg;
+      if (c2 < 0) {
+        VisL = cs.VisLam[c1];
+        VisT = cs.VisTur[c1];
+        dudx = dU[3 * c1]; dudy = dU[3 * c1 + 1]; dudz = dU[3 * c1 + 2];
+        dvdx = dV[3 * c1]; dvdy = dV[3 * c1 + 1]; dvdz = dV[3 * c1 + 2];
+        dwdx = dW[3 * c1]; dwdy = dW[3 * c1 + 1]; dwdz = dW[3 * c1 + 2];
+        vxg = cs.Un[c1];
+        vyg = cs.Vn[c1];
+        vzg = cs.Wn[c1];
+      } else {
+        double lambda = f.lambda, lambda2 = 1. - lambda;
+        VisL = lambda * cs.VisLam[c1] + lambda2 * cs.VisLam[c2];
+        VisT = lambda * cs.VisTur[c1] + lambda2 * cs.VisTur[c2];
+        dudx = lambda * dU[3 * c1] + lambda2 * dU[3 * c2];
+        dudy = lambda * dU[3 * c1 + 1] + lambda2 * dU[3 * c2 + 1];
+        dudz = lambda * dU[3 * c1 + 2] + lambda2 * dU[3 * c2 + 2];
+        dvdx = lambda * dV[3 * c1] + lambda2 * dV[3 * c2];
+        dvdy = lambda * dV[3 * c1 + 1] + lambda2 * dV[3 * c2 + 1];
+        dvdz = lambda * dV[3 * c1 + 2] + lambda2 * dV[3 * c2 + 2];
+        dwdx = lambda * dW[3 * c1] + lambda2 * dW[3 * c2];
+        dwdy = lambda * dW[3 * c1 + 1] + lambda2 * dW[3 * c2 + 1];
+        dwdz = lambda * dW[3 * c1 + 2] + lambda2 * dW[3 * c2 + 2];
+        vxg = lambda * cs.Un[c1] + lambda2 * cs.Un[c2];
+        vyg = lambda * cs.Vn[c1] + lambda2 * cs.Vn[c2];
+        vzg = lambda * cs.Wn[c1] + lambda2 * cs.Wn[c2];
+      }
+      double vmul = VisL + VisT;
+      double vlac = -2. / 3. * vmul;
+      double div = dudx + dvdy + dwdz;
+      double txx = 2. * vmul * dudx + vlac * div;
+      double tyy = 2. * vmul * dvdy + vlac * div;
+      double tzz = 2. * vmul * dwdz + vlac * div;
+      double txy = vmul * (dudy + dvdx);
+      double txz = vmul * (dudz + dwdx);
+      double tyz = vmul * (dvdz + dwdy);
+      double btx = vxg * txx + vyg * txy + vzg * txz;
+      double bty = vxg * txy + vyg * tyy + vzg * tyz;
+      double btz = vxg * txz + vyg * tyz + vzg * tzz;
+      double fvis = (btx * f.n[0] + bty * f.n[1] + btz * f.n[2]) / cs.cp;
+      ES[c1] += fvis;
+      if (c2 >= 0) ES[c2] -= fvis;
+    }
+  }
+  set_bc_temperature(cs);
+  if (!cs.IfSteady) {
+    for (int i = 0; i < n; i++) {
+      double coef = cs.Rn[i] / cs.dt * cs.C[i].vol;
+      if (cs.TimeScheme == 1) {
+        ApE[i] += coef;
+        ES[i] += coef * cs.Tnp[i];
+      } else if (cs.TimeScheme == 2) {
+        ApE[i] += 1.5 * coef;
+        ES[i] += coef * (2 * cs.Tnp[i] - 0.5 * cs.Tnp2[i]);
+      }
+    }
+  }
+  build_scalar_matrix(cs, 1, cs.Tn.data(), cs.BTem.data(), kcond, ES, ApE);
+}
+
+void update_energy(Case& cs) {
+  build_energy(cs);
+  solve_or_throw(cs, cs.As, 2, 1.e-8, 500, false, cs.bs.data(), cs.Tn.data(), "Energy");
+  cs.As.zero();
+}
+
+// SaveTransientOldData (navier.cpp:698-740).  The second-order branch assigns both previous
+// levels from the current one (Unp2 = Unp = Un), so the two levels are always equal.
+void save_transient_old_data(Case& cs) {
+  const int n = cs.Ncel;
+  const bool ke = cs.TurModel == 1;
+  if (cs.TimeScheme == 1) {
+    for (int i = 0; i < n; i++) {
+      cs.Rnp[i] = cs.Rn[i];
+      cs.Unp[i] = cs.Un[i];
+      cs.Vnp[i] = cs.Vn[i];
+      cs.Wnp[i] = cs.Wn[i];
+      cs.Tnp[i] = cs.Tn[i];
+      if (ke) {
+        cs.TEp[i] = cs.TE[i];
+        cs.EDp[i] = cs.ED[i];
+      }
+    }
+  } else if (cs.TimeScheme == 2) {
+    for (int i = 0; i < n; i++) {
+      cs.Rnp2[i] = cs.Rnp[i] = cs.Rn[i];
+      cs.Unp2[i] = cs.Unp[i] = cs.Un[i];
+      cs.Vnp2[i] = cs.Vnp[i] = cs.Vn[i];
+      cs.Wnp2[i] = cs.Wnp[i] = cs.Wn[i];
+      cs.Tnp2[i] = cs.Tnp[i] = cs.Tn[i];
+      if (ke) {
+        cs.TEp2[i] = cs.TEp[i] = cs.TE[i];
+        cs.EDp2[i] = cs.EDp[i] = cs.ED[i];
+      }
+    }
+  } else {
+    throw std::runtime_error("No unsteady time advance scheme");
+  }
+}
+
+int time_step(Case& cs, std::vector<double>* resmax, std::vector<double>* residuals, std::vector<KspResult>* ksp) {
+  if (cs.IfSteady) throw std::runtime_error("time_step needs a transient case");
+  save_transient_old_data(cs);
+  cs.cur_time += cs.dt;
+  double ResMax0 = 0.;
+  int iter;
+  for (iter = 1; iter < cs.MaxOuterStep; iter++) {
+    double ResMax = simple_iteration(cs);
+    if (resmax) resmax->push_back(ResMax);
+    if (residuals) residuals->insert(residuals->end(), cs.Residual, cs.Residual + RESIDUAL_LEN);
+    if (ksp) {
+      for (int k = 0; k < 8; k++) ksp->push_back(k < (int)cs.kspLog.size() ? cs.kspLog[k] : KspResult{-1, -1, 0});
+    }
+    if (iter == 1) ResMax0 = ResMax;
+    if (ResMax0 / (ResMax + 1.e-16) > 100.) break;
+  }
+  return iter < cs.MaxOuterStep ? iter : std::max(0, cs.MaxOuterStep - 1);
+}
+
+// one pass of the outer loop (navier.cpp:60-111)
 double simple_iteration(Case& cs) {
   std::fill(cs.localRes, cs.localRes + RESIDUAL_LEN, 0.0);
   std::fill(cs.Residual, cs.Residual + RESIDUAL_LEN, 0.0);
@@ -655,6 +880,7 @@ double simple_iteration(Case& cs) {
   calculate_velocity(cs);
   calculate_pressure(cs);
   if (cs.TurModel == 1) update_tur_kepsilon(cs);
+  if (cs.SolveEnergy) update_energy(cs);
   for (int i = 0; i < RESIDUAL_LEN; i++) cs.Residual[i] = cs.localRes[i];
   double s = 0.;
   for (int i = 0; i < RESIDUAL_LEN; i++) s = s > cs.Residual[i] ? s : cs.Residual[i];  // vec_max, tools.cpp:45-51

@@ -47,6 +47,8 @@ def lib():
         L.orc_set_ksp_perm.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_long]
         L.orc_stage.argtypes = [C.c_void_p, C.c_char_p]
         L.orc_iterate.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_physics.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_time_step.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_csr_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                     C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
@@ -93,7 +95,7 @@ class OracleCase:
             "dUdX": 3 * n, "dVdX": 3 * n, "dWdX": 3 * n, "dPdX": 3 * n, "dPhidX": 3 * n,
             "BRo": b, "BU": b, "BV": b, "BW": b, "BPre": b, "BTE": b, "BED": b,
             "Au_val": self.nnz, "Ap_val": self.nnz, "As_val": self.nnz, "residual": 10,
-            "vert": 3 * self.nvrt,
+            "vert": 3 * self.nvrt, "BTem": b,
             "face_cell1": f, "face_cell2": f, "face_bnd": f, "face_vertices": 4 * f,
             "cell_nface": n, "cell_rid": n, "cell_face": 6 * n, "cell_cell": 6 * n, "cell_vertices": 8 * n,
             "bnd_face": b, "bnd_rid": b, "bnd_type": b, "bnd_vertices": 4 * b,
@@ -138,6 +140,26 @@ class OracleCase:
         rc = lib().orc_stage(self.h, name.encode())
         if rc != 0:
             raise RuntimeError(f"stage {name}: {lib().orc_last_error().decode()}")
+
+    def physics(self):
+        """dict of the transient / energy / density switches read from param.in."""
+        iv = (C.c_int * 6)()
+        dv = (C.c_double * 4)()
+        lib().orc_physics(self.h, iv, dv)
+        return {"steady": bool(iv[0]), "time_scheme": iv[1], "max_outer": iv[2], "energy": bool(iv[3]),
+                "density": iv[4], "max_step": iv[5], "dt": dv[0], "total_time": dv[1], "cur_time": dv[2],
+                "pressure_reference": dv[3]}
+
+    def time_step(self, cap=64):
+        """One physical time step; returns dict(n, resmax [n], residual [n,10], ksp_its [n,8],
+        ksp_reason [n,8])."""
+        rm = np.zeros(cap); res = np.zeros((cap, 10))
+        its = np.zeros((cap, 8), dtype=np.int32); rs = np.zeros((cap, 8), dtype=np.int32)
+        n = lib().orc_time_step(self.h, cap, _ptr(rm), _ptr(res), _ptr(its), _ptr(rs))
+        if n < 0:
+            raise RuntimeError("oracle time step failed: " + lib().orc_last_error().decode())
+        k = min(n, cap)
+        return {"n": n, "resmax": rm[:k], "residual": res[:k], "ksp_its": its[:k], "ksp_reason": rs[:k]}
 
     def iterate(self, nsteps):
         res = np.zeros((nsteps, 10)); rm = np.zeros(nsteps)
@@ -197,10 +219,10 @@ def _block(vals):
     return "".join(out)
 
 
-def tecplot_text(vert, cell_vertices, f, turb):
+def tecplot_text(vert, cell_vertices, f, turb, density=0, pref=1.01325e5):
     """Output2Tecplot (NS/navierIO.cpp:161-283) at one rank: ``vert`` [nvrt, 3] or flat,
     ``cell_vertices`` zero-based [ncel * 8], ``f`` a dict of cell fields P U V W R T VisLam VisTur
-    [TE ED]."""
+    [TE ED]; with ``density`` 1 the Ma column is the Mach number (gamma 1.4)."""
     vert = np.asarray(vert, dtype=np.float64).reshape(-1, 3)
     cv = np.asarray(cell_vertices).reshape(-1, 8)
     n = cv.shape[0]
@@ -216,7 +238,11 @@ def tecplot_text(vert, cell_vertices, f, turb):
     for nm in ("P", "U", "V", "W", "R", "T"):
         parts.append(_block(f[nm]))
     U, V, W = (np.asarray(f[k], dtype=np.float64) for k in ("U", "V", "W"))
-    parts.append(_block(np.sqrt(U * U + V * V + W * W)))
+    if density == 1:
+        P, R = (np.asarray(f[k], dtype=np.float64) for k in ("P", "R"))
+        parts.append(_block(np.sqrt((U * U + V * V + W * W) / (1.4 * (P + pref) / R))))
+    else:
+        parts.append(_block(np.sqrt(U * U + V * V + W * W)))
     parts.append(_block(np.asarray(f["VisLam"]) + np.asarray(f["VisTur"])))
     if turb == 1:
         parts.append(_block(f["TE"]))

@@ -368,9 +368,12 @@ struct MomArgs {
   double *A, *bu, *bv, *bw, *Apr, *dinv, *old, *shear;
   double urf0, g0, g1, g2;
   int* warn;
+  const double *Unp, *Vnp, *Wnp;  // previous time level (scheme != 0)
+  int scheme;                     // 0 steady, 1 Euler, 2 second-order form
+  double dt;
 };
 
-// BuildVelocityMatrix cell loop (navier_velocity.cpp:100-383), steady
+// BuildVelocityMatrix cell loop (navier_velocity.cpp:100-383)
 __global__ void __launch_bounds__(kThreads) k_momentum(MomArgs a) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.ncel) return;
@@ -382,6 +385,21 @@ __global__ void __launch_bounds__(kThreads) k_momentum(MomArgs a) {
   double gv[3] = {a.dV[3 * i], a.dV[3 * i + 1], a.dV[3 * i + 2]};
   double gw[3] = {a.dW[3 * i], a.dW[3 * i + 1], a.dW[3 * i + 2]};
   double app = 0., su = 0., sv = 0., sw = 0.;
+  if (a.scheme != 0) {  // unsteady terms (navier_velocity.cpp:108-123)
+    double coef = a.R[i] / a.dt * a.c_vol[i];
+    double un = a.Unp[i], vn = a.Vnp[i], wn = a.Wnp[i];
+    if (a.scheme == 1) {
+      app += coef;
+      su += coef * un;
+      sv += coef * vn;
+      sw += coef * wn;
+    } else {  // both previous levels hold the same values (SaveTransientOldData)
+      app += 1.5 * coef;
+      su += coef * (2 * un - 0.5 * un);
+      sv += coef * (2 * vn - 0.5 * vn);
+      sw += coef * (2 * wn - 0.5 * wn);
+    }
+  }
   int nf = a.c_nface[i];
   for (int j = 0; j < nf; j++) {
     int iface = a.c_face[j * N + i];
@@ -619,6 +637,97 @@ __global__ void k_pressure(int ncel, const int* __restrict__ c_nface, const int*
   dinv[i] = 1.0 / valcen;
 }
 
+// BuildPressureMatrix, perfect gas (navier_pressure.cpp:106-224 with DensityModel 1): boundary
+// faces of inlets and outlets and the upwind density change enter the rows, which are no longer
+// symmetric
+__global__ void k_pressure_gas(int ncel, const int* __restrict__ c_nface, const int* __restrict__ c_face,
+                               const int* __restrict__ c_slot, const int* __restrict__ c_diag,
+                               const int* __restrict__ f_c1, const int* __restrict__ f_c2,
+                               const int* __restrict__ f_bnd, const int* __restrict__ b_type,
+                               const double* __restrict__ f_lambda, const double* __restrict__ f_rlencos,
+                               const double* __restrict__ c_vol, const double* __restrict__ R,
+                               const double* __restrict__ T, const double* __restrict__ BRo,
+                               const double* __restrict__ Apr, const double* __restrict__ RUFace, int unsteady,
+                               double dt, double* __restrict__ A, double* __restrict__ bp, double* __restrict__ dinv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncel) return;
+  const long N = ncel;
+  double valcen = 0., bpv = 0.;
+  double voli = c_vol[i], Ti = T[i];
+  if (unsteady) valcen += -voli / (dt * kRcpcv * Ti);
+  int nf = c_nface[i];
+  for (int j = 0; j < nf; j++) {
+    int iface = c_face[j * N + i];
+    int c1 = f_c1[iface], c2 = f_c2[iface];
+    bool own = (i == c1);
+    if (own) bpv += RUFace[iface];
+    else bpv -= RUFace[iface];
+    if (c2 < 0) {
+      int bnd = f_bnd[iface];
+      int t = b_type[bnd];
+      double RUn = RUFace[iface];
+      if (t == 2) {
+        double rof = BRo[bnd];
+        valcen += dmin(RUn, 0.) / (rof * kRcpcv * Ti);
+      } else if (t == 3) {
+        double rof = R[i];
+        valcen += (RUn > 0. ? RUn : 0.) / (rof * kRcpcv * Ti);
+      }
+      continue;
+    }
+    int in = own ? c2 : c1;
+    double lam = own ? f_lambda[iface] : 1. - f_lambda[iface];
+    double RUn = own ? RUFace[iface] : -RUFace[iface];
+    double lam2 = 1. - lam;
+    double roapf = R[i] * Apr[i] * lam + R[in] * Apr[in] * lam2;
+    double vol = voli * lam + c_vol[in] * lam2;
+    double tmp = roapf * vol * f_rlencos[iface];
+    valcen += -tmp;
+    double rof = lam * R[i] + lam2 * R[in];
+    if (RUn > 0.) {
+      double tmp2 = -RUn / (rof * kRcpcv * Ti);
+      valcen += tmp2;
+    }
+    double acn = tmp;
+    if (RUn < 0.) acn += -RUn / (rof * kRcpcv * T[in]);
+    A[c_slot[j * N + i]] = acn;
+  }
+  A[c_diag[i]] = valcen;
+  bp[i] = bpv;
+  dinv[i] = 1.0 / valcen;
+}
+
+// pressure, density and velocity correction for a perfect gas (navier_pressure.cpp:45-70,
+// DensityModel 1); block partial of localRes[3] as in k_correct_cells
+__global__ void k_correct_cells_gas(int ncel, const double* __restrict__ c_vol, const double* __restrict__ dp,
+                                    const double* __restrict__ Apr, const double* __restrict__ dPdX,
+                                    const double* __restrict__ T, int cell_pref, double urf_p, double* __restrict__ P,
+                                    double* __restrict__ R, double* __restrict__ U, double* __restrict__ V,
+                                    double* __restrict__ W, double* __restrict__ red) {
+  __shared__ double wsum[kThreads / 32];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double r = 0.0;
+  if (i < ncel) {
+    double ref = dp[cell_pref];
+    double vol = c_vol[i];
+    r = fabs(dp[i] - ref) * vol;
+    P[i] += urf_p * dp[i];
+    R[i] += dp[i] / (kRcpcv * T[i]);
+    double coef = vol * Apr[i];
+    U[i] -= coef * dPdX[3 * (long)i];
+    V[i] -= coef * dPdX[3 * (long)i + 1];
+    W[i] -= coef * dPdX[3 * (long)i + 2];
+  }
+  for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = r;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < kThreads / 32; q++) s += wsum[q];
+    red[blockIdx.x] = s;
+  }
+}
+
 // pressure and velocity correction (navier_pressure.cpp:45-70); block partial of
 // localRes[3] = sum |p' - p'_ref| * vol
 __global__ void k_correct_cells(int ncel, const double* __restrict__ c_vol, const double* __restrict__ dp,
@@ -681,7 +790,7 @@ __global__ void k_correct_cells_batch(const int* __restrict__ blk_lo, const int*
   }
 }
 
-// CorrectRUFace2, constant density (navier_pressure.cpp:235-278)
+// CorrectRUFace2 (navier_pressure.cpp:235-278); T is null for constant density
 __global__ void k_correct_ruface(int nfac, const int* __restrict__ f_c1, const int* __restrict__ f_c2,
                                  const int* __restrict__ f_bnd, const double* __restrict__ f_n,
                                  const double* __restrict__ f_lambda, const double* __restrict__ f_rlencos,
@@ -691,7 +800,7 @@ __global__ void k_correct_ruface(int nfac, const int* __restrict__ f_c1, const i
                                  const double* __restrict__ dp, const double* __restrict__ dPdX,
                                  const double* __restrict__ BRo, const double* __restrict__ BU,
                                  const double* __restrict__ BV, const double* __restrict__ BW, double urf_p,
-                                 double* __restrict__ RUFace) {
+                                 const double* __restrict__ T, double* __restrict__ RUFace) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nfac) return;
   int c1 = f_c1[i], c2 = f_c2[i];
@@ -708,6 +817,12 @@ __global__ void k_correct_ruface(int nfac, const int* __restrict__ f_c1, const i
   const double* xn = f_xnac + 3 * (long)i;
   const double* x1 = c_x + 3 * (long)c1;
   const double* x2 = c_x + 3 * (long)c2;
+  if (T) {  // perfect gas: ro' * u
+    double rop = dp[c1] / (kRcpcv * T[c1]) * lam + dp[c2] / (kRcpcv * T[c2]) * lam2;
+    double rof = R[c1] * lam + R[c2] * lam2;
+    double ru = RUFace[i];
+    RUFace[i] = ru + ru * rop / rof;
+  }
   double roapf = R[c1] * Apr[c1] * lam + R[c2] * Apr[c2] * lam2;
   double vol = c_vol[c1] * lam + c_vol[c2] * lam2;
   double coef = roapf * vol * f_rlencos[i];
@@ -933,6 +1048,102 @@ __global__ void k_eps_wall_rows(int n_wc, const int* __restrict__ wc_cell, const
   dinv[ic] = 1.0;
 }
 
+// unsteady terms of a scalar equation (navier_scalar.cpp:71-90, 290-305)
+__global__ void k_scalar_time(int ncel, const double* __restrict__ c_vol, const double* __restrict__ R, double dt,
+                              int scheme, const double* __restrict__ phi_old, double* ap, double* src) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncel) return;
+  double coef = R[i] / dt * c_vol[i];
+  double po = phi_old[i];
+  if (scheme == 1) {
+    ap[i] += coef;
+    src[i] += coef * po;
+  } else {
+    ap[i] += 1.5 * coef;
+    src[i] += coef * (2 * po - 0.5 * po);
+  }
+}
+
+// UpdateEnergy diffusion coefficient and sources (navier_scalar.cpp:215-281).  With a perfect
+// gas the work of the viscous stresses on each face enters its two cells with opposite signs;
+// every cell gathers its faces in ascending face order, the order of the reference's face loop.
+__global__ void k_energy_sources(int ncel, int gas, const int* __restrict__ c_nface, const int* __restrict__ c_gface,
+                                 const int* __restrict__ f_c1, const int* __restrict__ f_c2,
+                                 const double* __restrict__ f_lambda, const double* __restrict__ f_n,
+                                 const double* __restrict__ VisLam, const double* __restrict__ VisTur,
+                                 const double* __restrict__ dU, const double* __restrict__ dV,
+                                 const double* __restrict__ dW, const double* __restrict__ U,
+                                 const double* __restrict__ V, const double* __restrict__ W, double* kcond,
+                                 double* ES, double* ApE) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncel) return;
+  kcond[i] = kCp * (VisLam[i] / kPrl + VisTur[i] / kPrte) / kCp;
+  ApE[i] = 0.;
+  double es = 0.;
+  if (gas) {
+    const long N = ncel;
+    int nf = c_nface[i];
+    for (int j = 0; j < nf; j++) {
+      int f = c_gface[j * N + i];
+      int c1 = f_c1[f], c2 = f_c2[f];
+      double VisL, VisT, g[9], vx, vy, vz;
+      if (c2 < 0) {
+        VisL = VisLam[c1];
+        VisT = VisTur[c1];
+        for (int d = 0; d < 3; d++) {
+          g[d] = dU[3 * (long)c1 + d];
+          g[3 + d] = dV[3 * (long)c1 + d];
+          g[6 + d] = dW[3 * (long)c1 + d];
+        }
+        vx = U[c1];
+        vy = V[c1];
+        vz = W[c1];
+      } else {
+        double lam = f_lambda[f], lam2 = 1. - lam;
+        VisL = lam * VisLam[c1] + lam2 * VisLam[c2];
+        VisT = lam * VisTur[c1] + lam2 * VisTur[c2];
+        for (int d = 0; d < 3; d++) {
+          g[d] = lam * dU[3 * (long)c1 + d] + lam2 * dU[3 * (long)c2 + d];
+          g[3 + d] = lam * dV[3 * (long)c1 + d] + lam2 * dV[3 * (long)c2 + d];
+          g[6 + d] = lam * dW[3 * (long)c1 + d] + lam2 * dW[3 * (long)c2 + d];
+        }
+        vx = lam * U[c1] + lam2 * U[c2];
+        vy = lam * V[c1] + lam2 * V[c2];
+        vz = lam * W[c1] + lam2 * W[c2];
+      }
+      double dudx = g[0], dudy = g[1], dudz = g[2], dvdx = g[3], dvdy = g[4], dvdz = g[5];
+      double dwdx = g[6], dwdy = g[7], dwdz = g[8];
+      double vmul = VisL + VisT;
+      double vlac = -2. / 3. * vmul;
+      double div = dudx + dvdy + dwdz;
+      double txx = 2. * vmul * dudx + vlac * div;
+      double tyy = 2. * vmul * dvdy + vlac * div;
+      double tzz = 2. * vmul * dwdz + vlac * div;
+      double txy = vmul * (dudy + dvdx);
+      double txz = vmul * (dudz + dwdx);
+      double tyz = vmul * (dvdz + dwdy);
+      double btx = vx * txx + vy * txy + vz * txz;
+      double bty = vx * txy + vy * tyy + vz * tyz;
+      double btz = vx * txz + vy * tyz + vz * tzz;
+      const double* n = f_n + 3 * (long)f;
+      double fvis = (btx * n[0] + bty * n[1] + btz * n[2]) / kCp;
+      if (i == c1) es += fvis;
+      else es -= fvis;
+    }
+  }
+  ES[i] = es;
+}
+
+// SetBCTemperature (navier_bc.cpp:183-213): outlets and symmetry planes take the cell value;
+// walls and inlets keep theirs
+__global__ void k_bc_temperature(int nbnd, const int* __restrict__ b_face, const int* __restrict__ b_type,
+                                 const int* __restrict__ f_c1, const double* __restrict__ T, double* BTem) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbnd) return;
+  int t = b_type[b];
+  if (t == 3 || t == 4) BTem[b] = T[f_c1[b_face[b]]];
+}
+
 // epsilon clip and turbulent viscosity (navier_scalar.cpp:165-178)
 __global__ void k_finish_keps(int ncel, const double* __restrict__ R, const double* __restrict__ TE, double* ED,
                               double* VisTur) {
@@ -997,8 +1208,13 @@ void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, con
 }
 
 void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, const double* gravity,
-                     DevStatus* st, cudaStream_t s) {
+                     DevStatus* st, cudaStream_t s, const TimeConf& tc) {
   MomArgs a;
+  a.Unp = f.Unp;
+  a.Vnp = f.Vnp;
+  a.Wnp = f.Wnp;
+  a.scheme = tc.scheme;
+  a.dt = tc.dt;
   a.ncel = m.ncel;
   a.c_nface = m.c_nface;
   a.c_face = m.c_face;
@@ -1057,8 +1273,20 @@ void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s) {
                                                      f.RUFace, f.Ap, f.bp, f.dinv_p);
 }
 
+void launch_pressure_gas(const DevMesh& m, const DevFields& f, const TimeConf& tc, cudaStream_t s) {
+  ++g_launch_count, k_pressure_gas<<<blocks_for(m.ncel), kThreads, 0, s>>>(
+                        m.ncel, m.c_nface, m.c_face, m.c_slot, m.c_diag, m.f_c1, m.f_c2, m.f_bnd, m.b_type,
+                        m.f_lambda, m.f_rlencos, m.c_vol, f.R, f.T, f.BRo, f.Apr, f.RUFace, tc.scheme != 0 ? 1 : 0,
+                        tc.dt, f.Ap, f.bp, f.dinv_p);
+}
+
 void launch_correct_cells(const DevMesh& m, const DevFields& f, int cell_pref, double urf_p, double* red,
-                          cudaStream_t s, const DevBatch* b) {
+                          cudaStream_t s, const DevBatch* b, int density_model) {
+  if (density_model == 1) {
+    ++g_launch_count, k_correct_cells_gas<<<blocks_for(m.ncel), kThreads, 0, s>>>(
+                          m.ncel, m.c_vol, f.dp, f.Apr, f.dPdX, f.T, cell_pref, urf_p, f.P, f.R, f.U, f.V, f.W, red);
+    return;
+  }
   if (b) {
     ++g_launch_count, k_correct_cells_batch<<<b->nblk, kThreads, 0, s>>>(b->blk_lo, b->blk_hi, b->blk_case,
                                                                           b->case_pref, m.c_vol, f.dp, f.Apr, f.dPdX,
@@ -1069,11 +1297,29 @@ void launch_correct_cells(const DevMesh& m, const DevFields& f, int cell_pref, d
                                                           f.P, f.U, f.V, f.W, red);
 }
 
-void launch_correct_ruface(const DevMesh& m, const DevFields& f, double urf_p, cudaStream_t s) {
+void launch_correct_ruface(const DevMesh& m, const DevFields& f, double urf_p, cudaStream_t s, int density_model) {
   ++g_launch_count, k_correct_ruface<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.f_n, m.f_lambda,
                                                            m.f_rlencos, m.f_xpac, m.f_xnac, m.c_x, m.c_vol, f.R,
                                                            f.Apr, f.dp, f.dPdX, f.BRo, f.BU, f.BV, f.BW, urf_p,
-                                                           f.RUFace);
+                                                           density_model == 1 ? f.T : nullptr, f.RUFace);
+}
+
+void launch_scalar_time(const DevMesh& m, const DevFields& f, const TimeConf& tc, const double* phi_old, double* ap,
+                        double* src, cudaStream_t s) {
+  ++g_launch_count, k_scalar_time<<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_vol, f.R, tc.dt, tc.scheme,
+                                                                          phi_old, ap, src);
+}
+
+void launch_energy_sources(const DevMesh& m, const DevFields& f, int density_model, cudaStream_t s) {
+  ++g_launch_count, k_energy_sources<<<blocks_for(m.ncel), kThreads, 0, s>>>(
+                        m.ncel, density_model == 1 ? 1 : 0, m.c_nface, m.c_gface, m.f_c1, m.f_c2, m.f_lambda, m.f_n,
+                        f.VisLam, f.VisTur, f.dUdX, f.dVdX, f.dWdX, f.U, f.V, f.W, f.kcond, f.ES, f.ApE);
+}
+
+void launch_bc_temperature(const DevMesh& m, const DevFields& f, cudaStream_t s) {
+  if (m.nbnd > 0)
+    ++g_launch_count, k_bc_temperature<<<blocks_for(m.nbnd), kThreads, 0, s>>>(m.nbnd, m.b_face, m.b_type, m.f_c1, f.T,
+                                                                               f.BTem);
 }
 
 void launch_keps_sources(const DevMesh& m, const DevFields& f, cudaStream_t s) {

@@ -103,6 +103,11 @@ struct cycas_ctx {
   int red_parts = 0;
   int turb = 0, density = 0, cell_pref = 0;
   double urf[8], gravity[3];
+  TimeConf tc;                   // transient runs: scheme 0 when steady
+  int max_outer = 50;            // MaxOuterStep
+  int energy = 0;                // SolveEnergy
+  double pref = 1.01325e5;       // PressureReference
+  double cur_time = 0.0;
   KspConf ksp[3];
   int nsolve = 0;                // solves issued in the current iteration
   int solve_sys[8] = {0};        // system of each solve of the current iteration
@@ -406,6 +411,22 @@ void alloc_fields(cycas_ctx& c) {
   f.dinv_u = c.dfield("dinv_u", n);
   f.dinv_p = c.dfield("dinv_p", n);
   f.dinv_s = c.dfield("dinv_s", n);
+  f.Rnp = f.Unp = f.Vnp = f.Wnp = f.Tnp = f.TEp = f.EDp = nullptr;
+  if (c.tc.scheme != 0) {
+    f.Rnp = c.dfield("Rnp", n);
+    f.Unp = c.dfield("Unp", n);
+    f.Vnp = c.dfield("Vnp", n);
+    f.Wnp = c.dfield("Wnp", n);
+    f.Tnp = c.dfield("Tnp", n);
+    f.TEp = c.dfield("TEp", n);
+    f.EDp = c.dfield("EDp", n);
+  }
+  f.kcond = f.ES = f.ApE = nullptr;
+  if (c.energy) {
+    f.kcond = c.dfield("kcond", n);
+    f.ES = c.dfield("ESource", n);
+    f.ApE = c.dfield("ApE", n);
+  }
 }
 
 void alloc_krylov(cycas_ctx& c) {
@@ -470,10 +491,19 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
   c.device = o->device;
   CK(cudaSetDevice(c.device));
   CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-  require(p->density_model == 0, "only constant density (DensityModel 0) is on this path");
+  require(p->density_model == 0 || p->density_model == 1, "DensityModel must be 0 or 1");
   require(p->turb_model == 0 || p->turb_model == 1, "TurModel must be 0 or 1");
   c.turb = p->turb_model;
   c.density = p->density_model;
+  if (p->transient) {
+    require(p->time_scheme == 1 || p->time_scheme == 2, "TimeScheme must be 1 (Euler) or 2 (Dual)");
+    require(p->dt > 0.0, "dt must be positive");
+    c.tc.scheme = p->time_scheme;
+    c.tc.dt = p->dt;
+    c.max_outer = p->max_outer;
+  }
+  c.energy = (p->solve_energy || p->density_model == 1) ? 1 : 0;  // readparamfile.cpp:337-338
+  c.pref = p->pressure_reference > 0.0 ? p->pressure_reference : 1.01325e5;
   c.cell_pref = p->cell_pressure_ref;
   for (int i = 0; i < 8; i++) c.urf[i] = p->urf[i];
   for (int i = 0; i < 3; i++) c.gravity[i] = p->gravity[i];
@@ -509,9 +539,10 @@ void set_mixed(cycas_ctx& c, GmresCall& g) {
   g.inner_rtol = c.inner_rtol;
 }
 
-void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const double* b, double* x, bool guess_zero) {
+void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const double* b, double* x, bool guess_zero,
+           const KspConf* conf = nullptr) {
   require(c.nsolve < 8, "too many solves in one iteration");
-  const KspConf& k = c.ksp[sys];
+  const KspConf& k = conf ? *conf : c.ksp[sys];
   GmresCall g;
   g.n = c.m.ncel;
   g.rowptr = c.m.rowptr;
@@ -646,7 +677,7 @@ void grad1(cycas_ctx& c, const double* phi, const double* bphi, double* g) {
 void build_velocity(cycas_ctx& c) {
   bc_velocity(c, true);
   grad_uvwp(c);
-  launch_momentum(c.m, c.f, c.urf, c.gravity, c.st, c.stream);
+  launch_momentum(c.m, c.f, c.urf, c.gravity, c.st, c.stream, c.tc);
 }
 
 // CalculateVelocity (navier_velocity.cpp:10-60)
@@ -657,27 +688,47 @@ void calculate_velocity(cycas_ctx& c) {
 }
 
 void correct_cells(cycas_ctx& c) {
-  launch_correct_cells(c.m, c.f, c.cell_pref, c.urf[3], c.red, c.stream, c.bptr());
+  launch_correct_cells(c.m, c.f, c.cell_pref, c.urf[3], c.red, c.stream, c.bptr(), c.density);
   launch_finalize_residual(c.red, c.is_batch ? c.batch.nblk : (c.m.ncel + 255) / 256, 3, c.st, c.stream, c.bptr());
 }
 
-// CalculatePressure (navier_pressure.cpp:9-97)
+// the pressure-correction rows of the context's density model
+void build_pressure(cycas_ctx& c) {
+  if (c.density == 1) launch_pressure_gas(c.m, c.f, c.tc, c.stream);
+  else launch_pressure(c.m, c.f, c.stream);
+}
+
+// CalculatePressure (navier_pressure.cpp:9-97).  A perfect gas makes the system nonsymmetric:
+// the reference then switches PETSc to GMRES (MPIStructure.cpp:462-467); here GMRES(restart)
+// with the Jacobi preconditioner at the pressure system's tolerances.
 void calculate_pressure(cycas_ctx& c) {
   bc_velocity(c, false);
   launch_ruface2(c.m, c.f, c.stream);
-  launch_pressure(c.m, c.f, c.stream);
-  solve(c, CYCAS_SYS_PRESSURE, c.f.Ap, c.f.dinv_p, c.f.bp, c.f.dp, true);
+  build_pressure(c);
+  if (c.density == 1) {
+    KspConf k = c.ksp[CYCAS_SYS_PRESSURE];
+    k.type = CYCAS_KSP_GMRES;
+    if (k.pc == CYCAS_PC_AMG) k.pc = CYCAS_PC_JACOBI;
+    solve(c, CYCAS_SYS_PRESSURE, c.f.Ap, c.f.dinv_p, c.f.bp, c.f.dp, true, &k);
+  } else {
+    solve(c, CYCAS_SYS_PRESSURE, c.f.Ap, c.f.dinv_p, c.f.bp, c.f.dp, true);
+  }
   launch_bc_deltap(c.m, c.f, c.stream);
   grad1(c, c.f.dp, c.f.BPre, c.f.dPdX);
   correct_cells(c);
   bc_velocity(c, false);
-  launch_correct_ruface(c.m, c.f, c.urf[3], c.stream);
+  launch_correct_ruface(c.m, c.f, c.urf[3], c.stream, c.density);
 }
 
 // UpdateTurKEpsilon (navier_scalar.cpp:11-197)
 void update_keps(cycas_ctx& c) {
   launch_keps_sources(c.m, c.f, c.stream);
   launch_keps_wall(c.m, c.f, c.stream);
+  if (c.tc.scheme != 0) {  // unsteady terms (navier_scalar.cpp:71-90); the epsilon source is
+    // overwritten before its solve (navier_scalar.cpp:118), its diagonal share is kept
+    launch_scalar_time(c.m, c.f, c.tc, c.f.TEp, c.f.ApTE, c.f.TES, c.stream);
+    launch_scalar_time(c.m, c.f, c.tc, c.f.EDp, c.f.ApED, c.f.EDS, c.stream);
+  }
   grad1(c, c.f.TE, c.f.BTE, c.f.dPhidX);
   launch_scalar(c.m, c.f, c.f.TE, c.f.BTE, c.f.VisTE, c.f.TES, c.f.ApTE, c.urf[5], c.st, c.stream);
   solve(c, CYCAS_SYS_SCALAR, c.f.As, c.f.dinv_s, c.f.bs, c.f.TE, false);
@@ -687,6 +738,33 @@ void update_keps(cycas_ctx& c) {
   launch_eps_wall_rows(c.m, c.f, c.stream);
   solve(c, CYCAS_SYS_SCALAR, c.f.As, c.f.dinv_s, c.f.bs, c.f.ED, false);
   launch_finish_keps(c.m, c.f, c.stream);
+}
+
+// UpdateEnergy (navier_scalar.cpp:204-326): temperature transport with conductivity
+// cp (mu / Pr + mu_t / Pr_t) / cp, viscous heating with a perfect gas, GMRES at rtol 1e-8
+void build_energy(cycas_ctx& c) {
+  require(c.energy, "the energy equation is not solved in this context");
+  launch_energy_sources(c.m, c.f, c.density, c.stream);
+  launch_bc_temperature(c.m, c.f, c.stream);
+  if (c.tc.scheme != 0) launch_scalar_time(c.m, c.f, c.tc, c.f.Tnp, c.f.ApE, c.f.ES, c.stream);
+  grad1(c, c.f.T, c.f.BTem, c.f.dPhidX);
+  launch_scalar(c.m, c.f, c.f.T, c.f.BTem, c.f.kcond, c.f.ES, c.f.ApE, c.urf[5], c.st, c.stream);
+}
+
+void update_energy(cycas_ctx& c) {
+  build_energy(c);
+  solve(c, CYCAS_SYS_SCALAR, c.f.As, c.f.dinv_s, c.f.bs, c.f.T, false);
+}
+
+// SaveTransientOldData (navier.cpp:698-740)
+void save_old_level(cycas_ctx& c) {
+  require(c.tc.scheme != 0, "not a transient context");
+  const long n = c.m.ncel;
+  const double* cur[7] = {c.f.R, c.f.U, c.f.V, c.f.W, c.f.T, c.f.TE, c.f.ED};
+  double* old[7] = {c.f.Rnp, c.f.Unp, c.f.Vnp, c.f.Wnp, c.f.Tnp, c.f.TEp, c.f.EDp};
+  const int nf = c.turb == 1 ? 7 : 5;
+  for (int q = 0; q < nf; q++)
+    CK(cudaMemcpyAsync(old[q], cur[q], sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
 }
 
 void begin_iteration(cycas_ctx& c) {
@@ -704,6 +782,7 @@ void issue_iteration(cycas_ctx& c) {
   calculate_velocity(c);
   calculate_pressure(c);
   if (c.turb == 1) update_keps(c);
+  if (c.energy) update_energy(c);
 }
 
 // One iteration's device work.  In graph mode the first call captures begin + issue into a
@@ -1151,6 +1230,8 @@ void fetch_case_fields(cycas_ctx& c, int k, CaseFields& out) {
   CellFieldsView& v = out.view;
   v.ncel = n;
   v.turb = c.turb;
+  v.density = c.density;
+  v.pref = c.pref;
   v.P = out.a[0].data(), v.U = out.a[1].data(), v.V = out.a[2].data(), v.W = out.a[3].data();
   v.R = out.a[4].data(), v.T = out.a[5].data(), v.VisLam = out.a[6].data(), v.VisTur = out.a[7].data();
   v.TE = out.a[8].data(), v.ED = out.a[9].data();
@@ -1228,6 +1309,27 @@ int cycas_case_params(const cycas_case* c, double* residual_steady, double urf[8
   });
 }
 
+int cycas_case_physics(const cycas_case* c, int32_t iopt[6], double dopt[3]) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null case");
+    const HostCase& h = c->hc;
+    if (iopt) {
+      iopt[0] = h.steady;
+      iopt[1] = h.time_scheme;
+      iopt[2] = h.max_outer;
+      iopt[3] = h.solve_energy;
+      iopt[4] = h.density_model;
+      iopt[5] = h.max_step;
+    }
+    if (dopt) {
+      dopt[0] = h.dt;
+      dopt[1] = h.total_time;
+      dopt[2] = h.pressure_reference;
+    }
+    return CYCAS_OK;
+  });
+}
+
 int cycas_case_get_int(const cycas_case* c, const char* name, int32_t* dst, int64_t n) {
   return guard([&]() -> int {
     require(c && name && dst, "null argument");
@@ -1290,6 +1392,12 @@ int cycas_create_from_case(const cycas_case* cs, const cycas_options* opt, cycas
     p.cell_pressure_ref = h.cell_pressure_ref;
     for (int i = 0; i < 8; i++) p.urf[i] = h.urf[i];
     for (int i = 0; i < 3; i++) p.gravity[i] = h.gravity[i];
+    p.transient = h.steady ? 0 : 1;
+    p.time_scheme = h.time_scheme;
+    p.dt = h.dt;
+    p.max_outer = h.max_outer;
+    p.solve_energy = h.solve_energy;
+    p.pressure_reference = h.pressure_reference;
     require(h.cell_pressure_ref >= 0 && h.cell_pressure_ref < h.ncel, "PressureRef cell out of range");
     int rc = cycas_create(&v, &p, opt, out);
     if (rc != CYCAS_OK) return rc;
@@ -1386,6 +1494,39 @@ int cycas_simple_iterations(cycas_ctx* c, int32_t n, double* res_hist, double* r
   });
 }
 
+int cycas_time_step(cycas_ctx* c, int32_t cap, int32_t* n_outer, double* res_hist, double* resmax, int32_t* its,
+                    int32_t* reasons, double* cur_time) {
+  return guard([&]() -> int {
+    require(c != nullptr && cap >= 0, "bad argument");
+    require(!c->is_batch && c->tc.scheme != 0, "cycas_time_step needs a transient single-case context");
+    save_old_level(*c);
+    c->cur_time += c->tc.dt;
+    double ResMax0 = 0.0;
+    int rc = CYCAS_OK, done = 0;
+    for (int iter = 1; iter < c->max_outer; iter++) {
+      cycas_iter_stats st;
+      double res[10], rm;
+      run_iteration(*c);
+      rc = finish_iteration(*c, res, &rm, &st);
+      if (done < cap) {
+        if (res_hist) std::memcpy(res_hist + 10L * done, res, sizeof res);
+        if (resmax) resmax[done] = rm;
+        for (int k = 0; k < 8; k++) {
+          if (its) its[8L * done + k] = st.its[k];
+          if (reasons) reasons[8L * done + k] = st.reason[k];
+        }
+      }
+      done++;
+      if (rc != CYCAS_OK) break;
+      if (iter == 1) ResMax0 = rm;
+      if (ResMax0 / (rm + 1.e-16) > 100.) break;  // two orders of residual drop (navier.cpp:104-107)
+    }
+    if (n_outer) *n_outer = done;
+    if (cur_time) *cur_time = c->cur_time;
+    return rc;
+  });
+}
+
 int cycas_run_stage(cycas_ctx* c, const char* stage) {
   return guard([&]() -> int {
     require(c && stage, "null argument");
@@ -1404,12 +1545,15 @@ int cycas_run_stage(cycas_ctx* c, const char* stage) {
     else if (s == "grad_deltap") grad1(x, x.f.dp, x.f.BPre, x.f.dPdX);
     else if (s == "build_velocity") build_velocity(x);
     else if (s == "ruface2") launch_ruface2(x.m, x.f, x.stream);
-    else if (s == "build_pressure") launch_pressure(x.m, x.f, x.stream);
+    else if (s == "build_pressure") build_pressure(x);
     else if (s == "correct_cells") correct_cells(x);
-    else if (s == "correct_ruface") launch_correct_ruface(x.m, x.f, x.urf[3], x.stream);
+    else if (s == "correct_ruface") launch_correct_ruface(x.m, x.f, x.urf[3], x.stream, x.density);
     else if (s == "calculate_velocity") calculate_velocity(x);
     else if (s == "calculate_pressure") calculate_pressure(x);
     else if (s == "keps") update_keps(x);
+    else if (s == "energy") update_energy(x);
+    else if (s == "build_energy") build_energy(x);
+    else if (s == "save_transient") save_old_level(x);
     else throw StatusError(CYCAS_ERR_INVALID, "unknown stage " + s);
     return finish_iteration(x, nullptr, nullptr, nullptr);
   });
@@ -1569,6 +1713,8 @@ int cycas_batch_create(const cycas_case* const* cases, int32_t ncases, const cyc
       for (int i = 0; i < 8; i++) same = same && h->urf[i] == h0.urf[i];
       for (int i = 0; i < 3; i++) same = same && h->gravity[i] == h0.gravity[i];
       require(same, "batched cases must share the turbulence model, density model, relaxation and gravity");
+      require(h->steady && h->density_model == 0 && !h->solve_energy,
+              "batches hold steady, isothermal, constant-density cases");
     }
     UnionMesh u = build_union(hs);
     cycas_mesh_view v = view_of(u.h);
@@ -1902,8 +2048,9 @@ int cycas_dump_begin(cycas_ctx* c, int32_t k, const cycas_case* cs, int32_t kind
     const std::string tp = tecplot_path ? tecplot_path : "", dp = data_path ? data_path : "",
                       bp = backup_path ? backup_path : "";
     const HostCase* hc = (kinds & CYCAS_DUMP_TECPLOT) ? &cs->hc : nullptr;
-    const int turb = c->turb, device = c->device;
-    d.worker = std::thread([&d, hc, kinds, tp, dp, bp, n, turb, device]() {
+    const int turb = c->turb, device = c->device, density = c->density;
+    const double pref = c->pref;
+    d.worker = std::thread([&d, hc, kinds, tp, dp, bp, n, turb, device, density, pref]() {
       try {
         cudaSetDevice(device);
         cudaError_t e = cudaEventSynchronize(d.ev_host);
@@ -1911,6 +2058,8 @@ int cycas_dump_begin(cycas_ctx* c, int32_t k, const cycas_case* cs, int32_t kind
         CellFieldsView v;
         v.ncel = n;
         v.turb = turb;
+        v.density = density;
+        v.pref = pref;
         const double* b = d.host;
         v.P = b, v.U = b + n, v.V = b + 2 * n, v.W = b + 3 * n, v.R = b + 4 * n, v.T = b + 5 * n;
         v.VisLam = b + 6 * n, v.VisTur = b + 7 * n, v.TE = b + 8 * n, v.ED = b + 9 * n;

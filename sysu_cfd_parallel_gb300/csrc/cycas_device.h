@@ -62,7 +62,25 @@ struct DevFields {
   double *Au, *Ap, *As;                         // values on the shared pattern
   double *bu, *bv, *bw, *bp, *bs;
   double *dinv_u, *dinv_p, *dinv_s;             // Jacobi: reciprocal of the diagonal
+  // transient runs: the previous time level (null when steady).  The reference's second-order
+  // save assigns both previous levels from the current one, so one level serves both schemes.
+  double *Rnp, *Unp, *Vnp, *Wnp, *Tnp, *TEp, *EDp;
+  // energy equation (null when it is not solved)
+  double *kcond, *ES, *ApE;
 };
+
+// time discretisation of a transient run (scheme 0: steady)
+struct TimeConf {
+  int scheme = 0;  // 1 Euler, 2 the reference's second-order ("Dual") form
+  double dt = 1.0;
+};
+
+// perfect-gas constants of the reference (navier.cpp:486-493)
+constexpr double kCp = 1006.;
+constexpr double kGama = 1.4;
+constexpr double kPrl = 0.72;
+constexpr double kPrte = 0.9;
+constexpr double kRcpcv = kCp - kCp / kGama;
 
 // per-solve report written by the Krylov kernel
 struct KspOut {
@@ -128,12 +146,22 @@ void launch_bc_deltap(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
                      double* const* grad, cudaStream_t s);
 void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, const double* gravity,
-                     DevStatus* st, cudaStream_t s);
+                     DevStatus* st, cudaStream_t s, const TimeConf& tc = TimeConf());
 void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s);
+// compressible (perfect-gas) pressure-correction rows (navier_pressure.cpp:106-224, DensityModel 1)
+void launch_pressure_gas(const DevMesh& m, const DevFields& f, const TimeConf& tc, cudaStream_t s);
 void launch_correct_cells(const DevMesh& m, const DevFields& f, int cell_pref, double urf_p, double* red,
-                          cudaStream_t s, const DevBatch* b = nullptr);
-void launch_correct_ruface(const DevMesh& m, const DevFields& f, double urf_p, cudaStream_t s);
+                          cudaStream_t s, const DevBatch* b = nullptr, int density_model = 0);
+void launch_correct_ruface(const DevMesh& m, const DevFields& f, double urf_p, cudaStream_t s,
+                           int density_model = 0);
+// unsteady terms of a scalar equation: Ap += c (1.5 c), src += c * phi_old (c * (2 phi_old -
+// 0.5 phi_old)) with c = R / dt * vol
+void launch_scalar_time(const DevMesh& m, const DevFields& f, const TimeConf& tc, const double* phi_old,
+                        double* ap, double* src, cudaStream_t s);
+// UpdateEnergy sources (navier_scalar.cpp:209-281) and SetBCTemperature (navier_bc.cpp:183-213)
+void launch_energy_sources(const DevMesh& m, const DevFields& f, int density_model, cudaStream_t s);
+void launch_bc_temperature(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_keps_sources(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_keps_wall(const DevMesh& m, const DevFields& f, cudaStream_t s);
 void launch_scalar(const DevMesh& m, const DevFields& f, const double* phi, const double* bphi,

@@ -26,6 +26,8 @@ struct HostCase {
   // options pool defaults (NS/navier.cpp:475-516)
   int steady = 1, max_step = 10000, turb_model = 0, density_model = 0, solve_energy = 0;
   int limiter = 0, restart = 0, noutput = 1, cell_pressure_ref = 0;
+  int time_scheme = 1, max_outer = 50;  // TimeScheme, MaxOuterStep
+  double dt = 1.0, total_time = 0.0;
   double residual_steady = 1.e-6, pressure_reference = 1.01325e5;
   double urf[8] = {0.6, 0.6, 0.6, 0.5, 0.8, 0.8, 0.8, 0.8};
   double gravity[3] = {0, 0, 0};
@@ -55,6 +57,8 @@ void load_case(HostCase& hc, const std::string& paramPath, bool msh_binary = fal
 struct CellFieldsView {
   long ncel = 0;
   int turb = 0;
+  int density = 0;         // DensityModel: 1 writes the Mach number in the Ma column
+  double pref = 1.01325e5; // PressureReference
   const double *P = nullptr, *U = nullptr, *V = nullptr, *W = nullptr, *R = nullptr, *T = nullptr;
   const double *VisLam = nullptr, *VisTur = nullptr, *TE = nullptr, *ED = nullptr;
 };

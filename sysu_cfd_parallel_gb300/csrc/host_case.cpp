@@ -81,8 +81,16 @@ void load_params(HostCase& hc, const std::string& path) {
       hc.steady = 1;
       hc.max_step = std::atoi(kw[1].c_str());
       hc.residual_steady = num(2);
-    } else if (key == "transient") {
-      bad("transient time stepping is outside the steady SIMPLE path");
+    } else if (key == "transient") {  // readparamfile.cpp:84-101
+      if (nk != 4) bad("transient requies 3 parameters");
+      hc.steady = 0;
+      hc.dt = num(1);
+      hc.total_time = num(2);
+      hc.max_step = (int)(hc.total_time / hc.dt);
+      hc.max_outer = (int)num(3);
+      if (kw[4] == "Euler") hc.time_scheme = 1;
+      else if (kw[4] == "Dual") hc.time_scheme = 2;
+      else bad("unknown time scheme: " + kw[4]);
     } else if (key == "energy") {
       if (kw[1] == "on") hc.solve_energy = 1;
       else if (kw[1] == "off") hc.solve_energy = 0;
@@ -555,6 +563,10 @@ void init_fields(HostCase& hc) {
     hc.R[i] = iv[3];
     hc.T[i] = iv[4];
     hc.P[i] = 0.;
+    if (hc.density_model == 1) {  // perfect gas with the reference's constants (navier.cpp:486-493)
+      const double cp = 1006., cv = cp / 1.4;
+      hc.R[i] = (hc.P[i] + hc.pressure_reference) / ((cp - cv) * hc.T[i]);
+    }
     hc.VisLam[i] = iv[5];
     hc.VisTur[i] = 0.;
     if (hc.turb_model == 1) {

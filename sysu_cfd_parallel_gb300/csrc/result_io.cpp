@@ -93,8 +93,11 @@ std::string tecplot_text(const double* vert, long nvrt, const int32_t* cell_vert
   // blocks x y z, P U V W R T, Ma, mu, [TE ED], then the connectivity in chunks of cells; every
   // block is independent text, rendered in parallel and joined in order
   std::vector<double> ma((size_t)n), mu((size_t)n);
-  for (long i = 0; i < n; i++) {  // velocity magnitude (constant density); VisLam + VisTur
-    ma[i] = std::sqrt((f.U[i] * f.U[i] + f.V[i] * f.V[i] + f.W[i] * f.W[i]));
+  for (long i = 0; i < n; i++) {  // Mach number (perfect gas) or velocity magnitude; VisLam + VisTur
+    if (f.density == 1)
+      ma[i] = std::sqrt((f.U[i] * f.U[i] + f.V[i] * f.V[i] + f.W[i] * f.W[i]) / (1.4 * (f.P[i] + f.pref) / f.R[i]));
+    else
+      ma[i] = std::sqrt((f.U[i] * f.U[i] + f.V[i] * f.V[i] + f.W[i] * f.W[i]));
     mu[i] = f.VisLam[i] + f.VisTur[i];
   }
   std::vector<const double*> cols = {f.P, f.U, f.V, f.W, f.R, f.T, ma.data(), mu.data()};

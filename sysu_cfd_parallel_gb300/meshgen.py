@@ -162,29 +162,57 @@ def channel_mesh(nx, ny, nz, length=10.0, jitter=0.15, seed=2026):
     return nodes, [(2, np.stack([rid, rid], 1), bfaces.astype(np.int64)), (4, tt, tets.astype(np.int64))]
 
 
-def cavity_param(mesh_name, steps=200, mu=0.01, lid=1.0, residual=1e-300):
+def _time_and_physics(steps, residual, time, energy, density):
+    """The time line (steady, or transient with (dt, total_time, MaxOuterStep, scheme)) and the
+    optional energy / density lines of a param.in."""
+    if time is None:
+        lines = f"steady,{steps},{residual!r}\n"
+    else:
+        dt, total, outer, scheme = time
+        lines = f"transient,{dt!r},{total!r},{outer},{scheme}\n"
+    if energy:
+        lines += "energy,on\n"
+    if density:
+        lines += f"density,{density}\n"
+    return lines
+
+
+def gas_density(T, p_ref=1.01325e5):
+    """Perfect-gas density at gauge pressure 0 with the reference's constants (cp 1006, gamma 1.4)."""
+    cp = 1006.
+    cv = cp / 1.4
+    return p_ref / ((cp - cv) * T)
+
+
+def cavity_param(mesh_name, steps=200, mu=0.01, lid=1.0, residual=1e-300, time=None, energy=False, density=0,
+                 wall_t=None, lid_t=300):
+    ro = gas_density(300.0) if density == 1 else 1
+    ro_lid = gas_density(lid_t) if density == 1 else 1
+    wall = "bound,1,Hwall,walls,0\n" if wall_t is None else f"bound,1,Twall,walls,{wall_t!r}\n"
     return (f"gridfile,{mesh_name}\n"
-            f"steady,{steps},{residual!r}\n"
+            + _time_and_physics(steps, residual, time, energy, density) +
             "turbulence,no\n"
             "relaxation,0.6,0.5,0.8\n"
-            f"initflow,0,0,0,1,300,{mu!r},0,0\n"
-            "bound,1,Hwall,walls,0\n"
-            f"bound,2,inlet,lid,{lid!r},0,0,0,1,300,0,0\n"
-            f"volumn,3,fluid,fluid,0,0,0,1,300,{mu!r},0,0\n"
+            f"initflow,0,0,0,{ro!r},300,{mu!r},0,0\n"
+            + wall +
+            f"bound,2,inlet,lid,{lid!r},0,0,0,{ro_lid!r},{lid_t!r},0,0\n"
+            f"volumn,3,fluid,fluid,0,0,0,{ro!r},300,{mu!r},0,0\n"
             "output,100000,tecplot\n")
 
 
-def channel_param(mesh_name, steps=500, u_in=1.0, mu=2e-5, residual=1e-300):
+def channel_param(mesh_name, steps=500, u_in=1.0, mu=2e-5, residual=1e-300, time=None, energy=False,
+                  wall_t=None, t_in=300):
     k = 1.5 * (0.05 * u_in) ** 2
     eps = 0.09 ** 0.75 * k ** 1.5 / 0.07
+    wall = "bound,3,Hwall,walls,0\n" if wall_t is None else f"bound,3,Twall,walls,{wall_t!r}\n"
     return (f"gridfile,{mesh_name}\n"
             "turbulence,ke\n"
-            f"steady,{steps},{residual!r}\n"
+            + _time_and_physics(steps, residual, time, energy, 0) +
             "relaxation,0.6,0.5,0.8\n"
             f"initflow,{u_in!r},0,0,1,300,{mu!r},{k!r},{eps!r}\n"
-            f"bound,1,inlet,inlet,{u_in!r},0,0,0,1,300,{k!r},{eps!r}\n"
+            f"bound,1,inlet,inlet,{u_in!r},0,0,0,1,{t_in!r},{k!r},{eps!r}\n"
             "bound,2,outlet,outlet,0\n"
-            "bound,3,Hwall,walls,0\n"
+            + wall +
             f"volumn,4,fluid,fluid,{u_in!r},0,0,1,300,{mu!r},{k!r},{eps!r}\n"
             "output,100000,tecplot\n")
 

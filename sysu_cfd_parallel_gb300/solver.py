@@ -49,6 +49,11 @@ class Case:
         self.residual_steady = rs.value
         self.urf = list(urf)
         self.gravity = list(g)
+        iv, dv = (C.c_int32 * 6)(), (C.c_double * 3)()
+        capi.check(L.cycas_case_physics(h, iv, dv))
+        self.steady, self.time_scheme, self.max_outer = bool(iv[0]), int(iv[1]), int(iv[2])
+        self.solve_energy, self.density_model = bool(iv[3]), int(iv[4])
+        self.dt, self.total_time, self.pressure_reference = float(dv[0]), float(dv[1]), float(dv[2])
         no, rst = C.c_int32(), C.c_int32()
         capi.check(L.cycas_case_output(h, C.byref(no), C.byref(rst)))
         self.noutput = no.value
@@ -105,6 +110,7 @@ class NavierStokesSolver:
         capi.check(L.cycas_create_from_case(case._h, C.byref(self.options), C.byref(h)))
         self._h = h
         self.step = 0
+        self.cur_time = 0.0
         self.Residual = np.zeros(10)
         self.last_stats = None
 
@@ -185,6 +191,27 @@ class NavierStokesSolver:
         self.step += n
         return {"residual": res, "resmax": rm, "ksp_its": its, "ksp_reason": rs}
 
+    def time_step(self, cap: int = 64):
+        """One physical time step of a transient case (cycas_time_step): returns dict(n,
+        resmax [n], residual [n, 10], ksp_its [n, 8], ksp_reason [n, 8], cur_time)."""
+        n = C.c_int32()
+        t = C.c_double()
+        rm = np.zeros(cap); res = np.zeros((cap, 10))
+        its = np.zeros((cap, 8), dtype=np.int32); rs = np.zeros((cap, 8), dtype=np.int32)
+        rc = capi.load().cycas_time_step(self._h, cap, C.byref(n), capi.ptr(res), capi.ptr(rm), capi.ptr(its),
+                                         capi.ptr(rs), C.byref(t))
+        k = min(n.value, cap)
+        self.step += 1
+        self.cur_time = t.value
+        if rc == capi.CYCAS_NOT_CONVERGED and k > 0:
+            row = its[k - 1]
+            bad = [q for q in range(8) if rs[k - 1][q] < 0]
+            q = bad[0] if bad else 0
+            raise ConvergeError(int(row[q]), 0.0, _SOLVE_NAMES[q])
+        capi.check(rc)
+        return {"n": n.value, "resmax": rm[:k], "residual": res[:k], "ksp_its": its[:k], "ksp_reason": rs[:k],
+                "cur_time": t.value}
+
     # ---- result files (NS/navierIO.cpp); k is the case of a batch, 0 otherwise
     def _case_handle(self, k: int):
         if k != 0:
@@ -223,7 +250,9 @@ class NavierStokesSolver:
     def NSSolve(self, max_step: int | None = None, residual_steady: float | None = None, callback=None,
                 output_dir: str | None = None, out_binary: bool = False, noutput: int | None = None,
                 async_output: bool = True):
-        """Steady outer loop (NS/navier.cpp:52-141): stop when ResMax < ResidualSteady.
+        """Outer loop (NS/navier.cpp:52-141).  Steady: SIMPLE iterations until ResMax <
+        ResidualSteady.  Transient: time steps (each ``time_step``) until the clock reaches
+        total_time.
 
         With ``output_dir`` the reference's files are written under it at the reference's
         cadence: the grid before the loop (tec/geo with ``out_binary``, else tec/grid.dat;
@@ -248,8 +277,14 @@ class NavierStokesSolver:
             else:
                 self.case.OutputGrid(os.path.join(tec, "grid.dat"))
         rm = None
+        transient = not getattr(self.case, "steady", True)
         for step in range(1, max_step + 1):
-            rm = self.simple_iteration()
+            if transient:  # one physical time step of outer iterations (navier.cpp:52-111)
+                r = self.time_step()
+                rm = float(r["resmax"][-1]) if r["n"] else 0.0
+                self.Residual = r["residual"][-1] if r["n"] else np.zeros(10)
+            else:
+                rm = self.simple_iteration()
             if callback:
                 callback(self.step, rm, self.Residual)
             if output_dir is not None and (step - 1) % nout == 0:
@@ -264,7 +299,10 @@ class NavierStokesSolver:
                         self.Output2TecplotBinary(data)
                     else:
                         self.Output2Tecplot(res)
-            if rm < tol:
+            if transient:
+                if self.cur_time >= self.case.total_time:
+                    break
+            elif rm < tol:
                 break
         if output_dir is not None:
             if async_output:

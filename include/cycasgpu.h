@@ -301,6 +301,23 @@ int cycas_dump_begin(cycas_ctx* ctx, int32_t k, const cycas_case* c, int32_t kin
                      const char* data_path, const char* backup_path);
 int cycas_dump_wait(cycas_ctx* ctx);
 
+/* ---- DataPartition::solve* (NS/MPIStructure.h:224-228) on the systems the context assembled
+ * last (the build_velocity / build_pressure stages, or the scalar rows of the keps / build_energy
+ * stages): x is the caller's host array, read as the initial guess and overwritten with the
+ * solution, as the reference writes into the caller's arrays in place.  tol is the relative
+ * tolerance, maxit the iteration cap; the context's preconditioner and restart apply.  A solve
+ * that ends with a negative converged reason returns CYCAS_NOT_CONVERGED (the reference's
+ * ConvergeError) with its report in stats.
+ * solveVelocity_GMRES (MPIStructure.cpp:234-375): Au with bu, bv, bw, three right-hand sides. */
+int cycas_solve_velocity(cycas_ctx* ctx, double tol, int32_t maxit, double* xu, double* xv, double* xw,
+                         cycas_iter_stats* stats);
+/* solvePressureCorrection (MPIStructure.cpp:449-531): Ap with bp from a zero initial guess; CG when
+ * is_symmetric, GMRES otherwise (the AMG preconditioner is replaced by Jacobi for GMRES). */
+int cycas_solve_pressure(cycas_ctx* ctx, double tol, int32_t maxit, double* xp, int32_t is_symmetric,
+                         cycas_iter_stats* stats);
+/* solveScarlar_GMRES (MPIStructure.cpp:378-446): As with bs. */
+int cycas_solve_scalar(cycas_ctx* ctx, double tol, int32_t maxit, double* xs, cycas_iter_stats* stats);
+
 /* Standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
  * col[nnz], double val[nnz]); b and x are host arrays, x holds the initial guess unless
  * guess_zero.  Same GMRES/PC as the SIMPLE path. */

@@ -595,19 +595,22 @@ void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const d
 
 // solveVelocity_GMRES (MPIStructure.cpp:234-375): one operator, three right-hand sides, run in
 // lockstep by one persistent launch (each system keeps its own GMRES state)
-void solve_velocity(cycas_ctx& c) {
+// xs_in: the three solution vectors (default: the context's U, V, W); conf: method override
+void solve_velocity(cycas_ctx& c, double* const* xs_in = nullptr, const KspConf* conf = nullptr) {
   require(c.nsolve + 3 <= 8, "too many solves in one iteration");
-  const KspConf& k = c.ksp[CYCAS_SYS_VELOCITY];
+  const KspConf& k = conf ? *conf : c.ksp[CYCAS_SYS_VELOCITY];
+  double* xs[3] = {c.f.U, c.f.V, c.f.W};
+  if (xs_in)
+    for (int q = 0; q < 3; q++) xs[q] = xs_in[q];
   if (k.type == CYCAS_KSP_CG || k.pc == CYCAS_PC_AMG) {  // non-default methods: one solve at a time
     require(!c.is_batch, "batches solve the momentum equations with GMRES");
-    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bu, c.f.U, false);
-    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bv, c.f.V, false);
-    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bw, c.f.W, false);
+    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bu, xs[0], false, conf);
+    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bv, xs[1], false, conf);
+    solve(c, CYCAS_SYS_VELOCITY, c.f.Au, c.f.dinv_u, c.f.bw, xs[2], false, conf);
     return;
   }
   GmresCall g[3];
   const double* bs[3] = {c.f.bu, c.f.bv, c.f.bw};
-  double* xs[3] = {c.f.U, c.f.V, c.f.W};
   const int slot0 = c.nsolve;
   for (int q = 0; q < 3; q++) {
     g[q].n = c.m.ncel;
@@ -1524,6 +1527,90 @@ int cycas_time_step(cycas_ctx* c, int32_t cap, int32_t* n_outer, double* res_his
     if (n_outer) *n_outer = done;
     if (cur_time) *cur_time = c->cur_time;
     return rc;
+  });
+}
+
+}  // extern "C"
+
+namespace {
+
+// the caller's vectors in and out of a device scratch area for the DataPartition::solve* mirrors
+double* solve_scratch(cycas_ctx& c) {
+  auto it = c.dfields.find("x_solve");
+  if (it != c.dfields.end()) return it->second.first;
+  return c.dfield("x_solve", 3L * c.m.ncel);
+}
+
+KspConf solve_conf(cycas_ctx& c, int sys, double tol, int maxit) {
+  require(tol > 0.0 && maxit > 0, "tol and maxIter must be positive");
+  KspConf k = c.ksp[sys];
+  k.rtol = tol;
+  k.maxit = maxit;
+  return k;
+}
+
+// runs `issue` (which queues the solves), copies the solutions back and reports like an iteration
+template <class F>
+int run_solves(cycas_ctx& c, double* const* hx, int nx, F issue, cycas_iter_stats* st) {
+  require(!c.is_batch, "the solve entry points take a single-case context");
+  const long n = c.m.ncel;
+  double* d = solve_scratch(c);
+  for (int q = 0; q < nx; q++) {
+    require(hx[q] != nullptr, "null solution vector");
+    CK(cudaMemcpyAsync(d + q * n, hx[q], sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+  }
+  CK(cudaMemsetAsync(c.st, 0, sizeof(DevStatus), c.stream));
+  c.nsolve = 0;
+  issue(d);
+  for (int q = 0; q < nx; q++)
+    CK(cudaMemcpyAsync(hx[q], d + q * n, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+  return finish_iteration(c, nullptr, nullptr, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int cycas_solve_velocity(cycas_ctx* c, double tol, int32_t maxit, double* xu, double* xv, double* xw,
+                         cycas_iter_stats* stats) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    KspConf k = solve_conf(*c, CYCAS_SYS_VELOCITY, tol, maxit);
+    double* hx[3] = {xu, xv, xw};
+    const long n = c->m.ncel;
+    return run_solves(*c, hx, 3, [&](double* d) {
+      double* xs[3] = {d, d + n, d + 2 * n};
+      solve_velocity(*c, xs, &k);
+    }, stats);
+  });
+}
+
+int cycas_solve_pressure(cycas_ctx* c, double tol, int32_t maxit, double* xp, int32_t is_symmetric,
+                         cycas_iter_stats* stats) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    KspConf k = solve_conf(*c, CYCAS_SYS_PRESSURE, tol, maxit);
+    if (!is_symmetric) {
+      k.type = CYCAS_KSP_GMRES;
+      if (k.pc == CYCAS_PC_AMG) k.pc = CYCAS_PC_JACOBI;
+    } else if (k.type != CYCAS_KSP_CG) {
+      k.type = CYCAS_KSP_CG;
+    }
+    double* hx[1] = {xp};
+    return run_solves(*c, hx, 1, [&](double* d) {
+      solve(*c, CYCAS_SYS_PRESSURE, c->f.Ap, c->f.dinv_p, c->f.bp, d, true, &k);
+    }, stats);
+  });
+}
+
+int cycas_solve_scalar(cycas_ctx* c, double tol, int32_t maxit, double* xs, cycas_iter_stats* stats) {
+  return guard([&]() -> int {
+    require(c != nullptr, "null context");
+    KspConf k = solve_conf(*c, CYCAS_SYS_SCALAR, tol, maxit);
+    double* hx[1] = {xs};
+    return run_solves(*c, hx, 1, [&](double* d) {
+      solve(*c, CYCAS_SYS_SCALAR, c->f.As, c->f.dinv_s, c->f.bs, d, false, &k);
+    }, stats);
   });
 }
 

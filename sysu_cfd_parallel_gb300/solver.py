@@ -191,6 +191,40 @@ class NavierStokesSolver:
         self.step += n
         return {"residual": res, "resmax": rm, "ksp_its": its, "ksp_reason": rs}
 
+    # ---- DataPartition::solve* (MPIStructure.h:224-228) on the last assembled systems; the
+    # arrays are solved in place, as the reference writes into the caller's arrays
+    def _solved(self, rc, st, name):
+        self.last_stats = st
+        if rc == capi.CYCAS_NOT_CONVERGED and st.failed_solve >= 0:
+            k = st.failed_solve
+            raise ConvergeError(st.its[k], st.rnorm[k], name)
+        capi.check(rc)
+        return st
+
+    def solveVelocity_GMRES(self, tol: float, maxIter: int, xu: np.ndarray, xv: np.ndarray, xw: np.ndarray):
+        st = capi.IterStats()
+        for x in (xu, xv, xw):
+            if x.dtype != np.float64 or not x.flags.c_contiguous:
+                raise TypeError("solution arrays must be contiguous float64")
+        rc = capi.load().cycas_solve_velocity(self._h, tol, maxIter, capi.ptr(xu), capi.ptr(xv), capi.ptr(xw),
+                                              C.byref(st))
+        return self._solved(rc, st, "Un")
+
+    def solvePressureCorrection(self, tol: float, maxIter: int, xp: np.ndarray, isSymmetric: bool = True):
+        st = capi.IterStats()
+        if xp.dtype != np.float64 or not xp.flags.c_contiguous:
+            raise TypeError("solution array must be contiguous float64")
+        rc = capi.load().cycas_solve_pressure(self._h, tol, maxIter, capi.ptr(xp), 1 if isSymmetric else 0,
+                                              C.byref(st))
+        return self._solved(rc, st, "Pn")
+
+    def solveScarlar_GMRES(self, tol: float, maxIter: int, xs: np.ndarray):
+        st = capi.IterStats()
+        if xs.dtype != np.float64 or not xs.flags.c_contiguous:
+            raise TypeError("solution array must be contiguous float64")
+        rc = capi.load().cycas_solve_scalar(self._h, tol, maxIter, capi.ptr(xs), C.byref(st))
+        return self._solved(rc, st, "scalar")
+
     def time_step(self, cap: int = 64):
         """One physical time step of a transient case (cycas_time_step): returns dict(n,
         resmax [n], residual [n, 10], ksp_its [n, 8], ksp_reason [n, 8], cur_time)."""

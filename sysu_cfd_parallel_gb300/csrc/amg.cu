@@ -541,6 +541,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
 }
 
 __global__ void __launch_bounds__(kGmThreads, 1) k_cg_amg(CgAmgArgs a) {
+  if (launch_failed(a.err)) return;
   if (!a.sched) {
     const Team T{(int)blockIdx.x, a.nb, a.bar, a.part};
     cg_amg_team(a, T, 0);

@@ -103,18 +103,36 @@ __device__ __forceinline__ void row_gather_ms(const int* __restrict__ rowptr, co
   }
 }
 
-// w + sum_{q < cnt} coef[q] * V[q*ldv + r] in the basis precision, ascending q
+// w + sum_{q < cnt} coef[q] * V[q*ldv + r] in the basis precision, ascending q.  The
+// coefficients are already in the basis precision: converting FP64 to FP32 per element would
+// run on the FP64 pipe.
 template <class T>
-__device__ __forceinline__ T basis_axpy(T w, const T* V, long ldv, int r, const double* coef, int cnt) {
+__device__ __forceinline__ T basis_axpy(T w, const T* V, long ldv, int r, const T* coef, int cnt) {
   for (int q0 = 0; q0 < cnt; q0 += 8) {
     T v[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) v[k] = (q0 + k < cnt) ? __ldcg(V + (long)(q0 + k) * ldv + r) : T(0);
 #pragma unroll
     for (int k = 0; k < 8; k++)
-      if (q0 + k < cnt) w = fma((T)coef[q0 + k], v[k], w);
+      if (q0 + k < cnt) w = fma(coef[q0 + k], v[k], w);
   }
   return w;
+}
+
+// sum of load(blk) over blk = lane, lane + 32, lane + 64, ... < nb, added in that order (the
+// order every CTA uses); the loads of up to eight terms are in flight together
+template <class F>
+__device__ __forceinline__ double lane_sum(int lane, int nb, F load) {
+  double sum = 0.0;
+  for (int b0 = lane; b0 < nb; b0 += 32 * 8) {
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = b0 + 32 * k < nb ? load(b0 + 32 * k) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (b0 + 32 * k < nb) sum += v[k];
+  }
+  return sum;
 }
 
 template <int NS, class Tv>
@@ -124,6 +142,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
   __shared__ double s_hh[NS][(M + 1) * M];
   __shared__ double s_cc[NS][M], s_ss[NS][M], s_grs[NS][M + 1], s_nrs[NS][M];
   __shared__ double s_scale[NS][M + 1], s_h[NS][M + 1], s_coef[NS][M + 1];
+  __shared__ Tv s_coefT[NS][M + 1];  // s_coef in the basis precision
   __shared__ double s_pair[MAXP > 32 ? MAXP : 32];
   __shared__ double s_red[kDotGroup], s_warp[kGmWarps * kDotGroup];
   __shared__ double s_rnorm0[NS], s_ttol[NS], s_rnorm[NS], s_cyc[NS];
@@ -139,6 +158,28 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
   auto part_of = [&](int blk, int s) { return T.part + ((long)blk * NS + s) * kPartStride; };
   auto Vv = [&](int s, int q) { return a.V + ((long)s * (m + 1) + q) * a.ldv; };
   const bool mixed = a.inner_rtol > 0.0;
+
+  // w_s = D^-1 A v_{s,it[s]} / |v_{s,it[s]}| into v_{s,it[s]+1} for the systems in mask, over this
+  // CTA's rows taken by threads t0, t0 + stride, ...; a row's arithmetic does not depend on the
+  // thread that computes it
+  auto arnoldi_spmv = [&](unsigned mask, const int* it, int t0, int stride) {
+    const Tv* vj[NS];
+    Tv sj[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      vj[s] = Vv(s, it[s]);
+      sj[s] = (Tv)s_scale[s][it[s]];
+    }
+    for (int r = r0 + t0; r < r1; r += stride) {
+      Tv acc[NS];
+      row_gather_ms<NS, Tv>(a.rowptr, a.col, a.valT, r, vj, mask, acc);
+      const Tv d = a.dinvT ? a.dinvT[r] : Tv(1);
+#pragma unroll
+      for (int s = 0; s < NS; s++)
+        if ((mask >> s) & 1u) Vv(s, it[s] + 1)[r] = (acc[s] * sj[s]) * d;
+    }
+  };
+  unsigned spec_prev = 0;  // systems whose next Arnoldi product was computed during the last control phase
 
   if (tid < NS) {
     s_mode[tid] = M_START;
@@ -169,7 +210,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
       if (mode[s] == M_RESTART || mode[s] == M_FINAL) {
         const int cnt = s_nupd[s];
         for (int r = r0 + tid; r < r1; r += kGmThreads) {
-          const Tv t = basis_axpy<Tv>(Tv(0), Vv(s, 0), a.ldv, r, s_coef[s], cnt);
+          const Tv t = basis_axpy<Tv>(Tv(0), Vv(s, 0), a.ldv, r, s_coefT[s], cnt);
           a.x[s][r] += (double)t;
         }
       } else if (mode[s] == M_START && a.guess_zero) {
@@ -178,21 +219,8 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
       if (mode[s] == M_ARNOLDI) arn |= 1u << s;
     }
     if (arn) {
-      const Tv* vj[NS];
-      Tv sj[NS];
-#pragma unroll
-      for (int s = 0; s < NS; s++) {
-        vj[s] = Vv(s, itv[s]);
-        sj[s] = (Tv)s_scale[s][itv[s]];
-      }
-      for (int r = r0 + tid; r < r1; r += kGmThreads) {
-        Tv acc[NS];
-        row_gather_ms<NS, Tv>(a.rowptr, a.col, a.valT, r, vj, arn, acc);
-        const Tv d = a.dinvT ? a.dinvT[r] : Tv(1);
-#pragma unroll
-        for (int s = 0; s < NS; s++)
-          if ((arn >> s) & 1u) Vv(s, itv[s] + 1)[r] = (acc[s] * sj[s]) * d;
-      }
+      const unsigned todo = arn & ~spec_prev;
+      if (todo) arnoldi_spmv(todo, itv, tid, kGmThreads);
       // pairs (system, basis vector) for the dot products
       if (tid == 0) {
         int p = 0;
@@ -251,13 +279,13 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
       for (int p = wid; p < P; p += kGmWarps) {
         const int s = s_ps[p], q = s_pq[p];
         const double* base = T.part + (long)s * kPartStride + q;
-        double sum = 0.0;
-        for (int blk = lane; blk < nb; blk += 32) sum += ldcg(base + (long)blk * NS * kPartStride);
+        double sum = lane_sum(lane, nb, [&](int blk) { return ldcg(base + (long)blk * NS * kPartStride); });
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
         if (lane == 0) {
           const double h = sum * s_scale[s][q];
           s_h[s][q] = h;
           s_coef[s][q] = -(h * s_scale[s][q]);  // w -= h v_q / |v_q|
+          s_coefT[s][q] = (Tv)s_coef[s][q];
         }
       }
       __syncthreads();
@@ -269,7 +297,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
         Tv* w = Vv(s, itv[s] + 1);
         Tv nt = Tv(0);
         for (int r = r0 + tid; r < r1; r += kGmThreads) {
-          const Tv wr = basis_axpy<Tv>(__ldcg(w + r), Vv(s, 0), a.ldv, r, s_coef[s], itv[s] + 1);
+          const Tv wr = basis_axpy<Tv>(__ldcg(w + r), Vv(s, 0), a.ldv, r, s_coefT[s], itv[s] + 1);
           w[r] = wr;
           nt += wr * wr;
         }
@@ -315,27 +343,51 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
     if (!grid_barrier(T.bar, nb, a.err)) return;
 
     // ------------------------------------------------------------ phase Z (warp s controls system s)
+    // Systems whose cycle goes on unless this step meets the tolerance get their next Arnoldi
+    // product now, from the warps that do not control a system, while the control warps apply
+    // the Givens rotations (serial FP64 work); a cycle that ends discards that product.
+    unsigned spec = 0;
+#pragma unroll
+    for (int s = 0; s < NS; s++)
+      if (mode[s] == M_ARNOLDI && itv[s] + 1 < m && s_its[s] + 1 < a.maxit) spec |= 1u << s;
+    double tt = 0.0;  // the new subdiagonal entry, on lane 0 of the control warp
+    if (wid < NS && mode[wid] == M_ARNOLDI) {
+      const int s = wid;
+      double sum = lane_sum(lane, nb, [&](int blk) { return ldcg(part_of(blk, s) + kNorm); });
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+      double* hh = s_hh[s] + itv[s] * (m + 1);  // the new Hessenberg column, copied by the warp
+      for (int q = lane; q <= itv[s]; q += 32) hh[q] = s_h[s][q];
+      if (lane == 0) {
+        tt = sqrt(sum);
+        s_scale[s][itv[s] + 1] = __drcp_rn(tt);  // 1 / tt, correctly rounded
+      }
+    }
+    __syncthreads();
+    if (wid >= NS && spec) {
+      int itn[NS];
+#pragma unroll
+      for (int s = 0; s < NS; s++) itn[s] = itv[s] + 1;
+      arnoldi_spmv(spec, itn, tid - NS * 32, kGmThreads - NS * 32);
+    }
     if (wid < NS) {
       const int s = wid;
       const int md = mode[s];
       if (md == M_ARNOLDI) {
-        double sum = 0.0;
-        for (int blk = lane; blk < nb; blk += 32) sum += ldcg(part_of(blk, s) + kNorm);
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
         if (lane == 0) {
           const int it = itv[s];
-          const double tt = sqrt(sum);
           double* hh = s_hh[s] + it * (m + 1);
-          for (int q = 0; q <= it; q++) hh[q] = s_h[s][q];
           hh[it + 1] = tt;
-          s_scale[s][it + 1] = 1.0 / tt;
           // happy breakdown: tt < min(|tt / g_it|, haptol); the division only when tt < haptol
           const bool hapend = tt < a.haptol && tt < fabs(tt / s_grs[s][it]);
+          // the previous rotations applied to the new column; the entry carried from one
+          // rotation to the next stays in a register
+          double carry = hh[0];
           for (int j = 1; j <= it; j++) {
-            const double t0 = hh[j - 1];
-            hh[j - 1] = s_cc[s][j - 1] * t0 + s_ss[s][j - 1] * hh[j];
-            hh[j] = s_cc[s][j - 1] * hh[j] - s_ss[s][j - 1] * t0;
+            const double hj = hh[j], c = s_cc[s][j - 1], sn = s_ss[s][j - 1];
+            hh[j - 1] = c * carry + sn * hj;
+            carry = c * hj - sn * carry;
           }
+          hh[it] = carry;
           int rs = 0, used = it;
           bool brk = false;
           double res = s_rnorm[s];
@@ -345,7 +397,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
               rs = -5;
               brk = true;
             } else {
-              const double rd = 1.0 / d;
+              const double rd = __drcp_rn(d);
               s_cc[s][it] = hh[it] * rd;
               s_ss[s][it] = hh[it + 1] * rd;
               s_grs[s][it + 1] = -(s_ss[s][it] * s_grs[s][it]);
@@ -391,7 +443,10 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
                   for (int j = q + 1; j <= k; j++) t = t - HH(q, j) * s_nrs[s][j];
                   s_nrs[s][q] = t / HH(q, q);
                 }
-                for (int j = 0; j <= k; j++) s_coef[s][j] = s_nrs[s][j] * s_scale[s][j];
+                for (int j = 0; j <= k; j++) {
+                  s_coef[s][j] = s_nrs[s][j] * s_scale[s][j];
+                  s_coefT[s][j] = (Tv)s_coef[s][j];
+                }
                 nup = used;
               }
             }
@@ -407,11 +462,8 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
           }
         }
       } else if (md == M_START || md == M_RESTART) {
-        double s0 = 0.0, s1 = 0.0;
-        for (int blk = lane; blk < nb; blk += 32) {
-          s0 += ldcg(part_of(blk, s) + kInit);
-          s1 += ldcg(part_of(blk, s) + kInit + 1);
-        }
+        double s0 = lane_sum(lane, nb, [&](int blk) { return ldcg(part_of(blk, s) + kInit); });
+        double s1 = lane_sum(lane, nb, [&](int blk) { return ldcg(part_of(blk, s) + kInit + 1); });
         for (int o = 16; o > 0; o >>= 1) {
           s0 += __shfl_down_sync(0xffffffffu, s0, o);
           s1 += __shfl_down_sync(0xffffffffu, s1, o);
@@ -449,6 +501,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
       }
     }
     __syncthreads();
+    spec_prev = spec;
   }
   if (T.rank == 0 && tid < NS) {
     out[tid]->its = s_its[tid];
@@ -460,6 +513,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
 
 template <int NS, class Tv>
 __global__ void __launch_bounds__(kGmThreads, 1) k_gmres_ms(GmMsArgs<NS, Tv> a) {
+  if (launch_failed(a.err)) return;
   if (!a.sched) {
     const Team T{(int)blockIdx.x, a.nb, a.bar, a.part};
     gmres_team<NS, Tv>(a, T, 0, a.n, a.out);

@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_cg(CgArgs a) {
   __shared__ double s_warp[kGmWarps * kDotGroup];
   __shared__ double s_red[kDotGroup];
   __shared__ double s_g[4];
+  if (launch_failed(a.err)) return;
   const int nb = a.nb, tid = threadIdx.x;
   const int r0 = blockIdx.x * a.chunk;
   const int r1 = min(a.n, r0 + a.chunk);

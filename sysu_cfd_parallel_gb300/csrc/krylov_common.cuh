@@ -34,33 +34,51 @@ inline cudaError_t launch_cooperative(const void* fn, int grid, int block, void*
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
-// bounded grid barrier for a cooperative launch
+// gpu-scope acquire load (PTX memory model): what the releasing CTAs wrote before the barrier
+// word changed is visible after it
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// true when an earlier kernel or stage recorded an error: every CTA of a persistent Krylov
+// kernel reads the same value at its start (nothing writes it during the launch but a barrier
+// that gave up), so either all CTAs run or none does
+__device__ __forceinline__ bool launch_failed(const int* err) { return *(const volatile int*)err != 0; }
+
+// bounded grid barrier for a cooperative launch.  Thread 0 of each CTA arrives with a fenced
+// atomic increment; the last arrival resets the count and advances the generation word, which
+// the others wait for with acquire loads.  A wait that outlasts kSpinLimit, or that sees another
+// CTA give up, records bit 0 in *err and returns false (the kernel then returns).
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nb, int* err) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* gen = bar + 1;
-    unsigned g = *gen;
+    const unsigned g = *(volatile unsigned*)(bar + 1);
     __threadfence();
-    unsigned arrived = atomicAdd(bar, 1u);
+    const unsigned arrived = atomicAdd(bar, 1u);
     int ok = 1;
     if (arrived == nb - 1) {
       atomicExch(bar, 0u);
       __threadfence();
       atomicAdd(bar + 1, 1u);
     } else {
-      long long t0 = clock64();
-      while (*gen == g) {
+      const long long t0 = clock64();
+      unsigned spins = 0;
+      while (ld_acquire_gpu(bar + 1) == g) {
+        if ((++spins & 63u) == 0 && (*(volatile int*)err & 1)) {  // another CTA gave up
+          ok = 0;
+          break;
+        }
         if (clock64() - t0 > kSpinLimit) {
           atomicOr(err, 1);
           ok = 0;
           break;
         }
-        __nanosleep(64);
+        __nanosleep(32);
       }
     }
-    __threadfence();
-    if (*(volatile int*)err) ok = 0;
     s_ok = ok;
   }
   __syncthreads();

@@ -22,6 +22,8 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=20, help="cavity cells per side")
     ap.add_argument("--iters", type=int, default=2)
     ap.add_argument("--pressure-pc", default="amg", choices=["amg", "jacobi"])
+    ap.add_argument("--mixed", action="store_true", help="FP32 Arnoldi cycles in FP64 refinement")
+    ap.add_argument("--warmup", type=int, default=0, help="untimed iterations before the profiled ones")
     args = ap.parse_args(argv)
 
     from . import capi, meshgen
@@ -34,8 +36,12 @@ def main(argv=None):
         param = meshgen.write_case(d, "cavity", n=args.n, steps=args.iters)
     opt = capi.default_options(pc=capi.PC_JACOBI)
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG if args.pressure_pc == "amg" else capi.PC_JACOBI
+    opt.mixed = 1 if args.mixed else 0
     s = NavierStokesSolver(Case(param), opt)
+    if args.warmup:
+        s.iterate(args.warmup)
     s.set_profiling(True)
+    s.reset_profile()
     t0 = time.time()
     r = s.iterate(args.iters)
     dt = time.time() - t0

@@ -243,6 +243,75 @@ def serve_requests(args):
     return reqs
 
 
+def run_transient(args):
+    """Transient workload: the 480k-tet k-epsilon channel with the energy equation, the
+    reference's second-order ("Dual") time scheme, dt 0.1 and at most 9 outer iterations per
+    time step.  value: outer-iteration cell-iterations/s over `steps` time steps; the CPU sample
+    is the oracle on the same mesh for one time step of one outer iteration."""
+    import torch
+    from sysu_cfd_parallel_gb300 import capi, meshgen
+    from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    make_case()  # the headline mesh
+    mesh = os.path.join(case_dir(), "case.msh")
+    d = os.path.join(os.path.dirname(case_dir()), "transient_channel_200x20x20")
+    os.makedirs(d, exist_ok=True)
+    param = os.path.join(d, "param.in")
+    with open(param, "w") as f:
+        f.write(meshgen.channel_param(mesh, time=(0.1, 10.0, 10, "Dual"), energy=True, wall_t=290, t_in=300))
+    case = Case(param)
+    opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+    opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
+    s = NavierStokesSolver(case, opt)
+    stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
+    for _ in range(max(1, args.warmup)):
+        s.time_step()
+    clocks = Clocks(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    outer = 0
+    for _ in range(args.steps):
+        outer += s.time_step()["n"]
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    cpu = None
+    if not args.no_cpu_baseline:
+        import importlib
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        po = importlib.import_module("pyoracle")
+        d1 = os.path.join(os.path.dirname(case_dir()), "transient_channel_200x20x20_cpu")
+        os.makedirs(d1, exist_ok=True)
+        p1 = os.path.join(d1, "param.in")
+        with open(p1, "w") as f:
+            f.write(meshgen.channel_param(mesh, time=(0.1, 10.0, 2, "Dual"), energy=True, wall_t=290, t_in=300))
+        o = po.OracleCase(p1)
+        for w in (po.VELOCITY, po.PRESSURE, po.SCALAR):
+            o.set_ksp(w, po.PC_ILU0, 30)
+        t0 = time.time()
+        r = o.time_step()
+        dt = time.time() - t0
+        cpu = {"value": case.ncel * r["n"] / dt, "unit": "cell-iters/s", "cores": 1, "kind": "port",
+               "sample": f"one time step ({r['n']} outer iteration) of the same case, oracle with ILU(0), "
+                         f"{dt:.1f} s"}
+    line = {"metric": "cell-iters/s (transient SIMPLE-C outer iterations, k-eps + energy channel 480k tets)",
+            "value": case.ncel * outer / (ms / 1e3), "unit": "cell-iters/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(1, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "time_steps_per_s": args.steps / (ms / 1e3), "outer_iterations": outer,
+            "config": {"workload": "kepsilon + energy channel 200x20x20x6 jittered tets (480000 cells), transient "
+                                   "Dual scheme, dt 0.1, MaxOuterStep 10", "cells": case.ncel,
+                       "step": "one physical time step"},
+            "cpu_baseline": cpu, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    s.close()
+
+
 def run_precision(args):
     """Precision workload: the 400x40x40x6 channel (3.84M tets, seed 2027), plain FP64 against
     mixed-precision GMRES from the same initial state for the same iterations; throughput of
@@ -756,7 +825,7 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision and batched lines")
-    ap.add_argument("--workload", default="channel", choices=["channel", "serve", "precision"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "serve", "precision", "transient"])
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--drain", type=float, default=120.0)
@@ -773,6 +842,8 @@ def main():
         run_serve(args)
     elif args.workload == "precision":
         run_precision(args)
+    elif args.workload == "transient":
+        run_transient(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

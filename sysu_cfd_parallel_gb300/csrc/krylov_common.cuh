@@ -47,26 +47,30 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
 // that gave up), so either all CTAs run or none does
 __device__ __forceinline__ bool launch_failed(const int* err) { return *(const volatile int*)err != 0; }
 
-// bounded grid barrier for a cooperative launch.  Thread 0 of each CTA arrives with a fenced
-// atomic increment; the last arrival resets the count and advances the generation word, which
-// the others wait for with acquire loads.  A wait that outlasts kSpinLimit, or that sees another
-// CTA give up, records bit 0 in *err and returns false (the kernel then returns).
+// gpu-scope release increment of the barrier counter; returns the value before it
+__device__ __forceinline__ unsigned atom_add_release_gpu(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.release.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+// bounded grid barrier for a cooperative launch: a counting barrier on bar[0], zeroed before
+// the launch.  Thread 0 of each CTA adds one with release semantics; the k-th barrier of the
+// launch is complete when the counter reaches k * nb, which the value returned by the CTA's own
+// increment gives (old / nb + 1) * nb, so no CTA keeps state between barriers.  Waiting is a
+// poll with acquire loads.  A wait that outlasts kSpinLimit, or that sees another CTA give up,
+// records bit 0 in *err and returns false (the kernel then returns).
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nb, int* err) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned g = *(volatile unsigned*)(bar + 1);
-    __threadfence();
-    const unsigned arrived = atomicAdd(bar, 1u);
+    const unsigned old = atom_add_release_gpu(bar, 1u);
+    const unsigned target = (old / nb + 1u) * nb;
     int ok = 1;
-    if (arrived == nb - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
+    if (old + 1u != target) {
       const long long t0 = clock64();
       unsigned spins = 0;
-      while (ld_acquire_gpu(bar + 1) == g) {
+      while ((int)(ld_acquire_gpu(bar) - target) < 0) {
         if ((++spins & 63u) == 0 && (*(volatile int*)err & 1)) {  // another CTA gave up
           ok = 0;
           break;
@@ -78,6 +82,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nb, int* er
         }
         __nanosleep(32);
       }
+    } else {
+      __threadfence();  // the last arrival acquires every other CTA's writes
     }
     s_ok = ok;
   }

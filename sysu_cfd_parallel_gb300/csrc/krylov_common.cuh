@@ -102,10 +102,12 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double* s_warp /*[k
     if (lane == 0) s_warp[wid * K + k] = t;
   }
   __syncthreads();
-  if (threadIdx.x < K) {
-    double s = 0.0;
-    for (int w = 0; w < kGmWarps; w++) s += s_warp[w * K + threadIdx.x];
-    s_out[threadIdx.x] = s;
+  // warp k sums the per-warp values of quantity k as a shuffle tree (a serial chain of 32 FP64
+  // additions in one thread would cost 32 FP64 latencies)
+  if (wid < K) {
+    double t = s_warp[lane * K + wid];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) s_out[wid] = t;
   }
   __syncthreads();
 }
@@ -114,7 +116,14 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double* s_warp /*[k
 __device__ __forceinline__ double warp_sum_blocks(const double* part, int stride, int q, int nb) {
   const int lane = threadIdx.x & 31;
   double s = 0.0;
-  for (int b = lane; b < nb; b += 32) s += ldcg(part + (long)b * stride + q);
+  for (int b0 = lane; b0 < nb; b0 += 32 * 8) {  // same order, up to eight loads in flight
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = b0 + 32 * k < nb ? ldcg(part + (long)(b0 + 32 * k) * stride + q) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (b0 + 32 * k < nb) s += v[k];
+  }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   return __shfl_sync(0xffffffffu, s, 0);
 }

@@ -757,12 +757,12 @@ def run_gpu(args):
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
+    up = {nm: host[nm] for nm in names_in}
+    down = {nm: host[nm] for nm in names_out}
     for _ in range(e2e_steps):
-        for nm in names_in:
-            s.set(nm, host[nm])
+        s.set_fields(up)
         s.simple_iteration()
-        for nm in names_out:
-            host[nm][:] = s.get(nm)
+        s.get_fields(down)
     f1.record(stream)
     f1.synchronize()
     e2e_ms = f0.elapsed_time(f1)

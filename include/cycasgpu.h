@@ -202,6 +202,12 @@ void cycas_destroy(cycas_ctx* ctx);
 int cycas_get_field(cycas_ctx* ctx, const char* name, double* dst, int64_t n);
 int cycas_set_field(cycas_ctx* ctx, const char* name, const double* src, int64_t n);
 int cycas_get_int(cycas_ctx* ctx, const char* name, int32_t* dst, int64_t n); /* A_rowptr, A_col */
+/* Several named arrays in one call (the cycas_set_fields / cycas_get_fields of the proposed
+ * replacement surface): array i is names[i], n[i] doubles at src[i] / dst[i].  All names and
+ * sizes are checked first; the copies are queued on the context's stream and waited for once. */
+int cycas_set_fields(cycas_ctx* ctx, int32_t count, const char* const* names, const double* const* src,
+                     const int64_t* n);
+int cycas_get_fields(cycas_ctx* ctx, int32_t count, const char* const* names, double* const* dst, const int64_t* n);
 
 /* One physical time step of a transient context (NS/navier.cpp:52-111): SaveTransientOldData
  * (navier.cpp:698-740), the clock advanced by dt, then outer SIMPLE iterations (momentum,

@@ -90,7 +90,7 @@ EXPORTS = (
     "cycas_dump_begin", "cycas_dump_wait",
     "cycas_create", "cycas_create_from_case", "cycas_destroy",
     "cycas_get_field", "cycas_set_field", "cycas_get_int", "cycas_simple_iteration", "cycas_simple_iterations",
-    "cycas_time_step", "cycas_case_physics", "cycas_solve_velocity", "cycas_solve_pressure", "cycas_solve_scalar",
+    "cycas_time_step", "cycas_case_physics", "cycas_set_fields", "cycas_get_fields", "cycas_solve_velocity", "cycas_solve_pressure", "cycas_solve_scalar",
     "cycas_run_stage", "cycas_csr_solve", "cycas_get_stream", "cycas_set_profiling", "cycas_get_profile",
     "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels", "cycas_batch_create",
     "cycas_batch_size", "cycas_batch_offsets", "cycas_batch_iteration", "cycas_batch_residuals",
@@ -150,6 +150,8 @@ def load(build_if_missing: bool = True):
     L.cycas_get_field.argtypes = [_P, C.c_char_p, _P, C.c_int64]
     L.cycas_set_field.argtypes = [_P, C.c_char_p, _P, C.c_int64]
     L.cycas_get_int.argtypes = [_P, C.c_char_p, _P, C.c_int64]
+    L.cycas_set_fields.argtypes = [_P, C.c_int32, _P, _P, _P]
+    L.cycas_get_fields.argtypes = [_P, C.c_int32, _P, _P, _P]
     L.cycas_simple_iteration.argtypes = [_P, _F64P, _F64P, C.POINTER(IterStats)]
     L.cycas_simple_iterations.argtypes = [_P, C.c_int32, _P, _P, _P, _P]
     L.cycas_run_stage.argtypes = [_P, C.c_char_p]

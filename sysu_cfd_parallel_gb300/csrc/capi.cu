@@ -1456,6 +1456,37 @@ int cycas_set_field(cycas_ctx* c, const char* name, const double* src, int64_t n
   });
 }
 
+int cycas_set_fields(cycas_ctx* c, int32_t count, const char* const* names, const double* const* src,
+                     const int64_t* n) {
+  return guard([&]() -> int {
+    require(c && count >= 0 && (count == 0 || (names && src && n)), "null argument");
+    for (int i = 0; i < count; i++) {  // every name and size checked before any copy is queued
+      require(names[i] && src[i], "null field name or array");
+      require(lookup(*c, names[i]).second == n[i], std::string("size mismatch for ") + names[i]);
+    }
+    for (int i = 0; i < count; i++)
+      CK(cudaMemcpyAsync(lookup(*c, names[i]).first, src[i], sizeof(double) * n[i], cudaMemcpyHostToDevice,
+                         c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CYCAS_OK;
+  });
+}
+
+int cycas_get_fields(cycas_ctx* c, int32_t count, const char* const* names, double* const* dst, const int64_t* n) {
+  return guard([&]() -> int {
+    require(c && count >= 0 && (count == 0 || (names && dst && n)), "null argument");
+    for (int i = 0; i < count; i++) {
+      require(names[i] && dst[i], "null field name or array");
+      require(lookup(*c, names[i]).second == n[i], std::string("size mismatch for ") + names[i]);
+    }
+    for (int i = 0; i < count; i++)
+      CK(cudaMemcpyAsync(dst[i], lookup(*c, names[i]).first, sizeof(double) * n[i], cudaMemcpyDeviceToHost,
+                         c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return CYCAS_OK;
+  });
+}
+
 int cycas_get_int(cycas_ctx* c, const char* name, int32_t* dst, int64_t n) {
   return guard([&]() -> int {
     require(c && name && dst, "null argument");

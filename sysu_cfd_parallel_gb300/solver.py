@@ -146,6 +146,28 @@ class NavierStokesSolver:
         a = np.ascontiguousarray(values, dtype=np.float64)
         capi.check(capi.load().cycas_set_field(self._h, name.encode(), capi.ptr(a), a.size))
 
+    def _many(self, fn, arrays: dict, host_to_device: bool):
+        names = list(arrays)
+        k = len(names)
+        nm = (C.c_char_p * k)(*[x.encode() for x in names])
+        ptrs = (C.c_void_p * k)()
+        sizes = (C.c_int64 * k)()
+        for q, x in enumerate(names):
+            a = arrays[x]
+            if a.dtype != np.float64 or not a.flags.c_contiguous or (not host_to_device and not a.flags.writeable):
+                raise TypeError(f"{x}: contiguous float64 array required")
+            ptrs[q] = a.ctypes.data
+            sizes[q] = a.size
+        capi.check(fn(self._h, k, nm, ptrs, sizes))
+
+    def set_fields(self, arrays: dict) -> None:
+        """Uploads several named arrays with one synchronisation (cycas_set_fields)."""
+        self._many(capi.load().cycas_set_fields, arrays, True)
+
+    def get_fields(self, arrays: dict) -> None:
+        """Fills the given arrays from the named device arrays with one synchronisation."""
+        self._many(capi.load().cycas_get_fields, arrays, False)
+
     def get_int(self, name: str) -> np.ndarray:
         n = self.case.ncel + 1 if name == "A_rowptr" else self.case.nnz
         out = np.empty(n, dtype=np.int32)

@@ -82,3 +82,22 @@ def test_seam_reports_non_convergence(cases):
         g.solveVelocity_GMRES(1e-14, 1, *xs)
     with pytest.raises(capi.CycasError):
         g.solveScarlar_GMRES(-1.0, 10, xs[0])
+
+
+def test_set_and_get_fields_in_one_call(cases):
+    g = NavierStokesSolver(Case(cases("channel_tiny")), capi.default_options(pc=capi.PC_JACOBI))
+    n = g.case.ncel
+    rng = np.random.default_rng(5)
+    vals = {nm: rng.standard_normal(n) for nm in ("U", "V", "W", "P", "TE")}
+    g.set_fields(vals)
+    for nm, v in vals.items():
+        assert np.array_equal(g.get(nm), v), nm
+    out = {nm: np.empty(n) for nm in vals}
+    g.get_fields(out)
+    for nm in vals:
+        assert np.array_equal(out[nm], vals[nm]), nm
+    # a bad size anywhere rejects the whole call before anything is copied
+    bad = {"U": np.zeros(n), "V": np.zeros(n - 1)}
+    with pytest.raises(capi.CycasError):
+        g.set_fields(bad)
+    assert np.array_equal(g.get("U"), vals["U"])

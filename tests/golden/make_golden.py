@@ -9,7 +9,8 @@ oracle's outputs on them:
 * geometry (CellFaceInfo, geometry.cpp:391-752);
 * the fields, residual history and Krylov iteration counts after ``steps`` SIMPLE-C iterations
   (navier.cpp:60-111) with Jacobi-preconditioned GMRES(30) and CG for the pressure correction
-  at the reference's tolerances.
+  at the reference's tolerances -- or, for the transient cases, after ``steps`` physical time
+  steps (outer iterations of each, ``nouter``), with temperature and density.
 
 The reference itself cannot be built (it needs MPI, PETSc, METIS and CGNS), so these vectors
 pin the oracle and the GPU path against each other and against regressions, not against an
@@ -30,6 +31,11 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 CASES = {
     "cavity5j": dict(kind="cavity", n=5, jitter=0.1, seed=7, mu=0.02, steps=50, golden_steps=8),
     "channel_tiny": dict(kind="channel", nx=10, ny=2, nz=2, steps=20, golden_steps=6),
+    # transient cases: golden_steps physical time steps of outer iterations
+    "cavity5g_dual": dict(kind="cavity", n=5, jitter=0.1, seed=9, density=1, wall_t=300, lid_t=330,
+                          time=(0.05, 1.0, 8, "Dual"), golden_steps=3),
+    "channel_tiny_tr": dict(kind="channel", nx=10, ny=2, nz=2, time=(0.1, 1.0, 6, "Euler"), energy=True,
+                            wall_t=290, golden_steps=3),
 }
 INT_ARRAYS = ["face_cell1", "face_cell2", "face_bnd", "face_vertices", "cell_nface", "cell_face", "cell_cell",
               "cell_vertices", "bnd_face", "bnd_type", "A_rowptr", "A_col"]
@@ -56,11 +62,19 @@ def oracle_outputs(param, steps):
         o.set_ksp(w, po.PC_JACOBI, 30)
     out = {nm: o.geti(nm) for nm in INT_ARRAYS}
     out.update({nm: o.get(nm) for nm in GEOMETRY})
-    r = o.iterate(steps)
-    out["resmax"] = r["resmax"]
-    out["residual"] = r["residual"]
-    out["ksp_its"] = r["ksp_its"]
-    for nm in FIELDS + (FIELDS_KE if o.turb == 1 else []):
+    transient = not o.physics()["steady"]
+    if transient:
+        rs = [o.time_step() for _ in range(steps)]
+        out["nouter"] = np.array([r["n"] for r in rs])
+        out["resmax"] = np.concatenate([r["resmax"] for r in rs])
+        out["residual"] = np.concatenate([r["residual"] for r in rs])
+        out["ksp_its"] = np.concatenate([r["ksp_its"] for r in rs])
+    else:
+        r = o.iterate(steps)
+        out["resmax"] = r["resmax"]
+        out["residual"] = r["residual"]
+        out["ksp_its"] = r["ksp_its"]
+    for nm in FIELDS + (FIELDS_KE if o.turb == 1 else []) + (["T", "R"] if transient else []):
         out[nm] = o.get(nm)
     out["steps"] = np.array(steps)
     return out

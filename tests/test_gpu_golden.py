@@ -1,7 +1,8 @@
 """GPU path (through the C ABI) against the committed golden fixtures of tests/golden/.
 
-Geometry and the CSR pattern are bit-exact; fields after the fixture's SIMPLE iterations agree
-to relative L2 1e-8, residual histories to 1e-6, Krylov iteration counts within one.
+Geometry and the CSR pattern are bit-exact; fields after the fixture's SIMPLE iterations (or,
+for the transient fixtures, its time steps, with the same number of outer iterations in each)
+agree to relative L2 1e-8, residual histories to 1e-6, Krylov iteration counts within one.
 """
 import os
 
@@ -23,7 +24,7 @@ def _rel_l2(a, b):
     return np.linalg.norm(a - b) / s if s > 0 else np.linalg.norm(a - b)
 
 
-@pytest.mark.parametrize("name", ["cavity5j", "channel_tiny"])
+@pytest.mark.parametrize("name", ["cavity5j", "channel_tiny", "cavity5g_dual", "channel_tiny_tr"])
 def test_gpu_matches_golden(name):
     param = os.path.join(GOLDEN, name, "param.in")
     g = dict(np.load(os.path.join(GOLDEN, name, "golden.npz")))
@@ -35,10 +36,17 @@ def test_gpu_matches_golden(name):
     assert np.array_equal(s.get_int("A_rowptr"), g["A_rowptr"])
     assert np.array_equal(s.get_int("A_col"), g["A_col"])
     steps = int(g["steps"])
-    r = s.iterate(steps)
+    transient = "nouter" in g
+    if transient:  # physical time steps of outer iterations
+        rs = [s.time_step() for _ in range(steps)]
+        assert [x["n"] for x in rs] == list(g["nouter"])
+        r = {"ksp_its": np.concatenate([x["ksp_its"] for x in rs]), "resmax": np.concatenate([x["resmax"] for x in rs])}
+    else:
+        r = s.iterate(steps)
     assert np.all(np.abs(r["ksp_its"] - g["ksp_its"]) <= 1), (r["ksp_its"], g["ksp_its"])
     np.testing.assert_allclose(r["resmax"], g["resmax"], rtol=1e-6)
     fields = ["U", "V", "W", "P", "RUFace"] + (["TE", "ED", "VisTur"] if case.turb_model == 1 else [])
+    fields += ["T", "R"] if transient else []
     for nm in fields:
         err = _rel_l2(s.get(nm), g[nm])
         assert err < 1e-8, f"{nm}: relative L2 {err:.3e}"

@@ -389,6 +389,8 @@ int cycas_server_create(const cycas_options* opt, double hbm_budget_bytes, doubl
                         int32_t keep_fields, cycas_server** out);
 void cycas_server_destroy(cycas_server* s);
 double cycas_server_clock(void);
+/* queues a request; CYCAS_ERR_UNSUPPORTED for transient, energy or perfect-gas cases (batches
+ * hold steady, isothermal, constant-density cases) */
 int cycas_server_submit(cycas_server* s, const char* param_path, int64_t* id);
 int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued);
 /* results of requests finished since the last poll (at most max) */

@@ -237,34 +237,37 @@ __global__ void k_bc_outlet(int n_in, const int* __restrict__ in_list, int n_out
     n_out = out0[blockIdx.x + 1] - out0[blockIdx.x];
     if (n_out == 0) return;
   }
-  __shared__ double term[kThreads], aterm[kThreads];
+  // terms of both lists in shared memory, then the three serial sums on three warps at once
+  // (each sum is one dependent chain of FP64 additions; running them side by side hides two)
+  __shared__ double iterm[kThreads], oterm[kThreads], aterm[kThreads];
   __shared__ double s_min, s_mout, s_aout;
   if (threadIdx.x == 0) s_min = s_mout = s_aout = 0.0;
-  for (int pass = 0; pass < 2; pass++) {
-    int cnt = pass == 0 ? n_in : n_out;
-    const int* lst = pass == 0 ? in_list : out_list;
-    for (int base = 0; base < cnt; base += kThreads) {
-      __syncthreads();
-      int k = base + threadIdx.x;
-      if (k < cnt) {
-        int i = lst[k];
-        int iface = b_face[i];
-        const double* n = f_n + 3 * (long)iface;
-        term[threadIdx.x] = BRo[i] * (BU[i] * n[0] + BV[i] * n[1] + BW[i] * n[2]);
-        aterm[threadIdx.x] = BRo[i] * f_area[i];  // Face[i] with the boundary index, as written
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        int lim = min(kThreads, cnt - base);
-        for (int q = 0; q < lim; q++) {
-          if (pass == 0) {
-            s_min += term[q];
-          } else {
-            s_mout += term[q];
-            s_aout += aterm[q];
-          }
-        }
-      }
+  const int cmax = max(n_in, n_out);
+  for (int base = 0; base < cmax; base += kThreads) {
+    __syncthreads();
+    const int k = base + threadIdx.x;
+    if (k < n_in) {
+      const int i = in_list[k];
+      const double* n = f_n + 3 * (long)b_face[i];
+      iterm[threadIdx.x] = BRo[i] * (BU[i] * n[0] + BV[i] * n[1] + BW[i] * n[2]);
+    }
+    if (k < n_out) {
+      const int i = out_list[k];
+      const double* n = f_n + 3 * (long)b_face[i];
+      oterm[threadIdx.x] = BRo[i] * (BU[i] * n[0] + BV[i] * n[1] + BW[i] * n[2]);
+      aterm[threadIdx.x] = BRo[i] * f_area[i];  // Face[i] with the boundary index, as written
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0 && threadIdx.x < 96) {
+      const int w = threadIdx.x >> 5;
+      const int cnt = w == 0 ? n_in : n_out;
+      const int lim = min(kThreads, cnt - base);
+      const double* t = w == 0 ? iterm : (w == 1 ? oterm : aterm);
+      double acc = w == 0 ? s_min : (w == 1 ? s_mout : s_aout);
+      for (int q = 0; q < lim; q++) acc += t[q];
+      if (w == 0) s_min = acc;
+      else if (w == 1) s_mout = acc;
+      else s_aout = acc;
     }
   }
   __syncthreads();

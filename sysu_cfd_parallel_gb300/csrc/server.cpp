@@ -169,6 +169,14 @@ int cycas_server_submit(cycas_server* s, const char* param_path, int64_t* id) {
   r->param = param_path;
   int rc = cycas_case_load(param_path, &r->cs);
   if (rc != CYCAS_OK) return fail(s, rc);
+  int32_t iopt[6];
+  double dopt[3];
+  cycas_case_physics(r->cs, iopt, dopt);
+  if (!iopt[0] || iopt[3] || iopt[4]) {  // batches hold steady, isothermal, constant-density cases
+    cycas_case_free(r->cs);
+    s->err = std::string("the server runs steady, isothermal, constant-density requests: ") + param_path;
+    return CYCAS_ERR_UNSUPPORTED;
+  }
   cycas_case_dims(r->cs, r->dims);
   r->turb = (int)r->dims[4];
   r->footprint = cycas_footprint_estimate(r->cs);

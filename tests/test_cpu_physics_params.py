@@ -54,3 +54,18 @@ def test_bad_transient_lines(tmp_path, line, msg):
     with pytest.raises(capi.CycasError) as e:
         Case(p)
     assert msg in str(e.value)
+
+
+def test_server_refuses_non_steady_requests(tmp_path):
+    from sysu_cfd_parallel_gb300.solver import Server
+
+    srv = Server(hbm_budget_gb=1.0)
+    steady = meshgen.write_case(str(tmp_path / "s"), "cavity", n=3)
+    assert srv.submit(steady) >= 1
+    for name, kw in (("t", dict(time=(0.1, 1.0, 5, "Euler"))), ("e", dict(energy=True, wall_t=300)),
+                     ("g", dict(density=1, wall_t=300))):
+        p = meshgen.write_case(str(tmp_path / name), "cavity", n=3, **kw)
+        with pytest.raises(capi.CycasError) as e:
+            srv.submit(p)
+        assert e.value.code == capi.CYCAS_ERR_UNSUPPORTED and "steady" in str(e.value)
+    srv.close()

@@ -34,6 +34,17 @@ sys.path.insert(0, ROOT)
 CONFIG = {"nx": 200, "ny": 20, "nz": 20, "jitter": 0.15, "seed": 2026}
 WORKLOAD = "kepsilon channel 200x20x20x6 jittered tets (480000 cells), FP64 SIMPLE-C"
 METRIC = "cell-iters/s (steady SIMPLE-C, k-eps channel 480k tets)"
+GMRES_POLY = 2  # degree of the Jacobi-Neumann preconditioner of the GMRES systems in every GPU run
+
+
+def gmres_pc(opt):
+    """Sets the preconditioner of the GMRES systems (momentum, k, epsilon) of `opt` to the
+    Jacobi-Neumann polynomial of degree GMRES_POLY; the pressure correction keeps its own."""
+    from sysu_cfd_parallel_gb300 import capi
+    pc = capi.PC_POLY2 if GMRES_POLY == 2 else capi.PC_POLY1
+    opt.ksp[capi.SYS_VELOCITY].pc = pc
+    opt.ksp[capi.SYS_SCALAR].pc = pc
+    return opt
 
 
 def case_dir() -> str:
@@ -101,7 +112,7 @@ def measure_mixed(param, local, warmup, steps, ref_fields, fp64_ms):
     from sysu_cfd_parallel_gb300 import capi
     from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
     case = Case(param)
-    opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+    opt = gmres_pc(capi.default_options(pc=capi.PC_JACOBI, device=local))
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
     opt.mixed = 1
     s = NavierStokesSolver(case, opt)
@@ -161,7 +172,7 @@ def measure_batched(local, count, steps, mixed=False):
     import torch
     from sysu_cfd_parallel_gb300.solver import Batch, Case, NavierStokesSolver, batch_options
     params = batch_cases(count)
-    opt = batch_options(device=local)
+    opt = gmres_pc(batch_options(device=local))
     opt.mixed = 1 if mixed else 0
     cases = [Case(p) for p in params]
     cells = sum(c.ncel for c in cases)
@@ -176,7 +187,7 @@ def measure_batched(local, count, steps, mixed=False):
     ms_bg = timed_iterations(b, steps, stream)
     b.close()
     # the same batch with mixed-precision GMRES
-    opt_m = batch_options(device=local)
+    opt_m = gmres_pc(batch_options(device=local))
     opt_m.mixed = 1
     bm = Batch(cases, opt_m)
     stream_m = torch.cuda.ExternalStream(bm.stream_handle(), device=local)
@@ -261,7 +272,7 @@ def run_transient(args):
     with open(param, "w") as f:
         f.write(meshgen.channel_param(mesh, time=(0.1, 10.0, 10, "Dual"), energy=True, wall_t=290, t_in=300))
     case = Case(param)
-    opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+    opt = gmres_pc(capi.default_options(pc=capi.PC_JACOBI, device=local))
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
     s = NavierStokesSolver(case, opt)
     stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
@@ -332,7 +343,7 @@ def run_precision(args):
     fields = {}
     for mixed in (0, 1):
         case = Case(param)
-        opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+        opt = gmres_pc(capi.default_options(pc=capi.PC_JACOBI, device=local))
         opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
         for k in range(3):  # the precision workload's outer tolerance, for both runs
             opt.ksp[k].rtol = args.outer_rtol
@@ -369,7 +380,7 @@ def run_serve(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     reqs = serve_requests(args)
-    opt = batch_options(device=local)
+    opt = gmres_pc(batch_options(device=local))
     opt.mixed = 1 if args.mixed else 0
     srv = Server(hbm_budget_gb=args.budget_gb, residual_tol=args.tol, max_iters=args.max_iters, options=opt)
     t0 = Server.clock()
@@ -474,16 +485,20 @@ def vcycle_bytes(levels):
     return b + 8 * nc * nc + 16 * nc
 
 
-def krylov_bytes(its_row, turb, n, nnz, restart=30, levels=None):
+def krylov_bytes(its_row, turb, n, nnz, restart=30, levels=None, poly=0):
     """Algorithmic bytes of each Krylov launch of one iteration (solve slots in call order).
 
     CG iteration: reads A (12 nnz + 4 (n+1)), p, z, r, w, x, D^-1 (48 n); writes p, w, x, r, z
     (40 n); with the AMG preconditioner one V-cycle (vcycle_bytes) replaces D^-1.
     GMRES Arnoldi step j: SpMV + Jacobi (12 nnz + 4 (n+1) + 24 n), CGS dots (8 n (j+2)) and update
     (8 n (j+1) + 16 n); per restart cycle: initial residual (12 nnz + 4 (n+1) + 40 n) and the
-    solution update (8 n (m_used + 2)).
+    solution update (8 n (m_used + 2)).  A Jacobi-Neumann preconditioner of degree `poly` adds
+    per application `poly` stages (SpMV 12 nnz + 4 (n+1), z, own row, D^-1, write: 32 n) to every
+    Arnoldi step and restart residual, and |M^-1 b| once per solve (D^-1 b 24 n, its stages, the
+    norm 8 n).
     """
     spmv = 12 * nnz + 4 * (n + 1)
+    stage = spmv + 32 * n
     vc = vcycle_bytes(levels) if levels is not None else 0
     kinds = ["gmres", "gmres", "gmres", "cg"] + (["gmres", "gmres"] if turb else [])
     out = []
@@ -494,13 +509,13 @@ def krylov_bytes(its_row, turb, n, nnz, restart=30, levels=None):
         if kind == "cg":
             b = (spmv + 40 * n + vc) + its * (spmv + 88 * n + vc)
         else:
-            b = 0
+            b = (24 * n + poly * stage + 8 * n) if poly else 0
             left = its
             while True:
                 m = min(left, restart)
-                b += spmv + 40 * n
+                b += spmv + 40 * n + poly * stage
                 for j in range(m):
-                    b += spmv + 24 * n + 8 * n * (j + 2) + 8 * n * (j + 1) + 16 * n
+                    b += spmv + 24 * n + poly * stage + 8 * n * (j + 2) + 8 * n * (j + 1) + 16 * n
                 b += 8 * n * (m + 2)
                 left -= m
                 if left <= 0:
@@ -509,23 +524,26 @@ def krylov_bytes(its_row, turb, n, nnz, restart=30, levels=None):
     return out
 
 
-def krylov_fp64_flops(its_row, turb, n, nnz, restart=30):
+def krylov_fp64_flops(its_row, turb, n, nnz, restart=30, poly=0):
     """FP64 floating-point operations of each GMRES launch of one iteration (FP64 path): per
     Arnoldi step j the SpMV (2 nnz), the Jacobi and basis scaling (2 n), the Gram-Schmidt dots and
     update (4 n (j+1)) and the norm (2 n); per restart cycle the residual (2 nnz + 4 n) and the
-    solution update (2 n m_used).  CG slots are left out (their V-cycle is FP32)."""
+    solution update (2 n m_used).  A Jacobi-Neumann preconditioner of degree `poly` adds
+    2 nnz + 3 n per stage to every step and restart, and its application to D^-1 b once per
+    solve.  CG slots are left out (their V-cycle is FP32)."""
+    stage = 2 * nnz + 3 * n
     kinds = ["gmres", "gmres", "gmres", "cg"] + (["gmres", "gmres"] if turb else [])
     out = []
     for slot, kind in enumerate(kinds):
         its = int(its_row[slot])
         if its < 0 or kind == "cg":
             continue
-        f, left = 0, its
+        f, left = (n + poly * stage + 2 * n) if poly else 0, its
         while True:
             m = min(left, restart)
-            f += 2 * nnz + 4 * n
+            f += 2 * nnz + 4 * n + poly * stage
             for j in range(m):
-                f += 2 * nnz + 2 * n + 4 * n * (j + 1) + 2 * n
+                f += 2 * nnz + 2 * n + poly * stage + 4 * n * (j + 1) + 2 * n
             f += 2 * n * m
             left -= m
             if left <= 0:
@@ -675,7 +693,7 @@ def run_gpu(args):
     fp64_peak, fp32_peak = measure_fp_rates()
     param = make_case()
     case = Case(param)
-    opt = capi.default_options(pc=capi.PC_JACOBI, device=local)
+    opt = gmres_pc(capi.default_options(pc=capi.PC_JACOBI, device=local))
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
     s = NavierStokesSolver(case, opt)
     n, nnz, turb = case.ncel, case.nnz, case.turb_model == 1
@@ -709,7 +727,7 @@ def run_gpu(args):
     per_sys_bytes = {"cg": 0.0, "gmres_vel": 0.0, "gmres_scalar": 0.0}
     per_sys_launch = {"cg": 0, "gmres_vel": 0, "gmres_scalar": 0}
     for row in hist["ksp_its"]:
-        for kind, slot, its, b in krylov_bytes(row, turb, n, nnz, levels=levels):
+        for kind, slot, its, b in krylov_bytes(row, turb, n, nnz, levels=levels, poly=GMRES_POLY):
             key = "cg" if kind == "cg" else ("gmres_vel" if slot < 3 else "gmres_scalar")
             per_sys_bytes[key] += b
             per_sys_launch[key] += 1
@@ -718,13 +736,13 @@ def run_gpu(args):
     peak, peak_kind = measured_peak()
     launches = max(1, per_sys_launch[dom])
     achieved = (per_sys_bytes[dom] / launches) / (sys_ms[dom] / launches / 1e3) / 1e9 if sys_ms[dom] > 0 else 0.0
-    fp64 = None
-    if dom != "cg":
-        flops = sum(f for row in hist["ksp_its"] for slot, f in krylov_fp64_flops(row, turb, n, nnz)
-                    if (slot < 3) == (dom == "gmres_vel"))
-        ach = flops / (sys_ms[dom] / 1e3) / 1e12 if sys_ms[dom] > 0 else 0.0
-        fp64 = {"kernel": dom, "achieved_tflops": ach, "peak_tflops": fp64_peak, "peak_kind": "measured live",
-                "frac": ach / fp64_peak if fp64_peak > 0 else None, "fp32_peak_tflops": fp32_peak}
+    # FP64 roofline of the GMRES system with the larger share (the CG's V-cycle is FP32)
+    gdom = "gmres_vel" if sys_ms["gmres_vel"] >= sys_ms["gmres_scalar"] else "gmres_scalar"
+    flops = sum(f for row in hist["ksp_its"] for slot, f in krylov_fp64_flops(row, turb, n, nnz, poly=GMRES_POLY)
+                if (slot < 3) == (gdom == "gmres_vel"))
+    ach = flops / (sys_ms[gdom] / 1e3) / 1e12 if sys_ms[gdom] > 0 else 0.0
+    fp64 = {"kernel": gdom, "achieved_tflops": ach, "peak_tflops": fp64_peak, "peak_kind": "measured live",
+            "frac": ach / fp64_peak if fp64_peak > 0 else None, "fp32_peak_tflops": fp32_peak}
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
     if os.path.exists(tpath):
@@ -733,7 +751,8 @@ def run_gpu(args):
         try:
             t = json.load(open(tpath)).get(dom)
             if t:
-                its = [x[2] for row in hist["ksp_its"] for x in krylov_bytes(row, turb, n, nnz, levels=levels)
+                its = [x[2] for row in hist["ksp_its"]
+                       for x in krylov_bytes(row, turb, n, nnz, levels=levels, poly=GMRES_POLY)
                        if {"cg": x[0] == "cg", "gmres_vel": x[0] == "gmres" and x[1] < 3,
                            "gmres_scalar": x[0] == "gmres" and x[1] >= 3}[dom]]
                 traffic = t["bytes"] * (sum(its) / len(its)) / t["its"] if its else None
@@ -789,7 +808,8 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "cells": n, "faces": case.nfac, "nnz": nnz,
                        "parallelism": f"replicas{world}", "l2": "working set > 129 MB L2, no flush",
-                       "krylov": "GMRES(30)+Jacobi (u,v,w,k,eps), CG+AMG V-cycle (p'), reference tolerances",
+                       "krylov": "GMRES(30) with the Jacobi-Neumann polynomial preconditioner of degree %d "
+                                 "(u,v,w,k,eps), CG+AMG V-cycle (p'), reference tolerances" % GMRES_POLY,
                        "krylov_its_last_step": [int(x) for x in hist["ksp_its"][-1]],
                        "amg_levels_rows": [int(x) for x in levels[0]]},
             "e2e": {"value": e2e_value, "unit": "cell-iters/s", "h2d_bytes_per_step": int(h2d),

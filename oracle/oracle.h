@@ -66,7 +66,9 @@ struct Csr {
   void zero() { std::fill(val.begin(), val.end(), 0.0); }
 };
 
-enum PcType { PC_NONE = 0, PC_JACOBI = 1, PC_ILU0 = 2 };
+// PC_POLY1 / PC_POLY2: Jacobi-Neumann polynomials sum_{i<=d} (I - D^-1 A)^i D^-1 (the GPU
+// path's optional preconditioner for the GMRES systems)
+enum PcType { PC_NONE = 0, PC_JACOBI = 1, PC_ILU0 = 2, PC_POLY1 = 3, PC_POLY2 = 4 };
 
 enum KspType { KSP_GMRES = 0, KSP_CG = 1 };
 

@@ -37,7 +37,7 @@ struct Pc {
     type = s.pc;
     n = M.n;
     A = &M;
-    if (type == PC_JACOBI) {
+    if (type == PC_JACOBI || type == PC_POLY1 || type == PC_POLY2) {
       dinv.resize(n);
       for (int i = 0; i < n; i++) dinv[i] = 1.0 / M.val[M.diag[i]];
     } else if (type == PC_ILU0) {
@@ -94,6 +94,21 @@ struct Pc {
       std::copy(r, r + n, z);
     } else if (type == PC_JACOBI) {
       for (int i = 0; i < n; i++) z[i] = r[i] * dinv[i];
+    } else if (type == PC_POLY1 || type == PC_POLY2) {
+      // y_0 = D^-1 r, y_i = y_0 + y_{i-1} - D^-1 A y_{i-1}
+      const int deg = type == PC_POLY1 ? 1 : 2;
+      std::vector<double> z0(n), y(n), ay(n);
+      for (int i = 0; i < n; i++) z0[i] = r[i] * dinv[i];
+      y = z0;
+      for (int d = 0; d < deg; d++) {
+        for (int i = 0; i < n; i++) {
+          double s = 0.0;
+          for (int k = A->rowptr[i]; k < A->rowptr[i + 1]; k++) s += A->val[k] * y[A->col[k]];
+          ay[i] = s;
+        }
+        for (int i = 0; i < n; i++) y[i] = (z0[i] + y[i]) - dinv[i] * ay[i];
+      }
+      std::copy(y.begin(), y.end(), z);
     } else {
       std::vector<double> y(n);
       for (int i = 0; i < n; i++) {

@@ -23,7 +23,7 @@ CYCAS_ERR_TIMEOUT = 7
 CYCAS_ERR_MESH = 8
 CYCAS_ERR_UNSUPPORTED = 9
 
-PC_NONE, PC_JACOBI, PC_ILU0, PC_AMG = 0, 1, 2, 3
+PC_NONE, PC_JACOBI, PC_ILU0, PC_AMG, PC_POLY1, PC_POLY2 = 0, 1, 2, 3, 4, 5
 LOAD_MSH_BINARY = 1
 DUMP_TECPLOT, DUMP_DATA, DUMP_BACKUP = 1, 2, 4
 KSP_DEFAULT, KSP_GMRES, KSP_CG = 0, 1, 2

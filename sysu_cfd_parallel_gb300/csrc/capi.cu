@@ -436,7 +436,10 @@ void alloc_krylov(cycas_ctx& c) {
   KrylovWork& w = c.kw;
   w.m = maxm;
   w.ldv = ((long)c.m.ncel + 31) / 32 * 32;
-  w.v_len = 3L * (maxm + 1) * w.ldv;  // three momentum systems in lockstep
+  bool poly = false;
+  for (int s = 0; s < 3; s++) poly |= c.ksp[s].pc == CYCAS_PC_POLY1 || c.ksp[s].pc == CYCAS_PC_POLY2;
+  // three momentum systems in lockstep, each with two Neumann scratch vectors when needed
+  w.v_len = (3L * (maxm + 1) + (poly ? 6 : 0)) * w.ldv;
   w.V = c.alloc<double>(w.v_len);
   w.nblocks = gmres_max_blocks(c.device);
   // per CTA and per lockstep system (up to the three momentum components)
@@ -509,8 +512,12 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
   for (int i = 0; i < 3; i++) c.gravity[i] = p->gravity[i];
   for (int s = 0; s < 3; s++) {
     const cycas_ksp_options& k = o->ksp[s];
-    require(k.pc == CYCAS_PC_NONE || k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_AMG,
+    require(k.pc == CYCAS_PC_NONE || k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_AMG || k.pc == CYCAS_PC_POLY1 ||
+                k.pc == CYCAS_PC_POLY2,
             "preconditioner not available in this build");
+    require(!(k.pc == CYCAS_PC_POLY1 || k.pc == CYCAS_PC_POLY2) ||
+                (s != CYCAS_SYS_PRESSURE && k.type != CYCAS_KSP_CG),
+            "the polynomial preconditioner is for the GMRES systems (momentum, scalars)");
     require(k.restart >= 1 && k.restart <= kMaxRestart, "restart out of range");
     require(k.type >= CYCAS_KSP_DEFAULT && k.type <= CYCAS_KSP_CG, "unknown Krylov type");
     c.ksp[s].type = k.type != CYCAS_KSP_DEFAULT ? k.type : (s == CYCAS_SYS_PRESSURE ? CYCAS_KSP_CG : CYCAS_KSP_GMRES);
@@ -548,7 +555,8 @@ void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const d
   g.rowptr = c.m.rowptr;
   g.col = c.m.col;
   g.val = val;
-  g.dinv = k.pc == CYCAS_PC_JACOBI ? dinv : nullptr;
+  g.dinv = (k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_POLY1 || k.pc == CYCAS_PC_POLY2) ? dinv : nullptr;
+  g.poly = k.pc == CYCAS_PC_POLY1 ? 1 : (k.pc == CYCAS_PC_POLY2 ? 2 : 0);
   g.b = b;
   g.x = x;
   g.guess_zero = guess_zero ? 1 : 0;
@@ -617,7 +625,9 @@ void solve_velocity(cycas_ctx& c, double* const* xs_in = nullptr, const KspConf*
     g[q].rowptr = c.m.rowptr;
     g[q].col = c.m.col;
     g[q].val = c.f.Au;
-    g[q].dinv = k.pc == CYCAS_PC_JACOBI ? c.f.dinv_u : nullptr;
+    g[q].dinv = (k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_POLY1 || k.pc == CYCAS_PC_POLY2) ? c.f.dinv_u
+                                                                                                 : nullptr;
+    g[q].poly = k.pc == CYCAS_PC_POLY1 ? 1 : (k.pc == CYCAS_PC_POLY2 ? 2 : 0);
     g[q].b = bs[q];
     g[q].x = xs[q];
     g[q].guess_zero = 0;
@@ -1750,8 +1760,10 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
   return guard([&]() -> int {
     require(n > 0 && rowptr && col && val && b && x && ksp, "bad argument");
     require(ksp->restart >= 1 && ksp->restart <= kMaxRestart, "restart out of range");
-    require(ksp->pc == CYCAS_PC_NONE || ksp->pc == CYCAS_PC_JACOBI, "preconditioner not available in this build");
+    const bool poly = ksp->pc == CYCAS_PC_POLY1 || ksp->pc == CYCAS_PC_POLY2;
+    require(ksp->pc == CYCAS_PC_NONE || ksp->pc == CYCAS_PC_JACOBI || poly, "preconditioner not available in this build");
     require(ksp->type >= CYCAS_KSP_DEFAULT && ksp->type <= CYCAS_KSP_CG, "unknown Krylov type");
+    require(!(poly && ksp->type == CYCAS_KSP_CG), "the polynomial preconditioner is for GMRES");
     int nnz = rowptr[n];
     require(rowptr[0] == 0 && nnz >= 0, "bad rowptr");
     std::vector<double> dinv(n, 0.0);
@@ -1776,7 +1788,7 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
     DevStatus* st = c.alloc<DevStatus>(1);
     c.kw.m = std::max(ksp->restart, 3);
     c.kw.ldv = ((long)n + 31) / 32 * 32;
-    c.kw.v_len = (c.kw.m + 1) * c.kw.ldv;
+    c.kw.v_len = (c.kw.m + 1 + (poly ? 2 : 0)) * c.kw.ldv;
     c.kw.V = c.alloc<double>(c.kw.v_len);
     c.kw.nblocks = gmres_max_blocks(0);
     c.kw.part_len = (long)c.kw.nblocks * kGmresPartStride;
@@ -1787,7 +1799,8 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
     g.rowptr = d_rp;
     g.col = d_col;
     g.val = d_val;
-    g.dinv = ksp->pc == CYCAS_PC_JACOBI ? d_dinv : nullptr;
+    g.dinv = ksp->pc == CYCAS_PC_JACOBI || poly ? d_dinv : nullptr;
+    g.poly = ksp->pc == CYCAS_PC_POLY1 ? 1 : (ksp->pc == CYCAS_PC_POLY2 ? 2 : 0);
     g.b = d_b;
     g.x = d_x;
     g.guess_zero = guess_zero ? 1 : 0;

@@ -214,6 +214,10 @@ struct GmresCall {
   const float* val32 = nullptr;
   const float* dinv32 = nullptr;
   double inner_rtol = 0.0;
+  // Jacobi-Neumann polynomial preconditioner of this degree (1 or 2; needs dinv, and dinv32 in
+  // mixed precision, where its stages run in FP32 like the Arnoldi cycles and on the FP64
+  // residual stored in FP32); takes two more vectors per system in the Krylov workspace
+  int poly = 0;
 };
 int gmres_grid(int n, int device_blocks);
 int gmres_max_blocks(int device);

@@ -38,7 +38,8 @@ namespace {
 
 using namespace kry;
 
-enum Mode { M_START = 0, M_ARNOLDI = 1, M_RESTART = 2, M_FINAL = 3, M_DONE = 4 };
+// M_RES2: with the polynomial preconditioner, the (re)start residual's Neumann stages
+enum Mode { M_START = 0, M_ARNOLDI = 1, M_RESTART = 2, M_FINAL = 3, M_DONE = 4, M_RES2 = 5 };
 
 template <int NS, class T>
 struct GmMsArgs {
@@ -63,6 +64,11 @@ struct GmMsArgs {
   // batched solves: teams of CTAs, each solving its cases' row ranges in turn (null: one team
   // of the whole grid solving rows [0, n))
   const BatchSchedule* sched;
+  // polynomial preconditioner (degree 1 or 2; 0: the Jacobi scaling alone): two scratch vectors
+  // per system, Zs and S1, at (s * ldv)
+  int poly;
+  T* Zs;
+  T* S1;
 };
 
 // the CTAs that solve one row range together
@@ -158,8 +164,12 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
   auto part_of = [&](int blk, int s) { return T.part + ((long)blk * NS + s) * kPartStride; };
   auto Vv = [&](int s, int q) { return a.V + ((long)s * (m + 1) + q) * a.ldv; };
   const bool mixed = a.inner_rtol > 0.0;
+  const int poly = a.poly;
+  auto Zv = [&](int s) { return a.Zs + (long)s * a.ldv; };
+  auto S1v = [&](int s) { return a.S1 + (long)s * a.ldv; };
 
-  // w_s = D^-1 A v_{s,it[s]} / |v_{s,it[s]}| into v_{s,it[s]+1} for the systems in mask, over this
+  // w_s = D^-1 A v_{s,it[s]} / |v_{s,it[s]}| into v_{s,it[s]+1} (with the polynomial
+  // preconditioner: into z_s, the input of its Neumann stages) for the systems in mask, over this
   // CTA's rows taken by threads t0, t0 + stride, ...; a row's arithmetic does not depend on the
   // thread that computes it
   auto arnoldi_spmv = [&](unsigned mask, const int* it, int t0, int stride) {
@@ -176,8 +186,34 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
       const Tv d = a.dinvT ? a.dinvT[r] : Tv(1);
 #pragma unroll
       for (int s = 0; s < NS; s++)
-        if ((mask >> s) & 1u) Vv(s, it[s] + 1)[r] = (acc[s] * sj[s]) * d;
+        if ((mask >> s) & 1u) (poly ? Zv(s) : Vv(s, it[s] + 1))[r] = (acc[s] * sj[s]) * d;
     }
+  };
+  // Neumann preconditioner M^-1 = sum_{i<=poly} (I - D^-1 A)^i D^-1, applied to z_s = D^-1 y_s
+  // (already in z_s) for the systems in mask: y_0 = z, y_i = z + y_{i-1} - D^-1 A y_{i-1}, the
+  // last stage into dst[s].  Each stage follows a barrier (its input must be complete over the
+  // team's rows); false after a barrier gave up.
+  auto poly_apply = [&](unsigned mask, Tv* const* dst) -> bool {
+    for (int st = 1; st <= poly; st++) {
+      if (!grid_barrier(T.bar, nb, a.err)) return false;
+      const Tv* src[NS];
+      Tv* outp[NS];
+#pragma unroll
+      for (int s = 0; s < NS; s++) {
+        src[s] = st == 1 ? Zv(s) : S1v(s);
+        outp[s] = st == poly ? dst[s] : S1v(s);
+      }
+      for (int r = r0 + tid; r < r1; r += kGmThreads) {
+        Tv acc[NS];
+        row_gather_ms<NS, Tv>(a.rowptr, a.col, a.valT, r, src, mask, acc);
+        const Tv d = a.dinvT[r];
+#pragma unroll
+        for (int s = 0; s < NS; s++)
+          if ((mask >> s) & 1u) outp[s][r] = (__ldcg(Zv(s) + r) + __ldcg(src[s] + r)) - d * acc[s];
+      }
+    }
+    __syncthreads();
+    return true;
   };
   unsigned spec_prev = 0;  // systems whose next Arnoldi product was computed during the last control phase
 
@@ -191,6 +227,27 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
     s_rnorm[tid] = 0.0;
   }
   __syncthreads();
+  if (poly && !a.guess_zero) {  // |M^-1 b|, the reference norm of a nonzero initial guess
+    for (int r = r0 + tid; r < r1; r += kGmThreads)
+#pragma unroll
+      for (int s = 0; s < NS; s++) Zv(s)[r] = (Tv)(a.b[s][r] * a.dinv[r]);
+    Tv* dst[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++) dst[s] = Vv(s, 0);
+    if (!poly_apply((1u << NS) - 1u, dst)) return;
+    double acc[NS];
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      Tv t = Tv(0);
+      for (int r = r0 + tid; r < r1; r += kGmThreads) {
+        const Tv y = Vv(s, 0)[r];
+        t += y * y;
+      }
+      acc[s] = (double)t;
+    }
+    block_reduce<NS>(acc, s_warp, s_red);
+    if (tid < NS) part_of(T.rank, tid)[kInit + 1] = s_red[tid];
+  }
 
   while (true) {
     int mode[NS], itv[NS];
@@ -204,9 +261,10 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
     if (!any) break;
 
     // ------------------------------------------------------------ phase X
-    unsigned arn = 0;
+    unsigned arn = 0, res2 = 0;
 #pragma unroll
     for (int s = 0; s < NS; s++) {
+      if (mode[s] == M_RES2) res2 |= 1u << s;
       if (mode[s] == M_RESTART || mode[s] == M_FINAL) {
         const int cnt = s_nupd[s];
         for (int r = r0 + tid; r < r1; r += kGmThreads) {
@@ -221,6 +279,30 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
     if (arn) {
       const unsigned todo = arn & ~spec_prev;
       if (todo) arnoldi_spmv(todo, itv, tid, kGmThreads);
+    }
+    if (poly && (arn | res2)) {
+      // Neumann stages: Arnoldi products into v_{it+1}, (re)start residuals into v_0
+      Tv* dst[NS];
+#pragma unroll
+      for (int s = 0; s < NS; s++) dst[s] = ((arn >> s) & 1u) ? Vv(s, itv[s] + 1) : Vv(s, 0);
+      if (!poly_apply(arn | res2, dst)) return;
+      if (res2) {
+        double acc[NS];
+#pragma unroll
+        for (int s = 0; s < NS; s++) {
+          double t = 0.0;
+          if ((res2 >> s) & 1u)
+            for (int r = r0 + tid; r < r1; r += kGmThreads) {
+              const double y = (double)Vv(s, 0)[r];
+              t += y * y;
+            }
+          acc[s] = t;
+        }
+        block_reduce<NS>(acc, s_warp, s_red);
+        if (tid < NS && ((res2 >> tid) & 1u)) part_of(T.rank, tid)[kInit] = s_red[tid];
+      }
+    }
+    if (arn) {
       // pairs (system, basis vector) for the dot products
       if (tid == 0) {
         int p = 0;
@@ -329,7 +411,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
           const double br = a.b[s][r];
           const double t = ((gmask >> s) & 1u) ? br - ax[s] : br;
           const double z = t * d;
-          Vv(s, 0)[r] = (Tv)z;
+          (poly ? Zv(s) : Vv(s, 0))[r] = (Tv)z;  // with the polynomial: its stages come next
           acc[2 * s] += z * z;
           if (mode[s] == M_START && !a.guess_zero) {
             const double zb = br * d;
@@ -338,7 +420,8 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
         }
       }
       block_reduce<2 * NS>(acc, s_warp, s_red);
-      if (tid < 2 * NS && ((res_mask >> (tid >> 1)) & 1u)) part_of(T.rank, tid >> 1)[kInit + (tid & 1)] = s_red[tid];
+      if (!poly && tid < 2 * NS && ((res_mask >> (tid >> 1)) & 1u))
+        part_of(T.rank, tid >> 1)[kInit + (tid & 1)] = s_red[tid];
     }
     if (!grid_barrier(T.bar, nb, a.err)) return;
 
@@ -461,7 +544,9 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
             s_it[s] = 0;
           }
         }
-      } else if (md == M_START || md == M_RESTART) {
+      } else if (poly && (md == M_START || md == M_RESTART)) {
+        if (lane == 0) s_mode[s] = M_RES2;  // the residual's Neumann stages run next
+      } else if (md == M_START || md == M_RESTART || md == M_RES2) {
         double s0 = lane_sum(lane, nb, [&](int blk) { return ldcg(part_of(blk, s) + kInit); });
         double s1 = lane_sum(lane, nb, [&](int blk) { return ldcg(part_of(blk, s) + kInit + 1); });
         for (int o = 16; o > 0; o >>= 1) {
@@ -540,8 +625,10 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
   const GmresCall& c = calls[0];
   // workspace bounds: basis NS*(m+1) vectors, partials nb*NS*stride
   const int nb = sched ? grid : gmres_grid(c.n, w.nblocks);
-  if (c.restart < 1 || c.restart > kMaxRestart || (long)NS * (c.restart + 1) * w.ldv > w.v_len ||
-      (long)nb * NS * kPartStride > w.part_len || w.ldv < c.n)
+  const int extra = c.poly ? 2 * NS : 0;  // Neumann scratch vectors
+  if (c.restart < 1 || c.restart > kMaxRestart || ((long)NS * (c.restart + 1) + extra) * w.ldv > w.v_len ||
+      (long)nb * NS * kPartStride > w.part_len || w.ldv < c.n || c.poly < 0 || c.poly > 2 ||
+      (c.poly && (!c.dinv || (sizeof(Tv) != sizeof(double) && !c.dinv32))))
     return cudaErrorInvalidValue;
   a.n = c.n;
   a.m = c.restart;
@@ -570,6 +657,9 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
   a.guess_zero = c.guess_zero;
   a.V = reinterpret_cast<Tv*>(w.V);
   a.ldv = w.ldv;
+  a.poly = c.poly;
+  a.Zs = a.V + (long)NS * (c.restart + 1) * w.ldv;
+  a.S1 = a.Zs + (long)NS * w.ldv;
   a.part = w.part;
   a.bar = w.bar;
   a.err = c.err;

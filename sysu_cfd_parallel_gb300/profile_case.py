@@ -23,6 +23,8 @@ def main(argv=None):
     ap.add_argument("--iters", type=int, default=2)
     ap.add_argument("--pressure-pc", default="amg", choices=["amg", "jacobi"])
     ap.add_argument("--mixed", action="store_true", help="FP32 Arnoldi cycles in FP64 refinement")
+    ap.add_argument("--pc", default="jacobi", choices=["jacobi", "poly1", "poly2"],
+                    help="preconditioner of the GMRES systems (momentum, scalars)")
     ap.add_argument("--warmup", type=int, default=0, help="untimed iterations before the profiled ones")
     args = ap.parse_args(argv)
 
@@ -37,6 +39,9 @@ def main(argv=None):
     opt = capi.default_options(pc=capi.PC_JACOBI)
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG if args.pressure_pc == "amg" else capi.PC_JACOBI
     opt.mixed = 1 if args.mixed else 0
+    gpc = {"jacobi": capi.PC_JACOBI, "poly1": capi.PC_POLY1, "poly2": capi.PC_POLY2}[args.pc]
+    opt.ksp[capi.SYS_VELOCITY].pc = gpc
+    opt.ksp[capi.SYS_SCALAR].pc = gpc
     s = NavierStokesSolver(Case(param), opt)
     if args.warmup:
         s.iterate(args.warmup)

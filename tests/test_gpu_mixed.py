@@ -61,3 +61,23 @@ def test_mixed_batch_matches_mixed_alone(cases):
         assert np.all(rb["ksp_reason"][:, c, :4] > 0)
         for nm in ("U", "V", "W", "P"):
             assert _rel_l2(b.case_field(nm, c), s.get(nm)) < 1e-5, (names[c], nm)
+
+
+@pytest.mark.parametrize("name,steps", [("cavity8j", 8), ("channel_small", 5)])
+def test_mixed_polynomial_matches_fp64_polynomial(cases, name, steps):
+    """Mixed precision with the Jacobi-Neumann preconditioner of degree 2 (its stages in FP32)
+    against the FP64 path with the same preconditioner."""
+    p = cases(name)
+    opts = [_opts(False), _opts(True)]
+    for o in opts:
+        o.ksp[capi.SYS_VELOCITY].pc = capi.PC_POLY2
+        o.ksp[capi.SYS_SCALAR].pc = capi.PC_POLY2
+    g64 = NavierStokesSolver(Case(p), opts[0])
+    g32 = NavierStokesSolver(Case(p), opts[1])
+    r64 = g64.iterate(steps)
+    r32 = g32.iterate(steps)
+    nsolve = 6 if g32.case.turb_model == 1 else 4
+    assert np.all(r32["ksp_reason"][:, :nsolve] > 0), r32["ksp_reason"]
+    for nm in ["U", "V", "W", "P"] + (["TE", "ED"] if g32.case.turb_model == 1 else []):
+        assert _rel_l2(g32.get(nm), g64.get(nm)) < 1e-5, nm
+    np.testing.assert_allclose(r32["resmax"], r64["resmax"], rtol=1e-3)

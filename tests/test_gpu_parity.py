@@ -179,3 +179,43 @@ def test_amg_cuts_pressure_iterations(cases):
     r2 = g2.iterate(3)
     assert np.all(r2["ksp_reason"][:, 3] > 0)
     assert r2["ksp_its"][:, 3].max() * 3 < r1["ksp_its"][:, 3].min()
+
+
+@pytest.mark.parametrize("name,steps,poly", [("cavity8j", 8, 1), ("channel_small", 5, 1), ("channel_small", 4, 2)])
+def test_polynomial_preconditioner_matches_oracle(cases, name, steps, poly):
+    """GMRES with the Jacobi-Neumann polynomial preconditioner (momentum and scalars; CG with
+    Jacobi for the pressure correction), GPU against the oracle's restatement of it."""
+    p = cases(name)
+    opc = po.PC_POLY1 if poly == 1 else po.PC_POLY2
+    gpc = capi.PC_POLY1 if poly == 1 else capi.PC_POLY2
+    o = po.OracleCase(p)
+    o.set_ksp(po.VELOCITY, opc, 30)
+    o.set_ksp(po.PRESSURE, po.PC_JACOBI, 30)
+    o.set_ksp(po.SCALAR, opc, 30)
+    opts = capi.default_options(pc=capi.PC_JACOBI)
+    opts.ksp[capi.SYS_VELOCITY].pc = gpc
+    opts.ksp[capi.SYS_SCALAR].pc = gpc
+    g = NavierStokesSolver(Case(p), opts)
+    ro = o.iterate(steps)
+    rg = g.iterate(steps)
+    assert np.all(np.abs(rg["ksp_its"] - ro["ksp_its"]) <= 1), (rg["ksp_its"], ro["ksp_its"])
+    np.testing.assert_allclose(rg["resmax"], ro["resmax"], rtol=1e-6)
+    for nm in ["U", "V", "W", "P"] + (["TE", "ED"] if o.turb == 1 else []):
+        err = _rel_l2(g.get(nm), o.get(nm))
+        assert err < 1e-8, f"{nm}: relative L2 {err:.3e}"
+
+
+def test_polynomial_preconditioner_nonzero_guess_csr(cases):
+    """The standalone solve with a nonzero initial guess: |M^-1 b| is the reference norm."""
+    from sysu_cfd_parallel_gb300.solver import csr_solve
+    o, g = _pair(cases("channel_small"))
+    o.iterate(2)
+    _copy_state(o, g, True)
+    g.stage("build_velocity")
+    rp, col, val, b = g.get_int("A_rowptr"), g.get_int("A_col"), g.get("Au_val"), g.get("bu")
+    x0 = g.get("U")
+    xr, its_r, reason_r, _ = po.csr_solve(rp, col, val, b, x0=x0, pc=po.PC_POLY2, rtol=1e-8, maxit=1000,
+                                          guess_zero=False)
+    xg, its_g, reason_g, _ = csr_solve(rp, col, val, b, x0=x0, pc=capi.PC_POLY2, rtol=1e-8, guess_zero=False)
+    assert reason_r > 0 and reason_g > 0 and abs(its_g - its_r) <= 1, (its_g, its_r)
+    assert _rel_l2(xg, xr) < 1e-8

@@ -811,7 +811,8 @@ def run_gpu(args):
                        "krylov": "GMRES(30) with the Jacobi-Neumann polynomial preconditioner of degree %d "
                                  "(u,v,w,k,eps), CG+AMG V-cycle (p'), reference tolerances" % GMRES_POLY,
                        "krylov_its_last_step": [int(x) for x in hist["ksp_its"][-1]],
-                       "amg_levels_rows": [int(x) for x in levels[0]]},
+                       "amg_levels_rows": [int(x) for x in levels[0]],
+                       "amg_levels_nnz": [int(x) for x in levels[1]]},
             "e2e": {"value": e2e_value, "unit": "cell-iters/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "roofline": {"bound": "hbm", "kernel": {"cg": "k_cg_amg (pressure correction: CG + AMG V-cycle)",

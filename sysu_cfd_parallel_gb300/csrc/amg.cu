@@ -122,6 +122,7 @@ struct CgAmgArgs {
   KspOut* out;  // [ncases]
   double rtol, abstol, dtol;
   float alpha;
+  int gamma;  // cycles at the first coarse level of the shared-memory tail
   const AmgCaseDesc* cases;
   const BatchSchedule* sched;
 };
@@ -202,11 +203,97 @@ __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, c
   __syncthreads();
 }
 
-// rank 0 of a team: the V-cycle from level T.tail down, in shared memory; its input residual
+// Tail levels in shared memory, cycled by rank 0 of a team.  Per level l: R (residual in),
+// X (correction out), T (scratch); R_l is read-only while a cycle runs through level l.
+
+// pre-smoothing and restriction: X_l = w D^-1 R_l, T_l = R_l - A_l X_l, R_{l+1} = P^T T_l
+__device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned char* sb, int l) {
+  const int tid = threadIdx.x;
+  const TailLevelOff& o = T.lv[l];
+  const int n = L[l].n, nc = L[l + 1].n;
+  const int* rp = at<int>(sb, o.rowptr);
+  const int* cl = at<int>(sb, o.col);
+  const float* va = at<float>(sb, o.val);
+  const float* wd = at<float>(sb, o.wdinv);
+  const float* R = at<float>(sb, o.R);
+  float* X = at<float>(sb, o.X);
+  float* Tt = at<float>(sb, o.T);
+  for (int i = tid; i < n; i += kGmThreads) X[i] = wd[i] * R[i];
+  __syncthreads();
+  for (int i = tid; i < n; i += kGmThreads) {
+    float acc = 0.0f;
+    for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * X[cl[k]];
+    Tt[i] = R[i] - acc;
+  }
+  __syncthreads();
+  const int* pp = at<int>(sb, o.ptptr);
+  const int* pr = at<int>(sb, o.ptrow);
+  float* Rn = at<float>(sb, T.lv[l + 1].R);
+  for (int I = tid; I < nc; I += kGmThreads) {
+    float s = 0.0f;
+    for (int q = pp[I]; q < pp[I + 1]; q++) s += Tt[pr[q]];
+    Rn[I] = s;
+  }
+  __syncthreads();
+}
+
+// the coarsest level: X = (A + s 11^T)^-1 R, one warp per row
+__device__ void tail_coarsest(const AmgDevLevel* L, int nlev, const TailLayout& T, unsigned char* sb) {
+  const int tid = threadIdx.x;
+  const int n = L[nlev - 1].n;
+  const float* inv = at<float>(sb, T.inv);
+  const float* R = at<float>(sb, T.lv[nlev - 1].R);
+  float* X = at<float>(sb, T.lv[nlev - 1].X);
+  const int lane = tid & 31, wid = tid >> 5;
+  for (int i = wid; i < n; i += kGmWarps) {
+    float s = 0.0f;
+    for (int j = lane; j < n; j += 32) s += inv[i * n + j] * R[j];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) X[i] = s;
+  }
+  __syncthreads();
+}
+
+// prolongation and post-smoothing: Y = X_l + alpha P X_{l+1}, X_l = Y + w D^-1 (R_l - A_l Y)
+__device__ void tail_up(const AmgDevLevel* L, const TailLayout& T, float alpha, unsigned char* sb, int l) {
+  const int tid = threadIdx.x;
+  const TailLevelOff& o = T.lv[l];
+  const int n = L[l].n;
+  const int* rp = at<int>(sb, o.rowptr);
+  const int* cl = at<int>(sb, o.col);
+  const float* va = at<float>(sb, o.val);
+  const float* wd = at<float>(sb, o.wdinv);
+  const int* ag = at<int>(sb, o.agg);
+  const float* R = at<float>(sb, o.R);
+  float* X = at<float>(sb, o.X);
+  float* Y = at<float>(sb, o.T);
+  const float* Xc = at<float>(sb, T.lv[l + 1].X);
+  for (int i = tid; i < n; i += kGmThreads) Y[i] = X[i] + alpha * Xc[ag[i]];
+  __syncthreads();
+  for (int i = tid; i < n; i += kGmThreads) {
+    float acc = 0.0f;
+    for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * Y[cl[k]];
+    X[i] = Y[i] + wd[i] * (R[i] - acc);
+  }
+  __syncthreads();
+}
+
+// V-cycle from tail level s to the coarsest: R_s in, X_s out
+__device__ void tail_v(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, unsigned char* sb, int s) {
+  for (int l = s; l + 1 < nlev; l++) tail_down(L, T, sb, l);
+  tail_coarsest(L, nlev, T, sb);
+  for (int l = nlev - 2; l >= s; l--) tail_up(L, T, alpha, sb, l);
+}
+
+// rank 0 of a team: the cycle from level T.tail down, in shared memory.  Its input residual
 // is the tail level's r, its correction goes to the tail level's t (or, when the tail is the
-// whole hierarchy, to rows [lo, hi) of the FP64 vector z)
-__device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, unsigned char* sb,
-                           int lo, double* z) {
+// whole hierarchy, to rows [lo, hi) of the FP64 vector z).  The first coarse level of the tail
+// (g = max(tail, 1)) is solved by gamma cycles, x <- x + V(r_g - A_g x) (a W-cycle for
+// gamma 2): the tail levels are cheap, with no grid barrier, and a more accurate coarse
+// correction cuts the outer CG iterations.  `buf` holds the accumulated x and the original
+// r_g (2 n_g floats).
+__device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma,
+                           unsigned char* sb, float* buf, int lo, double* z) {
   const int tid = threadIdx.x;
   const int t0 = T.tail;
   {
@@ -215,68 +302,38 @@ __device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, 
     for (int i = tid; i < L[t0].n; i += kGmThreads) R[i] = ldcgf(rin + i);
   }
   __syncthreads();
-  for (int l = t0; l + 1 < nlev; l++) {
-    const TailLevelOff& o = T.lv[l];
-    const int n = L[l].n, nc = L[l + 1].n;
+  const int g = t0 > 1 ? t0 : 1;
+  if (gamma > 1 && g < nlev - 1 && 2 * L[g].n <= kAmgDownBuf) {
+    for (int l = t0; l < g; l++) tail_down(L, T, sb, l);
+    const TailLevelOff& o = T.lv[g];
+    const int n = L[g].n;
     const int* rp = at<int>(sb, o.rowptr);
     const int* cl = at<int>(sb, o.col);
     const float* va = at<float>(sb, o.val);
-    const float* wd = at<float>(sb, o.wdinv);
-    const float* R = at<float>(sb, o.R);
+    float* R = at<float>(sb, o.R);
     float* X = at<float>(sb, o.X);
-    float* Tt = at<float>(sb, o.T);
-    for (int i = tid; i < n; i += kGmThreads) X[i] = wd[i] * R[i];
-    __syncthreads();
-    for (int i = tid; i < n; i += kGmThreads) {
-      float acc = 0.0f;
-      for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * X[cl[k]];
-      Tt[i] = R[i] - acc;
+    float* S = buf;      // accumulated correction
+    float* Q = buf + n;  // the level's original residual
+    tail_v(L, nlev, T, alpha, sb, g);
+    for (int rep = 1; rep < gamma; rep++) {
+      for (int i = tid; i < n; i += kGmThreads) {
+        S[i] = rep == 1 ? X[i] : S[i] + X[i];
+        if (rep == 1) Q[i] = R[i];
+      }
+      __syncthreads();
+      for (int i = tid; i < n; i += kGmThreads) {
+        float acc = 0.0f;
+        for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * S[cl[k]];
+        R[i] = Q[i] - acc;
+      }
+      __syncthreads();
+      tail_v(L, nlev, T, alpha, sb, g);
     }
+    for (int i = tid; i < n; i += kGmThreads) X[i] = S[i] + X[i];
     __syncthreads();
-    const int* pp = at<int>(sb, o.ptptr);
-    const int* pr = at<int>(sb, o.ptrow);
-    float* Rn = at<float>(sb, T.lv[l + 1].R);
-    for (int I = tid; I < nc; I += kGmThreads) {
-      float s = 0.0f;
-      for (int q = pp[I]; q < pp[I + 1]; q++) s += Tt[pr[q]];
-      Rn[I] = s;
-    }
-    __syncthreads();
-  }
-  {
-    const int n = L[nlev - 1].n;
-    const float* inv = at<float>(sb, T.inv);
-    const float* R = at<float>(sb, T.lv[nlev - 1].R);
-    float* X = at<float>(sb, T.lv[nlev - 1].X);
-    const int lane = tid & 31, wid = tid >> 5;
-    for (int i = wid; i < n; i += kGmWarps) {
-      float s = 0.0f;
-      for (int j = lane; j < n; j += 32) s += inv[i * n + j] * R[j];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) X[i] = s;
-    }
-  }
-  __syncthreads();
-  for (int l = nlev - 2; l >= t0; l--) {
-    const TailLevelOff& o = T.lv[l];
-    const int n = L[l].n;
-    const int* rp = at<int>(sb, o.rowptr);
-    const int* cl = at<int>(sb, o.col);
-    const float* va = at<float>(sb, o.val);
-    const float* wd = at<float>(sb, o.wdinv);
-    const int* ag = at<int>(sb, o.agg);
-    const float* R = at<float>(sb, o.R);
-    float* X = at<float>(sb, o.X);
-    float* Y = at<float>(sb, o.T);
-    const float* Xc = at<float>(sb, T.lv[l + 1].X);
-    for (int i = tid; i < n; i += kGmThreads) Y[i] = X[i] + alpha * Xc[ag[i]];
-    __syncthreads();
-    for (int i = tid; i < n; i += kGmThreads) {
-      float acc = 0.0f;
-      for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * Y[cl[k]];
-      X[i] = Y[i] + wd[i] * (R[i] - acc);
-    }
-    __syncthreads();
+    for (int l = g - 1; l >= t0; l--) tail_up(L, T, alpha, sb, l);
+  } else {
+    tail_v(L, nlev, T, alpha, sb, t0);
   }
   {
     const float* X = at<float>(sb, T.lv[t0].X);
@@ -340,14 +397,14 @@ __device__ __forceinline__ void grid_up(const AmgDevLevel& F, const float* xc, f
 
 // z = M r for the case's rows [lo, hi) of the residual held in L[0].r; false after a barrier
 // timeout
-__device__ bool vcycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, unsigned char* sb,
+__device__ bool vcycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma, unsigned char* sb,
                        float* buf, int lo, int hi, double* z, const Team& Tm, int* err) {
   const int t0 = T.tail;
   for (int l = 0; l < t0; l++) {
     grid_down(L[l], L[l + 1], Tm, buf);
     if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   }
-  if (Tm.rank == 0) tail_cycle(L, nlev, T, alpha, sb, lo, z);
+  if (Tm.rank == 0) tail_cycle(L, nlev, T, alpha, gamma, sb, buf, lo, z);
   if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   for (int l = t0 - 1; l >= 0; l--) {
     const Rows rw = l == 0 ? share(lo, hi, Tm) : share(0, L[l].n, Tm);
@@ -407,7 +464,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
   }
   if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
   if (!a.guess_zero) {  // |M b| is the reference norm of a nonzero initial guess
-    if (!vcycle(s_lv, nlev, s_tl, alc, sb, buf, lo, hi, a.u, Tm, a.err)) return;
+    if (!vcycle(s_lv, nlev, s_tl, alc, a.gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
     double acc[1] = {0.0};
     for (int r = own.r0 + tid; r < own.r1; r += kGmThreads) {
       const double zb = ldcg(a.u + r);
@@ -418,7 +475,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
     if (tid == 0) mypart[kMaxRestart + 3] = s_red[0];
     if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
   }
-  if (!vcycle(s_lv, nlev, s_tl, alc, sb, buf, lo, hi, a.u, Tm, a.err)) return;
+  if (!vcycle(s_lv, nlev, s_tl, alc, a.gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
 
   // CG scalars are uniform over the CTA: thread 0 keeps them in shared memory
   __shared__ double s_sc[8];  // rnorm0, ttol, dp, gam_old, dpi_old, alpha, beta
@@ -530,7 +587,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
       }
     }
     if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
-    if (!vcycle(s_lv, nlev, s_tl, alc, sb, buf, lo, hi, a.u, Tm, a.err)) return;
+    if (!vcycle(s_lv, nlev, s_tl, alc, a.gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
   }
   if (Tm.rank == 0 && tid == 0) {
     a.out[c].its = s_st[1];
@@ -614,6 +671,7 @@ cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& 
   a.abstol = 1e-50;
   a.dtol = 1e4;
   a.alpha = h.alpha;
+  a.gamma = h.gamma;
   a.cases = h.d_cases;
   a.sched = sched;
   const int smem = h.smem_bytes;

@@ -74,7 +74,12 @@ struct AmgCaseDesc {
 // host-side record of the device hierarchies of all cases
 struct AmgHostView {
   int ncases = 0;
-  float omega = 2.0f / 3.0f, alpha = 2.0f;
+  // Jacobi weight of the smoother, coarse-correction scale, and cycles at the first coarse
+  // level of the shared-memory tail.  A scale above 2 puts an eigenvalue 1 - alpha below -1
+  // on the coarse space once the coarse solve is accurate (the W-cycle makes it so), and the
+  // cycle stops being a definite preconditioner; 2 is the largest safe value.
+  float omega = 0.9f, alpha = 2.0f;
+  int gamma = 2;
   std::vector<AmgCaseDesc> cases;                // host copies (level pointers are device arrays)
   std::vector<std::vector<AmgDevLevel>> levels;  // [case][level] host copies
   AmgCaseDesc* d_cases = nullptr;                // device [ncases]

@@ -91,21 +91,50 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nb, int* er
   return s_ok != 0;
 }
 
-// reduce K per-thread values over the block; result valid in s_out[0..K) after the call
+// reduce K per-thread values over the block in a fixed order; result valid in s_out[0..K)
+// after the call.
+//
+// A warp-wide FP64 addition occupies GB300's FP64 pipe for about 19 SM cycles, so the cost of
+// a block reduction is its count of warp-wide additions.  One shuffle tree per quantity spends
+// 5 per quantity in every warp; here the lane stage is a reduce-scatter butterfly: the K
+// quantities (padded to P, a power of two) are halved at each of the first log2 P xor levels
+// (a lane keeps one half and adds the partner's copy of it), so after P - 1 additions every
+// lane carries one quantity, and two plain xor levels leave 8 / P distinct partial sums of it
+// per warp -- P + 1 additions per lane in all.  The 8 partials per warp go to s_warp; warp k
+// then sums quantity k's 32 * 8 / P partials (a chain of 8 / P per lane, then a tree).
 template <int K>
-__device__ __forceinline__ void block_reduce(double (&v)[K], double* s_warp /*[kGmWarps*K]*/, double* s_out) {
+__device__ __forceinline__ void block_reduce(double (&v)[K], double* s_warp /*[kGmWarps*kDotGroup]*/,
+                                             double* s_out) {
+  static_assert(K >= 1 && K <= kDotGroup, "block_reduce: at most kDotGroup quantities");
+  constexpr int P = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : 8;
+  constexpr int G = kDotGroup / P;                   // partials per quantity per warp
+  constexpr int LOGP = P == 1 ? 0 : P == 2 ? 1 : P == 4 ? 2 : 3;
+  constexpr int MP = 16 >> LOGP;                     // first plain xor level
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double a[P];
 #pragma unroll
-  for (int k = 0; k < K; k++) {
-    double t = v[k];
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-    if (lane == 0) s_warp[wid * K + k] = t;
+  for (int k = 0; k < P; k++) a[k] = k < K ? v[k] : 0.0;
+  int q = 0;  // quantity held in a[0] once the scatter levels are done
+#pragma unroll
+  for (int h = P / 2, m = 16; h >= 1; h >>= 1, m >>= 1) {
+    const bool up = (lane & m) != 0;
+#pragma unroll
+    for (int j = 0; j < h; j++) {
+      const double send = up ? a[j] : a[j + h];
+      const double keep = up ? a[j + h] : a[j];
+      a[j] = keep + __shfl_xor_sync(0xffffffffu, send, m);
+    }
+    if (up) q += h;
   }
+  a[0] += __shfl_xor_sync(0xffffffffu, a[0], MP);
+  a[0] += __shfl_xor_sync(0xffffffffu, a[0], MP >> 1);
+  if ((lane & (MP | (MP >> 1))) == 0 && q < K) s_warp[wid * kDotGroup + q * G + (lane & (G - 1))] = a[0];
   __syncthreads();
-  // warp k sums the per-warp values of quantity k as a shuffle tree (a serial chain of 32 FP64
-  // additions in one thread would cost 32 FP64 latencies)
   if (wid < K) {
-    double t = s_warp[lane * K + wid];
+    const double* src = s_warp + lane * kDotGroup + wid * G;  // lane l takes warp l's partials
+    double t = src[0];
+#pragma unroll
+    for (int g = 1; g < G; g++) t += src[g];
     for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
     if (lane == 0) s_out[wid] = t;
   }

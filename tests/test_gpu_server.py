@@ -3,9 +3,13 @@
 Requests join and leave the running batches while others iterate (the batch is re-formed and
 the state of continuing cases moved on the device), laminar cavities and k-epsilon channels
 run in separate batches, and the HBM budget holds requests back in arrival order.  Each
-finished request must match the same case run alone for the same number of iterations, to the
-tolerance of two runs whose Krylov inner products sum in different orders (relative L2 1e-5 at
-the reference's tolerances).
+finished request must match the same case run alone for the same number of iterations.  A
+request's Krylov solves run on a team of CTAs whose inner products sum in another order than a
+solve alone; with every solve converged tightly (rtol 1e-12) the two runs agree like two runs of
+the same algorithm (relative L2 1e-8).  At the reference's tolerances the k-epsilon channels'
+solves can stop one iteration apart and the fields then differ by the solver tolerance times the
+conditioning of the SIMPLE iteration (up to ~1e-4 on the small channel after 25 iterations), so
+the comparison is made with tight solves.
 """
 import numpy as np
 import pytest
@@ -21,13 +25,20 @@ def _rel_l2(a, b):
     return np.linalg.norm(a - b) / s if s > 0 else np.linalg.norm(a - b)
 
 
+def _tight():
+    o = batch_options()
+    for k in range(3):
+        o.ksp[k].rtol = 1e-12
+    return o
+
+
 def test_server_continuous_batching_matches_alone(cases):
     names = ["cavity8", "channel_tiny", "cavity8j", "cavity4", "channel_small", "cavity12"]
     params = {n: cases(n) for n in names}
     # a budget for the two largest requests: the others wait in arrival order
     fp = sorted(Case(p).footprint() for p in params.values())
     budget_gb = (fp[-1] + fp[-2]) / 1e9
-    srv = Server(hbm_budget_gb=budget_gb, residual_tol=1e-4, max_iters=25, keep_fields=True)
+    srv = Server(hbm_budget_gb=budget_gb, residual_tol=1e-4, max_iters=25, keep_fields=True, options=_tight())
     ids = {}
     ids[names[0]] = srv.submit(params[names[0]])
     ids[names[1]] = srv.submit(params[names[1]])
@@ -46,11 +57,11 @@ def test_server_continuous_batching_matches_alone(cases):
         r = srv.results[ids[n]]
         assert r["status"] in (capi.REQ_CONVERGED, capi.REQ_MAX_ITERS), (n, r)
         assert r["t_arrival"] <= r["t_admit"] <= r["t_done"]
-        s = NavierStokesSolver(Case(params[n]), batch_options())
+        s = NavierStokesSolver(Case(params[n]), _tight())
         s.iterate(r["iterations"])
         fields = ["U", "V", "W", "P"] + (["TE", "ED"] if s.case.turb_model == 1 else [])
         for nm in fields:
             got = srv.result_field(ids[n], nm, s.case.ncel)
             err = _rel_l2(got, s.get(nm))
-            assert err < 1e-5, f"{n} {nm}: relative L2 {err:.3e}"
+            assert err < 1e-8, f"{n} {nm}: relative L2 {err:.3e}"
     srv.close()

@@ -206,7 +206,31 @@ __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, c
 // Tail levels in shared memory, cycled by rank 0 of a team.  Per level l: R (residual in),
 // X (correction out), T (scratch); R_l is read-only while a cycle runs through level l.
 
-// pre-smoothing and restriction: X_l = w D^-1 R_l, T_l = R_l - A_l X_l, R_{l+1} = P^T T_l
+// sum over the shared-memory CSR row i of va[k] * f(cl[k]) in column order; the loads of up to
+// eight entries are issued together, so a row costs a few shared-memory round trips rather
+// than two per entry
+template <class F>
+__device__ __forceinline__ float smem_row(const int* rp, const int* cl, const float* va, int i, F f) {
+  const int k0 = rp[i], k1 = rp[i + 1];
+  float s = 0.0f;
+  for (int b = k0; b < k1; b += 8) {
+    int c[8];
+    float v[8], x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      c[q] = b + q < k1 ? cl[b + q] : 0;
+      v[q] = b + q < k1 ? va[b + q] : 0.0f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = b + q < k1 ? f(c[q]) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 8; q++) s += v[q] * x[q];
+  }
+  return s;
+}
+
+// pre-smoothing and restriction: X_l = w D^-1 R_l, T_l = R_l - A_l X_l, R_{l+1} = P^T T_l.  The
+// residual takes w D^-1 R of the neighbours directly, so X needs no pass (and sync) of its own.
 __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned char* sb, int l) {
   const int tid = threadIdx.x;
   const TailLevelOff& o = T.lv[l];
@@ -218,20 +242,25 @@ __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned ch
   const float* R = at<float>(sb, o.R);
   float* X = at<float>(sb, o.X);
   float* Tt = at<float>(sb, o.T);
-  for (int i = tid; i < n; i += kGmThreads) X[i] = wd[i] * R[i];
-  __syncthreads();
   for (int i = tid; i < n; i += kGmThreads) {
-    float acc = 0.0f;
-    for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * X[cl[k]];
-    Tt[i] = R[i] - acc;
+    const float ri = R[i];
+    X[i] = wd[i] * ri;
+    Tt[i] = ri - smem_row(rp, cl, va, i, [&](int j) { return wd[j] * R[j]; });
   }
   __syncthreads();
   const int* pp = at<int>(sb, o.ptptr);
   const int* pr = at<int>(sb, o.ptrow);
   float* Rn = at<float>(sb, T.lv[l + 1].R);
   for (int I = tid; I < nc; I += kGmThreads) {
+    const int q0 = pp[I], q1 = pp[I + 1];
     float s = 0.0f;
-    for (int q = pp[I]; q < pp[I + 1]; q++) s += Tt[pr[q]];
+    for (int q = q0; q < q1; q += 8) {
+      float t[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) t[u] = q + u < q1 ? Tt[pr[q + u]] : 0.0f;
+#pragma unroll
+      for (int u = 0; u < 8; u++) s += t[u];
+    }
     Rn[I] = s;
   }
   __syncthreads();
@@ -271,8 +300,7 @@ __device__ void tail_up(const AmgDevLevel* L, const TailLayout& T, float alpha, 
   for (int i = tid; i < n; i += kGmThreads) Y[i] = X[i] + alpha * Xc[ag[i]];
   __syncthreads();
   for (int i = tid; i < n; i += kGmThreads) {
-    float acc = 0.0f;
-    for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * Y[cl[k]];
+    const float acc = smem_row(rp, cl, va, i, [&](int j) { return Y[j]; });
     X[i] = Y[i] + wd[i] * (R[i] - acc);
   }
   __syncthreads();
@@ -292,7 +320,7 @@ __device__ void tail_v(const AmgDevLevel* L, int nlev, const TailLayout& T, floa
 // gamma 2): the tail levels are cheap, with no grid barrier, and a more accurate coarse
 // correction cuts the outer CG iterations.  `buf` holds the accumulated x and the original
 // r_g (2 n_g floats).
-__device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma,
+__device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma,
                            unsigned char* sb, float* buf, int lo, double* z) {
   const int tid = threadIdx.x;
   const int t0 = T.tail;
@@ -321,11 +349,7 @@ __device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, 
         if (rep == 1) Q[i] = R[i];
       }
       __syncthreads();
-      for (int i = tid; i < n; i += kGmThreads) {
-        float acc = 0.0f;
-        for (int k = rp[i]; k < rp[i + 1]; k++) acc += va[k] * S[cl[k]];
-        R[i] = Q[i] - acc;
-      }
+      for (int i = tid; i < n; i += kGmThreads) R[i] = Q[i] - smem_row(rp, cl, va, i, [&](int j) { return S[j]; });
       __syncthreads();
       tail_v(L, nlev, T, alpha, sb, g);
     }

@@ -410,7 +410,7 @@ def run_serve(args):
         "p99_s": float(np.percentile(lat, 99)), "requests": len(reqs), "finished": len(res),
         "converged": len(conv), "server_steps": steps, "wall_s": wall,
         "cell_iters_per_s": cell_iters / wall, "n_gpus": 1, "dtype": "f64" if not args.mixed else "mixed",
-        "data": "synthetic",
+        "data": "synthetic", "loop": srv.stats(),
         "config": {"workload": f"Poisson {args.rate}/s for {args.duration}s; cavities n={args.cavity_n}, "
                                f"channels m={args.channel_m}; tol {args.tol}; cap {args.max_iters} iterations; "
                                f"budget {args.budget_gb} GB; drain {args.drain}s",

@@ -183,7 +183,15 @@ typedef struct {
                                relative drop of inner_rtol, convergence tested on the FP64 true
                                residual to the system's rtol (no counterpart in the reference) */
   double inner_rtol;        /* <= 0: 1e-4 */
-  int32_t reserved[4];
+  /* pressure AMG cycle (CYCAS_PC_AMG; no counterpart in the reference, whose pressure PC is
+   * PETSc's ILU(0)); 0 selects the default */
+  float amg_omega;          /* Jacobi weight of the smoother, in (0, 1]; default 0.9 */
+  float amg_alpha;          /* coarse-correction scale, in (0, 2]; default 2 (above 2 the cycle
+                               can stop being a definite preconditioner) */
+  int32_t amg_gamma;        /* cycles at the first level held in shared memory, 1..4 (1: a
+                               V-cycle throughout, 2: a W-cycle at that level); default 2 for
+                               cases of at least 80000 pressure rows, 1 below */
+  int32_t reserved;
 } cycas_options;
 
 /* fills defaults: the reference's Krylov methods (GMRES(30); CG for pressure), Jacobi,
@@ -404,6 +412,10 @@ int cycas_server_poll(cycas_server* s, cycas_request_result* out, int32_t max, i
 /* final U V W P TE ED of a finished request (server created with keep_fields) */
 int cycas_server_result_field(cycas_server* s, int64_t id, const char* name, double* dst, int64_t n);
 const char* cycas_server_last_error(cycas_server* s);
+/* where the loop's host time went: out[0] steps, out[1] batch rebuilds (membership changes),
+ * out[2] seconds in rebuilds (union mesh, device setup, AMG hierarchies, state copies),
+ * out[3] seconds in batch iterations */
+int cycas_server_stats(cycas_server* s, double* out);
 
 /* No counterpart in the reference: the GMRES solve of cycas_csr_solve for callers that cannot
  * allocate device memory (their HBM is pre-reserved by another allocator, or they must not add

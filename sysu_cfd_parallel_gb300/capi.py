@@ -56,7 +56,7 @@ class KspOptions(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("ksp", KspOptions * 3), ("device", C.c_int32), ("mixed", C.c_int32), ("inner_rtol", C.c_double),
-                ("reserved", C.c_int32 * 4)]
+                ("amg_omega", C.c_float), ("amg_alpha", C.c_float), ("amg_gamma", C.c_int32), ("reserved", C.c_int32)]
 
 
 class RequestResult(C.Structure):
@@ -96,7 +96,7 @@ EXPORTS = (
     "cycas_batch_size", "cycas_batch_offsets", "cycas_batch_iteration", "cycas_batch_residuals",
     "cycas_batch_copy_case", "cycas_batch_case_field", "cycas_server_create", "cycas_server_destroy",
     "cycas_server_clock", "cycas_server_submit", "cycas_server_step", "cycas_server_poll",
-    "cycas_server_result_field", "cycas_server_last_error", "cycas_footprint_estimate",
+    "cycas_server_result_field", "cycas_server_last_error", "cycas_server_stats", "cycas_footprint_estimate",
     "cycas_measure_fp_rates", "cycas_set_graph", "cycas_batch_autotune",
 )
 
@@ -190,6 +190,7 @@ def load(build_if_missing: bool = True):
     L.cycas_footprint_estimate.restype = C.c_double
     L.cycas_server_last_error.argtypes = [_P]
     L.cycas_server_last_error.restype = C.c_char_p
+    L.cycas_server_stats.argtypes = [_P, _P]
     L.cycas_csr_solve_noalloc.argtypes = [C.c_int32, _P, _P, _P, _P, _P, C.POINTER(KspOptions), C.c_double,
                                           C.c_int32, C.c_int32, _P, C.POINTER(SolveStats)]
     _lib = L

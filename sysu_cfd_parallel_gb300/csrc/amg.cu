@@ -122,7 +122,6 @@ struct CgAmgArgs {
   KspOut* out;  // [ncases]
   double rtol, abstol, dtol;
   float alpha;
-  int gamma;  // cycles at the first coarse level of the shared-memory tail
   const AmgCaseDesc* cases;
   const BatchSchedule* sched;
 };
@@ -448,18 +447,19 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
   __shared__ double s_g[5];
   __shared__ AmgDevLevel s_lv[kAmgMaxLevels];
   __shared__ TailLayout s_tl;
-  __shared__ int s_case[3];  // lo, hi, nlev
+  __shared__ int s_case[4];  // lo, hi, nlev, gamma
   const int tid = threadIdx.x;
   const AmgCaseDesc* cd = a.cases + c;
   if (tid == 0) {
     s_case[0] = cd->lo;
     s_case[1] = cd->hi;
     s_case[2] = cd->nlev;
+    s_case[3] = cd->gamma;
   }
   for (int k = tid; k < (int)(sizeof(TailLayout) / sizeof(int)); k += kGmThreads)
     reinterpret_cast<int*>(&s_tl)[k] = reinterpret_cast<const int*>(&cd->tl)[k];
   __syncthreads();
-  const int lo = s_case[0], hi = s_case[1], nlev = s_case[2];
+  const int lo = s_case[0], hi = s_case[1], nlev = s_case[2], gamma = s_case[3];
   for (int l = tid; l < nlev; l += kGmThreads) s_lv[l] = cd->levels[l];
   __syncthreads();
   unsigned char* sb = s_dyn;
@@ -488,7 +488,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
   }
   if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
   if (!a.guess_zero) {  // |M b| is the reference norm of a nonzero initial guess
-    if (!vcycle(s_lv, nlev, s_tl, alc, a.gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
+    if (!vcycle(s_lv, nlev, s_tl, alc, gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
     double acc[1] = {0.0};
     for (int r = own.r0 + tid; r < own.r1; r += kGmThreads) {
       const double zb = ldcg(a.u + r);
@@ -499,7 +499,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
     if (tid == 0) mypart[kMaxRestart + 3] = s_red[0];
     if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
   }
-  if (!vcycle(s_lv, nlev, s_tl, alc, a.gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
+  if (!vcycle(s_lv, nlev, s_tl, alc, gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
 
   // CG scalars are uniform over the CTA: thread 0 keeps them in shared memory
   __shared__ double s_sc[8];  // rnorm0, ttol, dp, gam_old, dpi_old, alpha, beta
@@ -611,7 +611,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
       }
     }
     if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
-    if (!vcycle(s_lv, nlev, s_tl, alc, a.gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
+    if (!vcycle(s_lv, nlev, s_tl, alc, gamma, sb, buf, lo, hi, a.u, Tm, a.err)) return;
   }
   if (Tm.rank == 0 && tid == 0) {
     a.out[c].its = s_st[1];
@@ -695,7 +695,6 @@ cudaError_t launch_cg_amg(const GmresCall& c, const AmgHostView& h, KrylovWork& 
   a.abstol = 1e-50;
   a.dtol = 1e4;
   a.alpha = h.alpha;
-  a.gamma = h.gamma;
   a.cases = h.d_cases;
   a.sched = sched;
   const int smem = h.smem_bytes;

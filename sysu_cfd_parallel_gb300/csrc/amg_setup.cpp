@@ -192,33 +192,49 @@ TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz) {
 
 void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, const double* weight,
                      const int* rowptr_dev, const int* col_dev, const int* diag_dev, const double* val64_dev,
-                     const std::vector<int>& lo, const std::vector<int>& hi, AmgUploader& up) {
+                     const std::vector<int>& lo, const std::vector<int>& hi, AmgUploader& up,
+                     std::vector<std::shared_ptr<const AmgHostHierarchy>>* cache) {
   const int nc = (int)lo.size();
-  std::vector<AmgHostHierarchy> H(nc);
+  if (cache && (int)cache->size() != nc) throw std::runtime_error("AMG: cache size differs from the case count");
+  std::vector<std::shared_ptr<const AmgHostHierarchy>> Hp(nc);
+  std::vector<int> case_nnz0(nc + 1, 0);  // first level-0 entry of every case (cases are contiguous)
   int D = 0;
   for (int c = 0; c < nc; c++) {
-    const int l0 = lo[c], nr = hi[c] - lo[c], k0 = rowptr[l0];
+    const int l0 = lo[c], nr = hi[c] - lo[c];
     if (nr < 1 || hi[c] > n) throw std::runtime_error("AMG: empty or out-of-range case");
-    std::vector<int> rp(nr + 1), cl(rowptr[hi[c]] - k0);
-    std::vector<double> w(cl.size());
-    for (int i = 0; i <= nr; i++) rp[i] = rowptr[l0 + i] - k0;
-    for (size_t k = 0; k < cl.size(); k++) {
-      const int j = col[k0 + k];
-      if (j < l0 || j >= hi[c]) throw std::runtime_error("AMG: the pressure system couples two cases");
-      cl[k] = j - l0;
-      w[k] = weight[k0 + k];
+    if (cache && (*cache)[c]) {
+      Hp[c] = (*cache)[c];
+      if (Hp[c]->lv.empty() || Hp[c]->lv[0].n != nr) throw std::runtime_error("AMG: cached hierarchy of another case");
+    } else {
+      if (!rowptr || !col || !weight) throw std::runtime_error("AMG: pattern needed to build a hierarchy");
+      const int k0 = rowptr[l0];
+      std::vector<int> rp(nr + 1), cl(rowptr[hi[c]] - k0);
+      std::vector<double> w(cl.size());
+      for (int i = 0; i <= nr; i++) rp[i] = rowptr[l0 + i] - k0;
+      for (size_t k = 0; k < cl.size(); k++) {
+        const int j = col[k0 + k];
+        if (j < l0 || j >= hi[c]) throw std::runtime_error("AMG: the pressure system couples two cases");
+        cl[k] = j - l0;
+        w[k] = weight[k0 + k];
+      }
+      auto h = std::make_shared<AmgHostHierarchy>(
+          amg_build(nr, rp.data(), cl.data(), w.data(), 4, kAmgCoarseMax, kAmgMaxLevels));
+      if (h->lv.back().n > kAmgCoarseMax)
+        throw std::runtime_error("aggregation did not reach a small enough coarsest level");
+      Hp[c] = h;
+      if (cache) (*cache)[c] = h;
     }
-    H[c] = amg_build(nr, rp.data(), cl.data(), w.data(), 4, kAmgCoarseMax, kAmgMaxLevels);
-    if (H[c].lv.back().n > kAmgCoarseMax)
-      throw std::runtime_error("aggregation did not reach a small enough coarsest level");
-    D = std::max(D, (int)H[c].lv.size());
+    case_nnz0[c + 1] = case_nnz0[c] + Hp[c]->lv[0].nnz;
+    if (rowptr && rowptr[l0] != case_nnz0[c]) throw std::runtime_error("AMG: cases are not contiguous in the pattern");
+    D = std::max(D, (int)Hp[c]->lv.size());
   }
+  auto H = [&](int c) -> const AmgHostHierarchy& { return *Hp[c]; };
   v.ncases = nc;
   v.val64 = val64_dev;
   v.dep.assign(D, AmgHostView::Depth{});
   v.levels.assign(nc, std::vector<AmgDevLevel>());
   v.cases.assign(nc, AmgCaseDesc{});
-  for (int c = 0; c < nc; c++) v.levels[c].assign(H[c].lv.size(), AmgDevLevel{});
+  for (int c = 0; c < nc; c++) v.levels[c].assign(H(c).lv.size(), AmgDevLevel{});
 
   // offsets of every case's slice per depth (cases without the level get none)
   std::vector<std::vector<int>> row_off(D, std::vector<int>(nc, -1)), nnz_off(D, std::vector<int>(nc, -1)),
@@ -227,17 +243,17 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
   std::vector<int> nrows(D, 0), nnzs(D, 0), nrp(D, 0), npt(D, 0), nptr(D, 0), ncp(D, 0);
   for (int l = 0; l < D; l++)
     for (int c = 0; c < nc; c++) {
-      if ((int)H[c].lv.size() <= l) continue;
-      const AmgHostLevel& L = H[c].lv[l];
+      if ((int)H(c).lv.size() <= l) continue;
+      const AmgHostLevel& L = H(c).lv[l];
       row_off[l][c] = l == 0 ? lo[c] : nrows[l];
-      nnz_off[l][c] = l == 0 ? rowptr[lo[c]] : nnzs[l];
+      nnz_off[l][c] = l == 0 ? case_nnz0[c] : nnzs[l];
       rp_off[l][c] = nrp[l];
       if (l > 0) {
         nrows[l] += L.n;
         nnzs[l] += L.nnz;
         nrp[l] += L.n + 1;
       }
-      if (l + 1 < (int)H[c].lv.size()) {
+      if (l + 1 < (int)H(c).lv.size()) {
         pt_off[l][c] = npt[l];
         npt[l] += (int)L.ptptr.size();
         ptr_off[l][c] = nptr[l];
@@ -247,7 +263,7 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
       }
     }
   nrows[0] = n;
-  nnzs[0] = rowptr[n];
+  nnzs[0] = case_nnz0[nc];
 
   // host arrays per depth
   for (int l = 0; l < D; l++) {
@@ -259,14 +275,14 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
     }
     ag.assign(l == 0 ? n : nrows[l], -1);
     for (int c = 0; c < nc; c++) {
-      if ((int)H[c].lv.size() <= l) continue;
-      const AmgHostLevel& L = H[c].lv[l];
+      if ((int)H(c).lv.size() <= l) continue;
+      const AmgHostLevel& L = H(c).lv[l];
       if (l > 0) {
         rp.insert(rp.end(), L.rowptr.begin(), L.rowptr.end());
         cl.insert(cl.end(), L.col.begin(), L.col.end());
         for (int i = 0; i < L.n; i++) dg.push_back(L.diag[i] + nnz_off[l][c]);
       }
-      if (l + 1 < (int)H[c].lv.size()) {
+      if (l + 1 < (int)H(c).lv.size()) {
         for (int i = 0; i < L.n; i++) ag[row_off[l][c] + i] = L.agg[i];
         pp.insert(pp.end(), L.ptptr.begin(), L.ptptr.end());
         for (int i = 0; i < L.n; i++) pr.push_back(L.ptrow[i] + (l == 0 ? lo[c] : 0));
@@ -276,8 +292,8 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
     if (l + 1 < D) {
       cptr.push_back(0);
       for (int c = 0; c < nc; c++) {
-        if ((int)H[c].lv.size() <= l + 1) continue;
-        const AmgHostLevel& L = H[c].lv[l];
+        if ((int)H(c).lv.size() <= l + 1) continue;
+        const AmgHostLevel& L = H(c).lv[l];
         const int base = cptr.back();
         for (size_t q = 1; q < L.cptr.size(); q++) cptr.push_back(base + L.cptr[q]);
         for (int k : L.csrc) csrc.push_back(k + nnz_off[l][c]);
@@ -302,8 +318,8 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
       d.nnz_next = (int)cptr.size() - 1;
     }
     for (int c = 0; c < nc; c++) {
-      if ((int)H[c].lv.size() <= l) continue;
-      const AmgHostLevel& L = H[c].lv[l];
+      if ((int)H(c).lv.size() <= l) continue;
+      const AmgHostLevel& L = H(c).lv[l];
       AmgDevLevel& e = v.levels[c][l];
       e.n = L.n;
       e.nnz = L.nnz;
@@ -340,24 +356,25 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
   std::vector<long> inv_off(nc);
   for (int c = 0; c < nc; c++) {
     inv_off[c] = ninv;
-    const int m = H[c].lv.back().n;
+    const int m = H(c).lv.back().n;
     ninv += (long)m * m;
   }
   v.coarse_inv = up.alloc_float(std::max(1L, ninv));
   int tail_max = 0;
   for (int c = 0; c < nc; c++) {
     std::vector<int> ln, lz;
-    for (const AmgHostLevel& L : H[c].lv) {
+    for (const AmgHostLevel& L : H(c).lv) {
       ln.push_back(L.n);
       lz.push_back(L.nnz);
     }
     AmgCaseDesc& cd = v.cases[c];
     cd.lo = lo[c];
     cd.hi = hi[c];
-    cd.nlev = (int)H[c].lv.size();
+    cd.nlev = (int)H(c).lv.size();
     cd.coarse_inv = v.coarse_inv + inv_off[c];
     cd.levels = (const AmgDevLevel*)up.upload_bytes(v.levels[c].data(), sizeof(AmgDevLevel) * cd.nlev);
     cd.tl = tail_layout(ln, lz);
+    cd.gamma = v.gamma > 0 ? v.gamma : (hi[c] - lo[c] >= kAmgWRows ? 2 : 1);
     tail_max = std::max(tail_max, cd.tl.bytes);
     if (c == 0) {
       v.rows0 = ln;

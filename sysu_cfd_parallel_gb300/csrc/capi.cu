@@ -10,6 +10,7 @@
 #include <cstring>
 #include <exception>
 #include <map>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -21,6 +22,10 @@
 
 struct cycas_case {
   cycas::HostCase hc;
+  // the case's pressure AMG hierarchy, built the first time a batch holds the case and reused
+  // by every later batch (it depends on the case's own mesh only); serving rebuilds a batch at
+  // every membership change
+  mutable std::shared_ptr<const cycas::AmgHostHierarchy> amg;
 };
 
 namespace cycas {
@@ -200,6 +205,11 @@ const int kRefMaxit[3] = {1000, 1000, 500};
 void require(bool ok, const std::string& msg) {
   if (!ok) throw StatusError(CYCAS_ERR_INVALID, msg);
 }
+// the same for a literal message: nothing is built unless the check fails (the mesh checks run
+// per face and per vertex, where a std::string per call cost more than the checks)
+void require(bool ok, const char* msg) {
+  if (!ok) throw StatusError(CYCAS_ERR_INVALID, msg);
+}
 
 // Host-side derived structure: gradient face order, CSR pattern and slots, boundary lists.
 void build_device_mesh(cycas_ctx& c, const cycas_mesh_view& v) {
@@ -216,8 +226,8 @@ void build_device_mesh(cycas_ctx& c, const cycas_mesh_view& v) {
   // validate topology (bounds) before anything reaches the device
   for (int i = 0; i < nf; i++) {
     int a = v.face_cell1[i], b = v.face_cell2[i];
-    require(a >= 0 && a < n, "face_cell1 out of range at face " + std::to_string(i));
-    require(b < n && (b >= 0 || b == -10), "face_cell2 must be a cell or -10 at face " + std::to_string(i));
+    if (!(a >= 0 && a < n)) require(false, "face_cell1 out of range at face " + std::to_string(i));
+    if (!(b < n && (b >= 0 || b == -10))) require(false, "face_cell2 must be a cell or -10 at face " + std::to_string(i));
     if (b < 0) require(v.face_bnd[i] >= 0 && v.face_bnd[i] < nb, "boundary face without boundary index");
   }
   for (int i = 0; i < nb; i++) {
@@ -457,7 +467,22 @@ void alloc_krylov(cycas_ctx& c) {
 
 // Aggregation hierarchy of the pressure system.  Strength of a connection = the face
 // coefficient area/|d.n| (Face.rlencos) of the face joining the two cells.
-void setup_amg(cycas_ctx& c) {
+void setup_amg(cycas_ctx& c, std::vector<std::shared_ptr<const AmgHostHierarchy>>* cache = nullptr) {
+  struct Up : AmgUploader {
+    cycas_ctx& c;
+    explicit Up(cycas_ctx& cc) : c(cc) {}
+    const int* upload_int(const int* h, long n) override { return c.upload(h, n); }
+    float* alloc_float(long n) override { return c.alloc<float>(n); }
+    void* upload_bytes(const void* h, long bytes) override { return c.upload((const unsigned char*)h, bytes); }
+  } up(c);
+  if (cache && std::all_of(cache->begin(), cache->end(), [](const auto& h) { return h != nullptr; })) {
+    // every hierarchy known: no host copy of the pattern is needed
+    amg_setup_cases(c.amg, c.m.ncel, nullptr, nullptr, nullptr, c.m.rowptr, c.m.col, c.m.c_diag, c.f.Ap,
+                    c.case_lo, c.case_hi, up, cache);
+    c.amg_sizes = c.amg.rows0;
+    c.amg_nnz = c.amg.nnz0;
+    return;
+  }
   const int n = c.m.ncel, nf = c.m.nfac, nnz = c.m.nnz;
   std::vector<double> rl(nf);
   std::vector<int> rowptr(n + 1), col(nnz), slot(6L * n), faces(6L * n), nface(n);
@@ -474,15 +499,8 @@ void setup_amg(cycas_ctx& c) {
       int s = slot[(size_t)j * n + i];
       if (s >= 0) w[s] = rl[faces[(size_t)j * n + i]];
     }
-  struct Up : AmgUploader {
-    cycas_ctx& c;
-    explicit Up(cycas_ctx& cc) : c(cc) {}
-    const int* upload_int(const int* h, long n) override { return c.upload(h, n); }
-    float* alloc_float(long n) override { return c.alloc<float>(n); }
-    void* upload_bytes(const void* h, long bytes) override { return c.upload((const unsigned char*)h, bytes); }
-  } up(c);
   amg_setup_cases(c.amg, n, rowptr.data(), col.data(), w.data(), c.m.rowptr, c.m.col, c.m.c_diag, c.f.Ap,
-                  c.case_lo, c.case_hi, up);
+                  c.case_lo, c.case_hi, up, cache);
   c.amg_sizes = c.amg.rows0;
   c.amg_nnz = c.amg.nnz0;
 }
@@ -530,6 +548,11 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
   }
   c.mixed = o->mixed != 0;
   c.inner_rtol = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
+  require(o->amg_omega <= 1.0f && o->amg_alpha <= 2.0f && o->amg_gamma >= 0 && o->amg_gamma <= 4,
+          "AMG options out of range (omega <= 1, alpha <= 2, gamma 0..4)");
+  if (o->amg_omega > 0.0f) c.amg.omega = o->amg_omega;
+  if (o->amg_alpha > 0.0f) c.amg.alpha = o->amg_alpha;
+  if (o->amg_gamma > 0) c.amg.gamma = o->amg_gamma;
   c.d_geom_err = c.alloc<int>(1);
   c.st = c.alloc<DevStatus>(1);
   CK(cudaMallocHost((void**)&c.st_host, sizeof(DevStatus)));
@@ -1864,7 +1887,10 @@ int cycas_batch_create(const cycas_case* const* cases, int32_t ncases, const cyc
       alloc_fields(*c);
       alloc_krylov(*c);
       setup_batch(*c, u, hs);
-      setup_amg(*c);
+      std::vector<std::shared_ptr<const AmgHostHierarchy>> cache(ncases);
+      for (int k = 0; k < ncases; k++) cache[k] = cases[k]->amg;
+      setup_amg(*c, &cache);
+      for (int k = 0; k < ncases; k++) cases[k]->amg = cache[k];
       const HostCase& h = u.h;
       const long n = h.ncel, nb = h.nbnd;
       set_field(*c, "U", h.U.data(), n);

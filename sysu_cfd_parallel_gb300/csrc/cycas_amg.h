@@ -9,6 +9,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <vector>
 
 namespace cycas {
@@ -17,6 +18,11 @@ constexpr int kAmgMaxLevels = 12;
 constexpr int kAmgCoarseMax = 64;            // the coarsest level is inverted densely by one CTA
 constexpr int kAmgDownBuf = 8192;            // floats of the per-CTA restriction buffer
 constexpr int kAmgTailBudget = 160 * 1024;   // shared-memory bytes for a case's tail levels
+// Cases with at least this many pressure rows solve the tail's first level by two cycles (a
+// W-cycle there).  The second cycle runs on one CTA, a fixed cost per CG iteration that the
+// saved iterations repay only on large cases: measured on GB300 per 10 SIMPLE iterations,
+// 480k-tet channel -7.5 %, 104k -4 %, 60k +8 %, 4k-cell cavity +5 %.
+constexpr int kAmgWRows = 80000;
 
 struct AmgHostLevel {
   int n = 0, nnz = 0;
@@ -69,17 +75,19 @@ struct AmgCaseDesc {
   const float* coarse_inv;    // dense inverse of the (regularised) coarsest level, row-major
   const AmgDevLevel* levels;  // device array [nlev]
   TailLayout tl;
+  int gamma;                  // cycles at the first level of the shared-memory tail
 };
 
 // host-side record of the device hierarchies of all cases
 struct AmgHostView {
   int ncases = 0;
   // Jacobi weight of the smoother, coarse-correction scale, and cycles at the first coarse
-  // level of the shared-memory tail.  A scale above 2 puts an eigenvalue 1 - alpha below -1
-  // on the coarse space once the coarse solve is accurate (the W-cycle makes it so), and the
-  // cycle stops being a definite preconditioner; 2 is the largest safe value.
+  // level of the shared-memory tail (0: by case size, kAmgWRows).  A scale above 2 puts an
+  // eigenvalue 1 - alpha below -1 on the coarse space once the coarse solve is accurate (the
+  // W-cycle makes it so), and the cycle stops being a definite preconditioner; 2 is the
+  // largest safe value.
   float omega = 0.9f, alpha = 2.0f;
-  int gamma = 2;
+  int gamma = 0;
   std::vector<AmgCaseDesc> cases;                // host copies (level pointers are device arrays)
   std::vector<std::vector<AmgDevLevel>> levels;  // [case][level] host copies
   AmgCaseDesc* d_cases = nullptr;                // device [ncases]
@@ -111,9 +119,12 @@ struct AmgUploader {
 // Builds and uploads the hierarchies of the cases [lo[c], hi[c]) of one pattern: rowptr/col
 // (host, all rows, global columns) with strength weights per entry; the *_dev pointers are the
 // same pattern on the device, diag_dev its diagonal positions and val64_dev the FP64 values.
+// cache (optional, one entry per case): a non-null entry is that case's hierarchy, used as it
+// is; null entries are built and stored.  With every entry given, rowptr/col/weight may be null.
 void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, const double* weight,
                      const int* rowptr_dev, const int* col_dev, const int* diag_dev, const double* val64_dev,
-                     const std::vector<int>& lo, const std::vector<int>& hi, AmgUploader& up);
+                     const std::vector<int>& lo, const std::vector<int>& hi, AmgUploader& up,
+                     std::vector<std::shared_ptr<const AmgHostHierarchy>>* cache = nullptr);
 
 struct GmresCall;
 struct KrylovWork;

@@ -77,6 +77,9 @@ struct cycas_server {
   std::vector<std::unique_ptr<Request>> finished;
   double in_use = 0.0;
   std::string err;
+  // host wall time of the loop's parts (cycas_server_stats)
+  double t_rebuild = 0.0, t_iterate = 0.0, t_admin = 0.0;
+  int64_t n_rebuild = 0, n_steps = 0;
 };
 
 namespace {
@@ -188,6 +191,7 @@ int cycas_server_submit(cycas_server* s, const char* param_path, int64_t* id) {
 
 int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
   if (!s) return CYCAS_ERR_INVALID;
+  s->n_steps++;
   // 1. admission, first come first served within the budget (a request larger than the whole
   // budget runs alone once nothing else is active)
   auto idle = [&]() {
@@ -208,14 +212,19 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
   for (auto& kv : s->classes) {
     auto& K = kv.second;
     if (K.dirty) {
+      const double t0 = now_s();
       int rc = rebuild(s, K);
+      s->t_rebuild += now_s() - t0;
+      s->n_rebuild++;
       if (rc != CYCAS_OK) return rc;
     }
     if (K.members.empty()) continue;
     const int nc = (int)K.members.size();
     std::vector<double> resmax(nc);
     std::vector<int32_t> its(8L * nc), reasons(8L * nc);
+    const double t0 = now_s();
     int rc = cycas_batch_iteration(K.ctx, resmax.data(), its.data(), reasons.data());
+    s->t_iterate += now_s() - t0;
     // per-case outcomes are judged below; only errors of the batch itself stop the server
     if (rc != CYCAS_OK && rc != CYCAS_NOT_CONVERGED && rc != CYCAS_NAN_DETECTED) return fail(s, rc);
     std::vector<int> retire;
@@ -304,5 +313,14 @@ int cycas_server_result_field(cycas_server* s, int64_t id, const char* name, dou
 }
 
 const char* cycas_server_last_error(cycas_server* s) { return s ? s->err.c_str() : ""; }
+
+int cycas_server_stats(cycas_server* s, double* out) {
+  if (!s || !out) return CYCAS_ERR_INVALID;
+  out[0] = (double)s->n_steps;
+  out[1] = (double)s->n_rebuild;
+  out[2] = s->t_rebuild;
+  out[3] = s->t_iterate;
+  return CYCAS_OK;
+}
 
 }  // extern "C"

@@ -26,6 +26,9 @@ def main(argv=None):
     ap.add_argument("--pc", default="jacobi", choices=["jacobi", "poly1", "poly2"],
                     help="preconditioner of the GMRES systems (momentum, scalars)")
     ap.add_argument("--warmup", type=int, default=0, help="untimed iterations before the profiled ones")
+    ap.add_argument("--amg-omega", type=float, default=0.0, help="AMG smoother weight (0: library default)")
+    ap.add_argument("--amg-gamma", type=int, default=0, help="AMG cycles at the first shared-memory level")
+    ap.add_argument("--jitter", type=float, default=0.0, help="interior node jitter (fraction of h)")
     args = ap.parse_args(argv)
 
     from . import capi, meshgen
@@ -33,12 +36,17 @@ def main(argv=None):
 
     d = tempfile.mkdtemp(prefix="cycas_prof_")
     if args.kind == "channel":
-        param = meshgen.write_case(d, "channel", nx=args.nx, ny=args.ny, nz=args.nz, steps=args.iters)
+        kw = {"jitter": args.jitter, "seed": 2026} if args.jitter > 0 else {}
+        param = meshgen.write_case(d, "channel", nx=args.nx, ny=args.ny, nz=args.nz, steps=args.iters + args.warmup,
+                                   **kw)
     else:
-        param = meshgen.write_case(d, "cavity", n=args.n, steps=args.iters)
+        kw = {"jitter": args.jitter, "seed": 1000} if args.jitter > 0 else {}
+        param = meshgen.write_case(d, "cavity", n=args.n, steps=args.iters + args.warmup, **kw)
     opt = capi.default_options(pc=capi.PC_JACOBI)
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG if args.pressure_pc == "amg" else capi.PC_JACOBI
     opt.mixed = 1 if args.mixed else 0
+    opt.amg_omega = args.amg_omega
+    opt.amg_gamma = args.amg_gamma
     gpc = {"jacobi": capi.PC_JACOBI, "poly1": capi.PC_POLY1, "poly2": capi.PC_POLY2}[args.pc]
     opt.ksp[capi.SYS_VELOCITY].pc = gpc
     opt.ksp[capi.SYS_SCALAR].pc = gpc

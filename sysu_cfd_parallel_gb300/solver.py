@@ -557,6 +557,13 @@ class Server:
         capi.check(capi.load().cycas_server_result_field(self._h, rid, name.encode(), capi.ptr(out), n))
         return out
 
+    def stats(self) -> dict:
+        """Host time of the loop's parts: steps, batch rebuilds and the seconds spent in them and
+        in batch iterations."""
+        out = np.zeros(4)
+        capi.check(capi.load().cycas_server_stats(self._h, capi.ptr(out)))
+        return {"steps": int(out[0]), "rebuilds": int(out[1]), "rebuild_s": float(out[2]), "iterate_s": float(out[3])}
+
     def close(self):
         if getattr(self, "_h", None):
             capi.load().cycas_server_destroy(self._h)

@@ -78,3 +78,25 @@ def test_batch_rejects_mixed_physics(cases):
     from sysu_cfd_parallel_gb300 import capi
     with pytest.raises(capi.CycasError):
         Batch([Case(cases("cavity4")), Case(cases("channel_tiny"))])
+
+
+def test_batch_rebuild_reuses_hierarchies_bit_identically(cases):
+    """A case keeps its pressure AMG hierarchy across batches (the server rebuilds a batch at
+    every membership change); a batch built from cached hierarchies runs bit-identically to one
+    built from fresh cases."""
+    names = ["cavity8", "cavity8j", "cavity12"]
+    params = [cases(n) for n in names]
+    cs = [Case(p) for p in params]
+    b1 = Batch(cs, _opts(1e-10))
+    r1 = b1.iterate(3)
+    b2 = Batch(cs, _opts(1e-10))  # every hierarchy from the cache
+    r2 = b2.iterate(3)
+    b3 = Batch([Case(params[0]), cs[1], Case(params[2])], _opts(1e-10))  # fresh and cached
+    r3 = b3.iterate(3)
+    for r in (r2, r3):
+        assert np.array_equal(r1["ksp_its"], r["ksp_its"])
+    for c in range(3):
+        for nm in ("U", "V", "W", "P"):
+            a = b1.case_field(nm, c).view(np.int64)
+            assert np.array_equal(a, b2.case_field(nm, c).view(np.int64)), (names[c], nm)
+            assert np.array_equal(a, b3.case_field(nm, c).view(np.int64)), (names[c], nm)

@@ -171,6 +171,51 @@ def test_amg_pressure_matches_reference_ilu(cases, name, steps):
         assert err < 1e-8, f"{nm}: relative L2 {err:.3e}"
 
 
+@pytest.mark.parametrize("name,steps,gamma,omega", [("cavity8", 4, 2, 0.0), ("channel_small", 3, 3, 0.0),
+                                                   ("cavity8j", 3, 1, 2.0 / 3.0)])
+def test_amg_cycle_options_match_reference_ilu(cases, name, steps, gamma, omega):
+    """The cycle's options (several cycles at the first shared-memory level -- which these
+    small cases only take when asked --, another smoother weight) change the Krylov path, not
+    the solution: tight solves agree with the reference's ILU(0)-CG."""
+    p = cases(name)
+    o = po.OracleCase(p)
+    o.set_ksp(po.VELOCITY, po.PC_JACOBI, rtol=1e-12)
+    o.set_ksp(po.SCALAR, po.PC_JACOBI, rtol=1e-12)
+    o.set_ksp(po.PRESSURE, po.PC_ILU0, rtol=1e-12, ksp_type=po.KSP_CG)
+    opt = _opts(capi.PC_AMG, rtol_p=1e-12, rtol_v=1e-12)
+    opt.amg_gamma = gamma
+    opt.amg_omega = omega
+    g = NavierStokesSolver(Case(p), opt)
+    o.iterate(steps)
+    rg = g.iterate(steps)
+    assert np.all(rg["ksp_reason"][:, :4] > 0)
+    fields = ["U", "V", "W", "P"] + (["TE", "ED"] if o.turb == 1 else [])
+    for nm in fields:
+        err = _rel_l2(g.get(nm), o.get(nm))
+        assert err < 1e-8, f"{nm}: relative L2 {err:.3e}"
+
+
+def test_amg_w_cycle_cuts_iterations(cases):
+    p = cases("channel_small")
+    its = {}
+    for gamma in (1, 2):
+        opt = _opts(capi.PC_AMG)
+        opt.amg_gamma = gamma
+        r = NavierStokesSolver(Case(p), opt).iterate(3)
+        assert np.all(r["ksp_reason"][:, 3] > 0)
+        its[gamma] = int(r["ksp_its"][:, 3].sum())
+    assert its[2] < its[1], its
+
+
+def test_amg_options_out_of_range_rejected(cases):
+    p = cases("cavity4")
+    for field, value in (("amg_alpha", 2.5), ("amg_omega", 1.2), ("amg_gamma", 5)):
+        opt = _opts(capi.PC_AMG)
+        setattr(opt, field, value)
+        with pytest.raises(capi.CycasError):
+            NavierStokesSolver(Case(p), opt)
+
+
 def test_amg_cuts_pressure_iterations(cases):
     p = cases("channel_small")
     g1 = NavierStokesSolver(Case(p), _opts(capi.PC_JACOBI))

@@ -248,6 +248,17 @@ int cycas_simple_iteration(cycas_ctx* ctx, double residual[10], double* resmax, 
 
 /* Runs n iterations back to back on the device and reads the residual history once at the
  * end (no host synchronisation between iterations). res_hist: [n*10], resmax: [n], its: [n*8]. */
+/* one SIMPLE-C iteration with the caller's host fields as its state: the nin input fields are
+ * uploaded before the stage that first reads them, the nout output fields downloaded once they
+ * are final, and both kinds of copies overlap the iteration where its stages allow (inputs of
+ * the k-epsilon stage upload during momentum and pressure; velocity, pressure and face-flux
+ * outputs download during k-epsilon).  Returns when every output is in host memory.  Results
+ * are those of cycas_set_fields + cycas_simple_iteration + cycas_get_fields; pinned host
+ * arrays make the copies asynchronous.  Single-case contexts only. */
+int cycas_simple_iteration_io(cycas_ctx* c, int32_t nin, const char* const* in_names, const double* const* in_src,
+                              const int64_t* in_n, int32_t nout, const char* const* out_names,
+                              double* const* out_dst, const int64_t* out_n, double residual[10], double* resmax,
+                              cycas_iter_stats* stats);
 int cycas_simple_iterations(cycas_ctx* ctx, int32_t n, double* res_hist, double* resmax, int32_t* its,
                             int32_t* reasons);
 

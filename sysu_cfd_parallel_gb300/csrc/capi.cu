@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <exception>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -89,6 +90,14 @@ struct DumpState {
   std::thread worker;
   int rc = 0;
   std::string err;
+};
+
+// Host field transfers of cycas_simple_iteration_io that overlap the iteration: a copy
+// stream and the events that order it against the compute stream.
+struct IoState {
+  cudaStream_t copy = nullptr;
+  cudaEvent_t ev_late_in = nullptr;   // the late inputs have landed
+  cudaEvent_t ev_early_out = nullptr; // the early outputs are final
 };
 
 }  // namespace cycas
@@ -177,7 +186,12 @@ struct cycas_ctx {
     return p;
   }
   DumpState dump;
+  IoState io;
   ~cycas_ctx() {
+    if (io.copy) cudaStreamSynchronize(io.copy);
+    if (io.ev_late_in) cudaEventDestroy(io.ev_late_in);
+    if (io.ev_early_out) cudaEventDestroy(io.ev_early_out);
+    if (io.copy) cudaStreamDestroy(io.copy);
     if (dump.worker.joinable()) dump.worker.join();
     if (dump.side) cudaStreamSynchronize(dump.side);
     if (dump.ev_snap) cudaEventDestroy(dump.ev_snap);
@@ -814,9 +828,12 @@ void begin_iteration(cycas_ctx& c) {
   if (c.profiling) CK(cudaEventRecord(c.ev_iter[0], c.stream));
 }
 
-void issue_iteration(cycas_ctx& c) {
+// after_pressure (optional) runs on the host once the pressure correction is queued, before
+// the k-epsilon and energy stages
+void issue_iteration(cycas_ctx& c, const std::function<void()>& after_pressure = nullptr) {
   calculate_velocity(c);
   calculate_pressure(c);
+  if (after_pressure) after_pressure();
   if (c.turb == 1) update_keps(c);
   if (c.energy) update_energy(c);
 }
@@ -1537,6 +1554,85 @@ int cycas_simple_iteration(cycas_ctx* c, double residual[10], double* resmax, cy
     require(c != nullptr, "null context");
     run_iteration(*c);
     return finish_iteration(*c, residual, resmax, stats);
+  });
+}
+
+namespace {
+// Inputs first read by the k-epsilon stage, and outputs final once the pressure correction is
+// done (the k-epsilon and energy stages only read them).  Checked against the kernels' argument
+// lists: momentum, Rhie-Chow, pressure and corrections take no k-epsilon field, and the
+// k-epsilon kernels write only TE, ED, their boundary values, sources and VisTur.
+bool late_input(const cycas_ctx& c, const char* nm) {
+  if (c.turb != 1) return false;
+  return !std::strcmp(nm, "TE") || !std::strcmp(nm, "ED") || !std::strcmp(nm, "BTE") || !std::strcmp(nm, "BED");
+}
+bool early_output(const cycas_ctx& c, const char* nm) {
+  if (c.turb != 1) return false;  // nothing runs after the pressure correction to overlap
+  static const char* names[] = {"U", "V", "W", "P", "RUFace", "BU", "BV", "BW", "BRo", "deltaP"};
+  for (const char* e : names)
+    if (!std::strcmp(nm, e)) return true;
+  return false;
+}
+}  // namespace
+
+int cycas_simple_iteration_io(cycas_ctx* c, int32_t nin, const char* const* in_names, const double* const* in_src,
+                              const int64_t* in_n, int32_t nout, const char* const* out_names,
+                              double* const* out_dst, const int64_t* out_n, double residual[10], double* resmax,
+                              cycas_iter_stats* stats) {
+  return guard([&]() -> int {
+    require(c != nullptr && nin >= 0 && nout >= 0, "bad argument");
+    require(nin == 0 || (in_names && in_src && in_n), "null input arrays");
+    require(nout == 0 || (out_names && out_dst && out_n), "null output arrays");
+    require(!c->is_batch, "cycas_simple_iteration_io takes a single-case context");
+    for (int i = 0; i < nin; i++) {
+      require(in_names[i] && in_src[i], "null input field");
+      require(lookup(*c, in_names[i]).second == in_n[i], std::string("size mismatch for ") + in_names[i]);
+    }
+    for (int i = 0; i < nout; i++) {
+      require(out_names[i] && out_dst[i], "null output field");
+      require(lookup(*c, out_names[i]).second == out_n[i], std::string("size mismatch for ") + out_names[i]);
+    }
+    cycas_ctx& x = *c;
+    if (!x.io.copy) {
+      CK(cudaStreamCreateWithFlags(&x.io.copy, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&x.io.ev_late_in, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&x.io.ev_early_out, cudaEventDisableTiming));
+    }
+    const bool overlap = !x.use_graph;  // a captured iteration has no stage boundary to hook
+    auto h2d = [&](int i, cudaStream_t s) {
+      CK(cudaMemcpyAsync(lookup(x, in_names[i]).first, in_src[i], sizeof(double) * in_n[i], cudaMemcpyHostToDevice, s));
+    };
+    auto d2h = [&](int i, cudaStream_t s) {
+      CK(cudaMemcpyAsync(out_dst[i], lookup(x, out_names[i]).first, sizeof(double) * out_n[i], cudaMemcpyDeviceToHost,
+                         s));
+    };
+    bool any_late = false, any_early = false;
+    for (int i = 0; i < nin; i++) {
+      const bool late = overlap && late_input(x, in_names[i]);
+      any_late = any_late || late;
+      h2d(i, late ? x.io.copy : x.stream);
+    }
+    if (any_late) CK(cudaEventRecord(x.io.ev_late_in, x.io.copy));
+    if (!overlap) {
+      run_iteration(x);
+    } else {
+      for (int i = 0; i < nout; i++) any_early = any_early || early_output(x, out_names[i]);
+      begin_iteration(x);
+      issue_iteration(x, [&]() {
+        if (any_early) {
+          CK(cudaEventRecord(x.io.ev_early_out, x.stream));
+          CK(cudaStreamWaitEvent(x.io.copy, x.io.ev_early_out, 0));
+          for (int i = 0; i < nout; i++)
+            if (early_output(x, out_names[i])) d2h(i, x.io.copy);
+        }
+        if (any_late) CK(cudaStreamWaitEvent(x.stream, x.io.ev_late_in, 0));
+      });
+    }
+    for (int i = 0; i < nout; i++)
+      if (!(overlap && any_early && early_output(x, out_names[i]))) d2h(i, x.stream);
+    const int rc = finish_iteration(x, residual, resmax, stats);
+    CK(cudaStreamSynchronize(x.io.copy));
+    return rc;
   });
 }
 

@@ -146,7 +146,8 @@ class NavierStokesSolver:
         a = np.ascontiguousarray(values, dtype=np.float64)
         capi.check(capi.load().cycas_set_field(self._h, name.encode(), capi.ptr(a), a.size))
 
-    def _many(self, fn, arrays: dict, host_to_device: bool):
+    @staticmethod
+    def _pack(arrays: dict, host_to_device: bool):
         names = list(arrays)
         k = len(names)
         nm = (C.c_char_p * k)(*[x.encode() for x in names])
@@ -158,7 +159,10 @@ class NavierStokesSolver:
                 raise TypeError(f"{x}: contiguous float64 array required")
             ptrs[q] = a.ctypes.data
             sizes[q] = a.size
-        capi.check(fn(self._h, k, nm, ptrs, sizes))
+        return k, nm, ptrs, sizes
+
+    def _many(self, fn, arrays: dict, host_to_device: bool):
+        capi.check(fn(self._h, *self._pack(arrays, host_to_device)))
 
     def set_fields(self, arrays: dict) -> None:
         """Uploads several named arrays with one synchronisation (cycas_set_fields)."""
@@ -198,6 +202,23 @@ class NavierStokesSolver:
         rm = C.c_double()
         st = capi.IterStats()
         rc = capi.load().cycas_simple_iteration(self._h, res, C.byref(rm), C.byref(st))
+        self.last_stats = st
+        self._raise_for(rc, st)
+        self.step += 1
+        self.Residual = np.array(list(res))
+        return rm.value
+
+    def simple_iteration_io(self, inputs: dict, outputs: dict):
+        """One iteration whose state comes from and goes to host arrays (cycas_simple_iteration_io):
+        the uploads of `inputs` and downloads into `outputs` overlap the iteration where its
+        stages allow; the same results as set_fields + simple_iteration + get_fields."""
+        res = (C.c_double * 10)()
+        rm = C.c_double()
+        st = capi.IterStats()
+        ni, inm, ip, isz = self._pack(inputs, True)
+        no, onm, op, osz = self._pack(outputs, False)
+        rc = capi.load().cycas_simple_iteration_io(self._h, ni, inm, ip, isz, no, onm, op, osz, res, C.byref(rm),
+                                                   C.byref(st))
         self.last_stats = st
         self._raise_for(rc, st)
         self.step += 1

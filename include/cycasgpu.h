@@ -264,7 +264,8 @@ int cycas_simple_iterations(cycas_ctx* ctx, int32_t n, double* res_hist, double*
 
 /* Individual stages for parity tests: bc_velocity bc_pressure bc_deltap grad_uvwp grad_deltap
  * build_velocity ruface2 build_pressure correct_cells correct_ruface calculate_velocity
- * calculate_pressure keps clear_residual. */
+ * calculate_pressure keps build_te (the k rows of keps) build_ed (the epsilon rows, on the
+ * current k) energy build_energy save_transient clear_residual. */
 int cycas_run_stage(cycas_ctx* ctx, const char* stage);
 
 /* DataPartition::solveVelocity_GMRES / solvePressureCorrection / solveScarlar_GMRES

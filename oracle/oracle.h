@@ -127,6 +127,7 @@ struct Case {
 
   // k-epsilon work arrays kept for inspection (navier_scalar.cpp:21-27)
   std::vector<double> Prod, TESource, EDSource, ApTE, ApED;
+  std::vector<double> VisTE, VisED;  // effective diffusivities of the k and epsilon rows
   // energy work arrays kept for inspection (navier_scalar.cpp:209-217)
   std::vector<double> kcond, ESource, ApE;
   int reverseInletWarnings = 0;
@@ -168,6 +169,11 @@ void correct_cells(Case& cs);
 int calculate_velocity(Case& cs);
 int calculate_pressure(Case& cs);
 void update_tur_kepsilon(Case& cs);
+// the two assembly halves of update_tur_kepsilon: the k rows (sources, wall functions, boundary
+// values, unsteady terms) and, on the solved k, the epsilon rows (k clipped, epsilon sources,
+// wall-cell rows) -- each ends with the system in As / bs
+void keps_build_te(Case& cs);
+void keps_build_ed(Case& cs);
 void build_scalar_matrix(Case& cs, int iSca, double* Phi, double* BPhi, double* DiffCoef, double* source, double* App);
 
 // linear algebra

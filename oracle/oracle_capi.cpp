@@ -62,6 +62,8 @@ std::vector<double>* field(Case& cs, const std::string& nm) {
   if (nm == "EDSource") return &cs.EDSource;
   if (nm == "ApTE") return &cs.ApTE;
   if (nm == "ApED") return &cs.ApED;
+  if (nm == "VisTE") return &cs.VisTE;
+  if (nm == "VisED") return &cs.VisED;
   if (nm == "vert") return &cs.Vert;
   if (nm == "BTem") return &cs.BTem;
   if (nm == "kcond") return &cs.kcond;
@@ -267,6 +269,8 @@ int orc_stage(void* hp, const char* name) {
     else if (s == "calculate_velocity") calculate_velocity(cs);
     else if (s == "calculate_pressure") calculate_pressure(cs);
     else if (s == "keps") update_tur_kepsilon(cs);
+    else if (s == "build_te") keps_build_te(cs);
+    else if (s == "build_ed") keps_build_ed(cs);
     else if (s == "build_energy") build_energy(cs);
     else if (s == "energy") update_energy(cs);
     else if (s == "save_transient") save_transient_old_data(cs);

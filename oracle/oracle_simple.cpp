@@ -617,15 +617,39 @@ void build_scalar_matrix(Case& cs, int iSca, double* Phi, double* BPhi, double* 
 }
 
 // UpdateTurKEpsilon (navier_scalar.cpp:11-197) with SetBCKEpsilon (navier_bc.cpp:220-345)
-void update_tur_kepsilon(Case& cs) {
-  const double kappa = 0.419, Cmu = 0.09, Ceps1 = 1.44, Ceps2 = 1.92, Sigma_k = 1.0, Sigma_e = 1.3;
+namespace {
+const double kKappa = 0.419, kCmuKE = 0.09, kCeps1 = 1.44, kCeps2 = 1.92, kSigmaK = 1.0, kSigmaE = 1.3;
+
+// TE^1.5 of the wall function (navier_bc.cpp:279, std::pow there), rounded once to nearest.
+// The C library's pow is within about 0.52 ulp and misrounds a small share of arguments (0.07 %
+// over 1e-9..1e2 with glibc), differently from one library to the next; this restatement takes
+// the mathematical value instead, which the GPU computes the same way: x*sqrt(x) with the
+// correctly rounded root s, its exact remainder x - s*s, the Newton correction
+// (x - s*s) / (2s), and the exact error of x*s (Dekker's two-product by FMA).
+double pow15(double x) {
+  if (x == 0.0) return 0.0;
+  const double s = std::sqrt(x);
+  const double r = std::fma(-s, s, x);
+  const double d = r / (2.0 * s);
+  const double p = x * s;
+  const double e = std::fma(x, s, -p);
+  return p + (e + x * d);
+}
+}
+
+// UpdateTurKEpsilon (navier_scalar.cpp:11-197): k rows
+void keps_build_te(Case& cs) {
+  const double kappa = kKappa, Cmu = kCmuKE, Sigma_k = kSigmaK, Sigma_e = kSigmaE;
   int n = cs.Ncel;
   cs.Prod.assign(n, 0.0);
   cs.TESource.assign(n, 0.0);
   cs.EDSource.assign(n, 0.0);
   cs.ApTE.assign(n, 0.0);
   cs.ApED.assign(n, 0.0);
-  std::vector<double> VisTE(n), VisED(n);
+  cs.VisTE.assign(n, 0.0);
+  cs.VisED.assign(n, 0.0);
+  std::vector<double>& VisTE = cs.VisTE;
+  std::vector<double>& VisED = cs.VisED;
   double *Prod = cs.Prod.data(), *TES = cs.TESource.data(), *EDS = cs.EDSource.data();
   double *ApTE = cs.ApTE.data(), *ApED = cs.ApED.data();
   for (int i = 0; i < n; i++) {
@@ -663,7 +687,7 @@ void update_tur_kepsilon(Case& cs) {
     if (yplus < 11.) utau = std::sqrt(tauw / cs.Rn[ic]);
     else utau = Cmu25 * std::sqrt(cs.TE[ic]);
     Prod[ic] = tauw * utau / (kappa * dist);
-    double eps = std::pow(Cmu, 0.75) * std::pow(cs.TE[ic], 1.5) / (kappa * dist);
+    double eps = std::pow(Cmu, 0.75) * pow15(cs.TE[ic]) / (kappa * dist);
     TES[ic] = Prod[ic] * vol;
     ApTE[ic] -= cs.Rn[ic] * cs.ED[ic] / cs.TE[ic] * vol;
     ApTE[ic] += cs.Rn[ic] * eps / cs.TE[ic] * vol;
@@ -695,7 +719,13 @@ void update_tur_kepsilon(Case& cs) {
     }
   }
   build_scalar_matrix(cs, 2, cs.TE.data(), cs.BTE.data(), VisTE.data(), TES, ApTE);
-  solve_or_throw(cs, cs.As, 2, 1.e-8, 500, false, cs.bs.data(), cs.TE.data(), "Tn");
+}
+
+// epsilon rows on the solved k
+void keps_build_ed(Case& cs) {
+  const double Ceps1 = kCeps1, Ceps2 = kCeps2;
+  int n = cs.Ncel;
+  double *Prod = cs.Prod.data(), *EDS = cs.EDSource.data(), *ApED = cs.ApED.data();
   cs.As.zero();
   for (int i = 0; i < n; i++)
     if (cs.TE[i] < 1.e-9) cs.TE[i] = 1.e-9;
@@ -704,7 +734,7 @@ void update_tur_kepsilon(Case& cs) {
     EDS[i] = Ceps1 * fact * Prod[i];
     ApED[i] += Ceps2 * fact * cs.Rn[i];
   }
-  build_scalar_matrix(cs, 3, cs.ED.data(), cs.BED.data(), VisED.data(), EDS, ApED);
+  build_scalar_matrix(cs, 3, cs.ED.data(), cs.BED.data(), cs.VisED.data(), EDS, ApED);
   for (int i = 0; i < cs.Nbnd; i++) {
     if (type1Of(cs, cs.B[i].rid) != 1) continue;
     int ic = cs.F[cs.B[i].face].cell1;
@@ -718,6 +748,14 @@ void update_tur_kepsilon(Case& cs) {
     }
     cs.bs[row] = cs.ED[ic];
   }
+}
+
+void update_tur_kepsilon(Case& cs) {
+  const double Cmu = kCmuKE;
+  const int n = cs.Ncel;
+  keps_build_te(cs);
+  solve_or_throw(cs, cs.As, 2, 1.e-8, 500, false, cs.bs.data(), cs.TE.data(), "Tn");
+  keps_build_ed(cs);
   solve_or_throw(cs, cs.As, 2, 1.e-8, 500, false, cs.bs.data(), cs.ED.data(), "ED");
   cs.As.zero();
   for (int i = 0; i < n; i++)

@@ -866,6 +866,24 @@ __global__ void k_keps_sources(int ncel, const double* __restrict__ c_vol, const
 // SetBCKEpsilon wall part (navier_bc.cpp:248-286): one thread per wall cell walks that
 // cell's wall faces in boundary order, so repeated updates of a corner cell happen in the
 // reference's sequence.
+// x^1.5 rounded once to nearest, the value pow(x, 1.5) stands for in the wall function
+// (navier_bc.cpp:279).  C libraries round pow to within about 0.52 ulp, so their results differ
+// from one another and from the exact rounding for a small share of arguments (0.07 % with
+// glibc's pow over 1e-9..1e2); the oracle computes the same function as below, so both agree
+// to the bit.  x*sqrt(x) with s = sqrt(x) correctly rounded (IEEE), the root's exact remainder
+// x - s*s (one FMA) and its Newton correction (x - s*s) / (2s), and the exact error of the
+// product x*s (Dekker's two-product by FMA); the sum is within 2^-100 relative of x^1.5 before
+// its one rounding.
+__device__ __forceinline__ double pow15(double x) {
+  if (x == 0.0) return 0.0;
+  const double s = sqrt(x);
+  const double r = fma(-s, s, x);
+  const double d = r / (2.0 * s);
+  const double p = x * s;
+  const double e = fma(x, s, -p);
+  return p + (e + x * d);
+}
+
 __global__ void k_keps_wall(int n_wc, const int* __restrict__ wc_cell, const int* __restrict__ wc_start,
                             const int* __restrict__ wc_bnd, const int* __restrict__ b_face,
                             const double* __restrict__ b_dist, const double* __restrict__ f_n,
@@ -900,7 +918,7 @@ __global__ void k_keps_wall(int n_wc, const int* __restrict__ wc_cell, const int
     if (yplus < 11.) utau = sqrt(tauw / ro);
     else utau = cmu25 * sqrt(te);
     prod = tauw * utau / (kappa * dist);
-    double eps = cmu75 * pow(te, 1.5) / (kappa * dist);
+    double eps = cmu75 * pow15(te) / (kappa * dist);
     tes = prod * vol;
     apte -= ro * ed / te * vol;
     apte += ro * eps / te * vol;

@@ -770,8 +770,9 @@ void calculate_pressure(cycas_ctx& c) {
   launch_correct_ruface(c.m, c.f, c.urf[3], c.stream, c.density);
 }
 
-// UpdateTurKEpsilon (navier_scalar.cpp:11-197)
-void update_keps(cycas_ctx& c) {
+// UpdateTurKEpsilon (navier_scalar.cpp:11-197), k rows: sources, wall functions and boundary
+// values, unsteady terms, the assembled system in As / bs
+void build_te(cycas_ctx& c) {
   launch_keps_sources(c.m, c.f, c.stream);
   launch_keps_wall(c.m, c.f, c.stream);
   if (c.tc.scheme != 0) {  // unsteady terms (navier_scalar.cpp:71-90); the epsilon source is
@@ -781,11 +782,20 @@ void update_keps(cycas_ctx& c) {
   }
   grad1(c, c.f.TE, c.f.BTE, c.f.dPhidX);
   launch_scalar(c.m, c.f, c.f.TE, c.f.BTE, c.f.VisTE, c.f.TES, c.f.ApTE, c.urf[5], c.st, c.stream);
-  solve(c, CYCAS_SYS_SCALAR, c.f.As, c.f.dinv_s, c.f.bs, c.f.TE, false);
+}
+
+// epsilon rows on the solved k: k clipped, epsilon sources, the wall cells' fixed rows
+void build_ed(cycas_ctx& c) {
   launch_clip_te(c.m, c.f, c.stream);
   grad1(c, c.f.ED, c.f.BED, c.f.dPhidX);
   launch_scalar(c.m, c.f, c.f.ED, c.f.BED, c.f.VisED, c.f.EDS, c.f.ApED, c.urf[5], c.st, c.stream);
   launch_eps_wall_rows(c.m, c.f, c.stream);
+}
+
+void update_keps(cycas_ctx& c) {
+  build_te(c);
+  solve(c, CYCAS_SYS_SCALAR, c.f.As, c.f.dinv_s, c.f.bs, c.f.TE, false);
+  build_ed(c);
   solve(c, CYCAS_SYS_SCALAR, c.f.As, c.f.dinv_s, c.f.bs, c.f.ED, false);
   launch_finish_keps(c.m, c.f, c.stream);
 }
@@ -1798,6 +1808,8 @@ int cycas_run_stage(cycas_ctx* c, const char* stage) {
     else if (s == "calculate_velocity") calculate_velocity(x);
     else if (s == "calculate_pressure") calculate_pressure(x);
     else if (s == "keps") update_keps(x);
+    else if (s == "build_te") build_te(x);
+    else if (s == "build_ed") build_ed(x);
     else if (s == "energy") update_energy(x);
     else if (s == "build_energy") build_energy(x);
     else if (s == "save_transient") save_old_level(x);

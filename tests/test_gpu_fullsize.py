@@ -83,6 +83,15 @@ def test_assembly_and_correction_stages_bit_exact(bench_pair):
             assert _bits_equal(a, b), f"{stage}/{nm}: max |diff| {np.max(np.abs(a - b))}"
 
 
+def test_keps_stages_bit_exact_at_full_size(bench_pair):
+    from test_gpu_parity import _keps_stages_bit_exact
+    o, g = bench_pair
+    g.iterate(1)
+    for nm in STATE + ["dUdX", "dVdX", "dWdX"]:
+        o.set(nm, g.get(nm))
+    _keps_stages_bit_exact(o, g)
+
+
 def _csr(g, name):
     n = g.case.ncel
     return sp.csr_matrix((g.get(name), g.get_int("A_col"), g.get_int("A_rowptr")), shape=(n, n))

@@ -50,6 +50,38 @@ def test_geometry_bit_exact(cases, name):
     assert np.array_equal(g.get_int("A_col"), o.geti("A_col"))
 
 
+KEPS_TE = ["Prod", "TESource", "ApTE", "VisTE", "VisED", "BTE", "BED", "ED", "dPhidX", "As_val", "bs"]
+KEPS_ED = ["TE", "EDSource", "ApED", "dPhidX", "As_val", "bs"]
+
+
+def _keps_stages_bit_exact(o, g):
+    """k rows, then epsilon rows on a k both sides share (the GPU's k after its own solve)."""
+    o.stage("build_te")
+    g.stage("build_te")
+    for nm in KEPS_TE:
+        a, b = g.get(nm), o.get(nm)
+        assert _bits_equal(a, b), f"build_te/{nm}: max |diff| {np.max(np.abs(a - b))}"
+    te = np.abs(np.random.default_rng(7).standard_normal(o.ncel)) * np.mean(np.abs(o.get("TE")))
+    te[::97] = 1e-12  # below the clip
+    o.set("TE", te)
+    g.set("TE", te)
+    o.stage("build_ed")
+    g.stage("build_ed")
+    for nm in KEPS_ED:
+        a, b = g.get(nm), o.get(nm)
+        assert _bits_equal(a, b), f"build_ed/{nm}: max |diff| {np.max(np.abs(a - b))}"
+
+
+@pytest.mark.parametrize("name", ["channel_tiny", "channel_small"])
+def test_keps_stages_bit_exact(cases, name):
+    o, g = _pair(cases(name))
+    o.iterate(3)
+    _copy_state(o, g, True)
+    for nm in ("dUdX", "dVdX", "dWdX"):
+        g.set(nm, o.get(nm))
+    _keps_stages_bit_exact(o, g)
+
+
 @pytest.mark.parametrize("name", ["cavity8", "channel_small"])
 def test_assembly_stages_bit_exact(cases, name):
     o, g = _pair(cases(name))

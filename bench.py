@@ -34,14 +34,23 @@ sys.path.insert(0, ROOT)
 CONFIG = {"nx": 200, "ny": 20, "nz": 20, "jitter": 0.15, "seed": 2026}
 WORKLOAD = "kepsilon channel 200x20x20x6 jittered tets (480000 cells), FP64 SIMPLE-C"
 METRIC = "cell-iters/s (steady SIMPLE-C, k-eps channel 480k tets)"
-GMRES_POLY = 2  # degree of the Jacobi-Neumann preconditioner of the GMRES systems in every GPU run
+# Degree of the Jacobi-Neumann preconditioner of the GMRES systems: single large cases (the
+# 480k and 3.84M-tet channels) run fastest at 5 -- each degree adds one matrix product per Krylov
+# iteration and saves iterations up to about there (GMRES ms per 10 iterations on the 480k
+# channel: degree 2 39.8, 3 34.6, 4 32.7, 5 31.3, 6 32.9); batches of small cases (the cavity
+# sample, the serving stream), whose systems converge in a few iterations anyway, at 1 to 3
+# (degrees 1/2/3/5 on the 32-cavity batch: 73.5/73.8/74.1/69.3 M cell-iters/s).
+GMRES_POLY = 5
+BATCH_POLY = 2
 
 
-def gmres_pc(opt):
+def gmres_pc(opt, degree=None):
     """Sets the preconditioner of the GMRES systems (momentum, k, epsilon) of `opt` to the
-    Jacobi-Neumann polynomial of degree GMRES_POLY; the pressure correction keeps its own."""
+    Jacobi-Neumann polynomial of the given degree (GMRES_POLY by default); the pressure
+    correction keeps its own."""
     from sysu_cfd_parallel_gb300 import capi
-    pc = capi.PC_POLY2 if GMRES_POLY == 2 else capi.PC_POLY1
+    degree = GMRES_POLY if degree is None else degree
+    pc = {1: capi.PC_POLY1, 2: capi.PC_POLY2, 3: capi.PC_POLY3, 4: capi.PC_POLY4, 5: capi.PC_POLY5}[degree]
     opt.ksp[capi.SYS_VELOCITY].pc = pc
     opt.ksp[capi.SYS_SCALAR].pc = pc
     return opt
@@ -172,7 +181,7 @@ def measure_batched(local, count, steps, mixed=False):
     import torch
     from sysu_cfd_parallel_gb300.solver import Batch, Case, NavierStokesSolver, batch_options
     params = batch_cases(count)
-    opt = gmres_pc(batch_options(device=local))
+    opt = gmres_pc(batch_options(device=local), BATCH_POLY)
     opt.mixed = 1 if mixed else 0
     cases = [Case(p) for p in params]
     cells = sum(c.ncel for c in cases)
@@ -187,7 +196,7 @@ def measure_batched(local, count, steps, mixed=False):
     ms_bg = timed_iterations(b, steps, stream)
     b.close()
     # the same batch with mixed-precision GMRES
-    opt_m = gmres_pc(batch_options(device=local))
+    opt_m = gmres_pc(batch_options(device=local), BATCH_POLY)
     opt_m.mixed = 1
     bm = Batch(cases, opt_m)
     stream_m = torch.cuda.ExternalStream(bm.stream_handle(), device=local)
@@ -380,7 +389,7 @@ def run_serve(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     reqs = serve_requests(args)
-    opt = gmres_pc(batch_options(device=local))
+    opt = gmres_pc(batch_options(device=local), BATCH_POLY)
     opt.mixed = 1 if args.mixed else 0
     srv = Server(hbm_budget_gb=args.budget_gb, residual_tol=args.tol, max_iters=args.max_iters, options=opt)
     t0 = Server.clock()

@@ -52,15 +52,21 @@ enum {
   CYCAS_PC_JACOBI = 1,   /* PCJACOBI: z = r / diag(A) */
   CYCAS_PC_ILU0 = 2,     /* ILU(0) in the natural (reference) cell order -- PETSc's
                             one-rank default PC (not available in this build) */
-  CYCAS_PC_AMG = 3,      /* one V-cycle of plain aggregation multigrid (pressure system, CG
-                            only): aggregates of <= 4 cells, weighted Jacobi w = 2/3, coarse
-                            correction scaled by 2, dense coarsest level (<= 64 rows) */
+  CYCAS_PC_AMG = 3,      /* one cycle of plain aggregation multigrid (pressure system, CG
+                            only): aggregates of <= 4 cells, weighted Jacobi (w 0.9), coarse
+                            correction scaled by 2, dense coarsest level (<= 64 rows); see
+                            cycas_options.amg_* */
   CYCAS_PC_POLY1 = 4,    /* Jacobi-Neumann polynomial of degree 1: M^-1 = (2I - D^-1 A) D^-1,
                             GMRES systems only (one more matrix product and grid barrier per
                             Krylov iteration, about half the iterations of Jacobi); in mixed
                             precision its stages run in FP32; no counterpart in the reference,
                             which uses PETSc's ILU(0) */
-  CYCAS_PC_POLY2 = 5     /* the same of degree 2: sum_{i<=2} (I - D^-1 A)^i D^-1 */
+  CYCAS_PC_POLY2 = 5,    /* the same of degree 2: sum_{i<=2} (I - D^-1 A)^i D^-1 */
+  CYCAS_PC_POLY3 = 6,    /* ... of degree 3 */
+  CYCAS_PC_POLY4 = 7,    /* ... of degree 4 */
+  CYCAS_PC_POLY5 = 8     /* ... of degree 5 (the fastest on the 480k-tet channel: each degree
+                            costs one matrix product and barrier per iteration and saves
+                            iterations up to about here) */
 };
 
 /* Krylov methods */

@@ -66,9 +66,11 @@ struct Csr {
   void zero() { std::fill(val.begin(), val.end(), 0.0); }
 };
 
-// PC_POLY1 / PC_POLY2: Jacobi-Neumann polynomials sum_{i<=d} (I - D^-1 A)^i D^-1 (the GPU
-// path's optional preconditioner for the GMRES systems)
-enum PcType { PC_NONE = 0, PC_JACOBI = 1, PC_ILU0 = 2, PC_POLY1 = 3, PC_POLY2 = 4 };
+// PC_POLY1..5: Jacobi-Neumann polynomials sum_{i<=d} (I - D^-1 A)^i D^-1 of degree d = 1..5
+// (the GPU path's optional preconditioner for the GMRES systems)
+enum PcType { PC_NONE = 0, PC_JACOBI = 1, PC_ILU0 = 2, PC_POLY1 = 3, PC_POLY2 = 4, PC_POLY3 = 5, PC_POLY4 = 6,
+              PC_POLY5 = 7 };
+inline int poly_degree(int pc) { return pc >= PC_POLY1 && pc <= PC_POLY5 ? pc - PC_POLY1 + 1 : 0; }
 
 enum KspType { KSP_GMRES = 0, KSP_CG = 1 };
 

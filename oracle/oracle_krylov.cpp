@@ -37,7 +37,7 @@ struct Pc {
     type = s.pc;
     n = M.n;
     A = &M;
-    if (type == PC_JACOBI || type == PC_POLY1 || type == PC_POLY2) {
+    if (type == PC_JACOBI || poly_degree(type) > 0) {
       dinv.resize(n);
       for (int i = 0; i < n; i++) dinv[i] = 1.0 / M.val[M.diag[i]];
     } else if (type == PC_ILU0) {
@@ -94,9 +94,9 @@ struct Pc {
       std::copy(r, r + n, z);
     } else if (type == PC_JACOBI) {
       for (int i = 0; i < n; i++) z[i] = r[i] * dinv[i];
-    } else if (type == PC_POLY1 || type == PC_POLY2) {
+    } else if (poly_degree(type) > 0) {
       // y_0 = D^-1 r, y_i = y_0 + y_{i-1} - D^-1 A y_{i-1}
-      const int deg = type == PC_POLY1 ? 1 : 2;
+      const int deg = poly_degree(type);
       std::vector<double> z0(n), y(n), ay(n);
       for (int i = 0; i < n; i++) z0[i] = r[i] * dinv[i];
       y = z0;

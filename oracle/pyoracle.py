@@ -15,7 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle_cycas.so")
 
-PC_NONE, PC_JACOBI, PC_ILU0, PC_POLY1, PC_POLY2 = 0, 1, 2, 3, 4
+PC_NONE, PC_JACOBI, PC_ILU0, PC_POLY1, PC_POLY2, PC_POLY3, PC_POLY4, PC_POLY5 = 0, 1, 2, 3, 4, 5, 6, 7
 KSP_GMRES, KSP_CG = 0, 1
 VELOCITY, PRESSURE, SCALAR = 0, 1, 2
 

@@ -23,7 +23,7 @@ CYCAS_ERR_TIMEOUT = 7
 CYCAS_ERR_MESH = 8
 CYCAS_ERR_UNSUPPORTED = 9
 
-PC_NONE, PC_JACOBI, PC_ILU0, PC_AMG, PC_POLY1, PC_POLY2 = 0, 1, 2, 3, 4, 5
+PC_NONE, PC_JACOBI, PC_ILU0, PC_AMG, PC_POLY1, PC_POLY2, PC_POLY3, PC_POLY4, PC_POLY5 = 0, 1, 2, 3, 4, 5, 6, 7, 8
 LOAD_MSH_BINARY = 1
 DUMP_TECPLOT, DUMP_DATA, DUMP_BACKUP = 1, 2, 4
 KSP_DEFAULT, KSP_GMRES, KSP_CG = 0, 1, 2

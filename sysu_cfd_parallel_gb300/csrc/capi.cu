@@ -219,6 +219,18 @@ const int kRefMaxit[3] = {1000, 1000, 500};
 void require(bool ok, const std::string& msg) {
   if (!ok) throw StatusError(CYCAS_ERR_INVALID, msg);
 }
+// degree of a Jacobi-Neumann polynomial preconditioner, 0 for the others
+int poly_degree(int pc) {
+  switch (pc) {
+    case CYCAS_PC_POLY1: return 1;
+    case CYCAS_PC_POLY2: return 2;
+    case CYCAS_PC_POLY3: return 3;
+    case CYCAS_PC_POLY4: return 4;
+    case CYCAS_PC_POLY5: return 5;
+    default: return 0;
+  }
+}
+
 // the same for a literal message: nothing is built unless the check fails (the mesh checks run
 // per face and per vertex, where a std::string per call cost more than the checks)
 void require(bool ok, const char* msg) {
@@ -460,10 +472,11 @@ void alloc_krylov(cycas_ctx& c) {
   KrylovWork& w = c.kw;
   w.m = maxm;
   w.ldv = ((long)c.m.ncel + 31) / 32 * 32;
-  bool poly = false;
-  for (int s = 0; s < 3; s++) poly |= c.ksp[s].pc == CYCAS_PC_POLY1 || c.ksp[s].pc == CYCAS_PC_POLY2;
-  // three momentum systems in lockstep, each with two Neumann scratch vectors when needed
-  w.v_len = (3L * (maxm + 1) + (poly ? 6 : 0)) * w.ldv;
+  int poly = 0;
+  for (int s = 0; s < 3; s++) poly = std::max(poly, poly_degree(c.ksp[s].pc));
+  // three momentum systems in lockstep, each with two Neumann scratch vectors (three from
+  // degree 3) when needed
+  w.v_len = (3L * (maxm + 1) + (poly ? 3L * (poly >= 3 ? 3 : 2) : 0)) * w.ldv;
   w.V = c.alloc<double>(w.v_len);
   w.nblocks = gmres_max_blocks(c.device);
   // per CTA and per lockstep system (up to the three momentum components)
@@ -544,10 +557,9 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
   for (int i = 0; i < 3; i++) c.gravity[i] = p->gravity[i];
   for (int s = 0; s < 3; s++) {
     const cycas_ksp_options& k = o->ksp[s];
-    require(k.pc == CYCAS_PC_NONE || k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_AMG || k.pc == CYCAS_PC_POLY1 ||
-                k.pc == CYCAS_PC_POLY2,
+    require(k.pc == CYCAS_PC_NONE || k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_AMG || poly_degree(k.pc) > 0,
             "preconditioner not available in this build");
-    require(!(k.pc == CYCAS_PC_POLY1 || k.pc == CYCAS_PC_POLY2) ||
+    require(poly_degree(k.pc) == 0 ||
                 (s != CYCAS_SYS_PRESSURE && k.type != CYCAS_KSP_CG),
             "the polynomial preconditioner is for the GMRES systems (momentum, scalars)");
     require(k.restart >= 1 && k.restart <= kMaxRestart, "restart out of range");
@@ -592,8 +604,8 @@ void solve(cycas_ctx& c, int sys, const double* val, const double* dinv, const d
   g.rowptr = c.m.rowptr;
   g.col = c.m.col;
   g.val = val;
-  g.dinv = (k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_POLY1 || k.pc == CYCAS_PC_POLY2) ? dinv : nullptr;
-  g.poly = k.pc == CYCAS_PC_POLY1 ? 1 : (k.pc == CYCAS_PC_POLY2 ? 2 : 0);
+  g.dinv = (k.pc == CYCAS_PC_JACOBI || poly_degree(k.pc) > 0) ? dinv : nullptr;
+  g.poly = poly_degree(k.pc);
   g.b = b;
   g.x = x;
   g.guess_zero = guess_zero ? 1 : 0;
@@ -662,9 +674,9 @@ void solve_velocity(cycas_ctx& c, double* const* xs_in = nullptr, const KspConf*
     g[q].rowptr = c.m.rowptr;
     g[q].col = c.m.col;
     g[q].val = c.f.Au;
-    g[q].dinv = (k.pc == CYCAS_PC_JACOBI || k.pc == CYCAS_PC_POLY1 || k.pc == CYCAS_PC_POLY2) ? c.f.dinv_u
+    g[q].dinv = (k.pc == CYCAS_PC_JACOBI || poly_degree(k.pc) > 0) ? c.f.dinv_u
                                                                                                  : nullptr;
-    g[q].poly = k.pc == CYCAS_PC_POLY1 ? 1 : (k.pc == CYCAS_PC_POLY2 ? 2 : 0);
+    g[q].poly = poly_degree(k.pc);
     g[q].b = bs[q];
     g[q].x = xs[q];
     g[q].guess_zero = 0;
@@ -1891,7 +1903,7 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
   return guard([&]() -> int {
     require(n > 0 && rowptr && col && val && b && x && ksp, "bad argument");
     require(ksp->restart >= 1 && ksp->restart <= kMaxRestart, "restart out of range");
-    const bool poly = ksp->pc == CYCAS_PC_POLY1 || ksp->pc == CYCAS_PC_POLY2;
+    const int poly = poly_degree(ksp->pc);
     require(ksp->pc == CYCAS_PC_NONE || ksp->pc == CYCAS_PC_JACOBI || poly, "preconditioner not available in this build");
     require(ksp->type >= CYCAS_KSP_DEFAULT && ksp->type <= CYCAS_KSP_CG, "unknown Krylov type");
     require(!(poly && ksp->type == CYCAS_KSP_CG), "the polynomial preconditioner is for GMRES");
@@ -1919,7 +1931,7 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
     DevStatus* st = c.alloc<DevStatus>(1);
     c.kw.m = std::max(ksp->restart, 3);
     c.kw.ldv = ((long)n + 31) / 32 * 32;
-    c.kw.v_len = (c.kw.m + 1 + (poly ? 2 : 0)) * c.kw.ldv;
+    c.kw.v_len = (c.kw.m + 1 + (poly ? (poly >= 3 ? 3 : 2) : 0)) * c.kw.ldv;
     c.kw.V = c.alloc<double>(c.kw.v_len);
     c.kw.nblocks = gmres_max_blocks(0);
     c.kw.part_len = (long)c.kw.nblocks * kGmresPartStride;
@@ -1931,7 +1943,7 @@ int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const 
     g.col = d_col;
     g.val = d_val;
     g.dinv = ksp->pc == CYCAS_PC_JACOBI || poly ? d_dinv : nullptr;
-    g.poly = ksp->pc == CYCAS_PC_POLY1 ? 1 : (ksp->pc == CYCAS_PC_POLY2 ? 2 : 0);
+    g.poly = poly;
     g.b = d_b;
     g.x = d_x;
     g.guess_zero = guess_zero ? 1 : 0;

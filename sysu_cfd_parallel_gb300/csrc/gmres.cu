@@ -64,11 +64,12 @@ struct GmMsArgs {
   // batched solves: teams of CTAs, each solving its cases' row ranges in turn (null: one team
   // of the whole grid solving rows [0, n))
   const BatchSchedule* sched;
-  // polynomial preconditioner (degree 1 or 2; 0: the Jacobi scaling alone): two scratch vectors
-  // per system, Zs and S1, at (s * ldv)
+  // polynomial preconditioner (degree 1 to 5; 0: the Jacobi scaling alone): scratch vectors per
+  // system at (s * ldv): Zs and S1, and S2 from degree 3 on
   int poly;
   T* Zs;
   T* S1;
+  T* S2;  // second stage scratch (degree 3)
 };
 
 // the CTAs that solve one row range together
@@ -167,6 +168,7 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
   const int poly = a.poly;
   auto Zv = [&](int s) { return a.Zs + (long)s * a.ldv; };
   auto S1v = [&](int s) { return a.S1 + (long)s * a.ldv; };
+  auto S2v = [&](int s) { return a.S2 + (long)s * a.ldv; };
 
   // w_s = D^-1 A v_{s,it[s]} / |v_{s,it[s]}| into v_{s,it[s]+1} (with the polynomial
   // preconditioner: into z_s, the input of its Neumann stages) for the systems in mask, over this
@@ -200,8 +202,9 @@ __device__ __forceinline__ void gmres_team(const GmMsArgs<NS, Tv>& a, const Team
       Tv* outp[NS];
 #pragma unroll
       for (int s = 0; s < NS; s++) {
-        src[s] = st == 1 ? Zv(s) : S1v(s);
-        outp[s] = st == poly ? dst[s] : S1v(s);
+        // stages alternate between the two scratch vectors, the last one writes dst
+        src[s] = st == 1 ? Zv(s) : (st % 2 == 0 ? S1v(s) : S2v(s));
+        outp[s] = st == poly ? dst[s] : (st % 2 == 1 ? S1v(s) : S2v(s));
       }
       for (int r = r0 + tid; r < r1; r += kGmThreads) {
         Tv acc[NS];
@@ -625,9 +628,9 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
   const GmresCall& c = calls[0];
   // workspace bounds: basis NS*(m+1) vectors, partials nb*NS*stride
   const int nb = sched ? grid : gmres_grid(c.n, w.nblocks);
-  const int extra = c.poly ? 2 * NS : 0;  // Neumann scratch vectors
+  const int extra = c.poly ? (c.poly >= 3 ? 3 : 2) * NS : 0;  // Neumann scratch vectors
   if (c.restart < 1 || c.restart > kMaxRestart || ((long)NS * (c.restart + 1) + extra) * w.ldv > w.v_len ||
-      (long)nb * NS * kPartStride > w.part_len || w.ldv < c.n || c.poly < 0 || c.poly > 2 ||
+      (long)nb * NS * kPartStride > w.part_len || w.ldv < c.n || c.poly < 0 || c.poly > 5 ||
       (c.poly && (!c.dinv || (sizeof(Tv) != sizeof(double) && !c.dinv32))))
     return cudaErrorInvalidValue;
   a.n = c.n;
@@ -660,6 +663,7 @@ cudaError_t launch_ms(const GmresCall* calls, KrylovWork& w, cudaStream_t s, con
   a.poly = c.poly;
   a.Zs = a.V + (long)NS * (c.restart + 1) * w.ldv;
   a.S1 = a.Zs + (long)NS * w.ldv;
+  a.S2 = a.S1 + (long)NS * w.ldv;  // used from degree 3 on (inside the capacity checked above)
   a.part = w.part;
   a.bar = w.bar;
   a.err = c.err;

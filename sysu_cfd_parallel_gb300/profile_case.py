@@ -23,7 +23,7 @@ def main(argv=None):
     ap.add_argument("--iters", type=int, default=2)
     ap.add_argument("--pressure-pc", default="amg", choices=["amg", "jacobi"])
     ap.add_argument("--mixed", action="store_true", help="FP32 Arnoldi cycles in FP64 refinement")
-    ap.add_argument("--pc", default="jacobi", choices=["jacobi", "poly1", "poly2"],
+    ap.add_argument("--pc", default="jacobi", choices=["jacobi", "poly1", "poly2", "poly3", "poly4", "poly5"],
                     help="preconditioner of the GMRES systems (momentum, scalars)")
     ap.add_argument("--warmup", type=int, default=0, help="untimed iterations before the profiled ones")
     ap.add_argument("--amg-omega", type=float, default=0.0, help="AMG smoother weight (0: library default)")
@@ -47,7 +47,8 @@ def main(argv=None):
     opt.mixed = 1 if args.mixed else 0
     opt.amg_omega = args.amg_omega
     opt.amg_gamma = args.amg_gamma
-    gpc = {"jacobi": capi.PC_JACOBI, "poly1": capi.PC_POLY1, "poly2": capi.PC_POLY2}[args.pc]
+    gpc = {"jacobi": capi.PC_JACOBI, "poly1": capi.PC_POLY1, "poly2": capi.PC_POLY2, "poly3": capi.PC_POLY3,
+           "poly4": capi.PC_POLY4, "poly5": capi.PC_POLY5}[args.pc]
     opt.ksp[capi.SYS_VELOCITY].pc = gpc
     opt.ksp[capi.SYS_SCALAR].pc = gpc
     s = NavierStokesSolver(Case(param), opt)

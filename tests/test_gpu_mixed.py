@@ -63,15 +63,16 @@ def test_mixed_batch_matches_mixed_alone(cases):
             assert _rel_l2(b.case_field(nm, c), s.get(nm)) < 1e-5, (names[c], nm)
 
 
-@pytest.mark.parametrize("name,steps", [("cavity8j", 8), ("channel_small", 5)])
-def test_mixed_polynomial_matches_fp64_polynomial(cases, name, steps):
-    """Mixed precision with the Jacobi-Neumann preconditioner of degree 2 (its stages in FP32)
-    against the FP64 path with the same preconditioner."""
+@pytest.mark.parametrize("name,steps,pc", [("cavity8j", 8, capi.PC_POLY2), ("channel_small", 5, capi.PC_POLY2),
+                                           ("channel_small", 5, capi.PC_POLY3)])
+def test_mixed_polynomial_matches_fp64_polynomial(cases, name, steps, pc):
+    """Mixed precision with a Jacobi-Neumann preconditioner (its stages in FP32) against the FP64
+    path with the same preconditioner."""
     p = cases(name)
     opts = [_opts(False), _opts(True)]
     for o in opts:
-        o.ksp[capi.SYS_VELOCITY].pc = capi.PC_POLY2
-        o.ksp[capi.SYS_SCALAR].pc = capi.PC_POLY2
+        o.ksp[capi.SYS_VELOCITY].pc = pc
+        o.ksp[capi.SYS_SCALAR].pc = pc
     g64 = NavierStokesSolver(Case(p), opts[0])
     g32 = NavierStokesSolver(Case(p), opts[1])
     r64 = g64.iterate(steps)

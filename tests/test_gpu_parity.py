@@ -258,13 +258,15 @@ def test_amg_cuts_pressure_iterations(cases):
     assert r2["ksp_its"][:, 3].max() * 3 < r1["ksp_its"][:, 3].min()
 
 
-@pytest.mark.parametrize("name,steps,poly", [("cavity8j", 8, 1), ("channel_small", 5, 1), ("channel_small", 4, 2)])
+@pytest.mark.parametrize("name,steps,poly", [("cavity8j", 8, 1), ("channel_small", 5, 1), ("channel_small", 4, 2),
+                                             ("cavity8j", 6, 3), ("channel_small", 4, 3), ("channel_small", 4, 5),
+                                             ("cavity8j", 5, 5)])
 def test_polynomial_preconditioner_matches_oracle(cases, name, steps, poly):
     """GMRES with the Jacobi-Neumann polynomial preconditioner (momentum and scalars; CG with
     Jacobi for the pressure correction), GPU against the oracle's restatement of it."""
     p = cases(name)
-    opc = po.PC_POLY1 if poly == 1 else po.PC_POLY2
-    gpc = capi.PC_POLY1 if poly == 1 else capi.PC_POLY2
+    opc = {1: po.PC_POLY1, 2: po.PC_POLY2, 3: po.PC_POLY3, 5: po.PC_POLY5}[poly]
+    gpc = {1: capi.PC_POLY1, 2: capi.PC_POLY2, 3: capi.PC_POLY3, 5: capi.PC_POLY5}[poly]
     o = po.OracleCase(p)
     o.set_ksp(po.VELOCITY, opc, 30)
     o.set_ksp(po.PRESSURE, po.PC_JACOBI, 30)

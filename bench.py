@@ -6,9 +6,10 @@ Workload (a "step" = one SIMPLE-C outer iteration over the whole case):
   jittered U(-0.15h, 0.15h) (seed 2026), inlet U=(1,0,0) with k=1.5(0.05U)^2 and
   eps=0.09^0.75 k^1.5/0.07, outlet, no-slip walls, rho=1, mu=2e-5; FP64 SIMPLE-C + standard
   k-epsilon with wall functions; the reference's Krylov methods and tolerances (GMRES(30)
-  rtol 1e-8 for velocity and k/eps with Jacobi, CG rtol 1e-6 for the pressure correction with
-  one aggregation-AMG V-cycle as preconditioner: the reference's ILU(0) needs ~390 CG
-  iterations per solve on this mesh and Jacobi does not converge within its 1000 cap).
+  rtol 1e-8 for velocity and k/eps, preconditioned by a Jacobi-Neumann polynomial of degree
+  GMRES_POLY; CG rtol 1e-6 for the pressure correction with one aggregation-AMG cycle as
+  preconditioner: the reference's ILU(0) needs ~390 CG iterations per solve on this mesh and
+  Jacobi does not converge within its 1000 cap).
 
 Metric: cell-iterations/s = cells x timed iterations / device time (CUDA events on the
 solver's stream).  The working set (fields, face geometry, three CSR systems, Krylov basis)
@@ -375,7 +376,7 @@ def run_precision(args):
             "dtype": "mixed", "data": "synthetic",
             "config": {"workload": "kepsilon channel 400x40x40x6 jittered tets (3840000 cells), seed 2027",
                        "krylov": "GMRES systems: FP32 Arnoldi cycles (inner rtol 1e-4) in FP64 iterative "
-                                 "refinement; CG + FP32 AMG V-cycle (p'); every system to the outer rtol "
+                                 "refinement; CG + FP32 AMG cycle (p'); every system to the outer rtol "
                                  "in both runs", "outer_rtol": args.outer_rtol}}
     print(json.dumps(line), flush=True)
 
@@ -479,7 +480,9 @@ class Clocks:
 
 # ---------------------------------------------------------------- roofline bookkeeping
 def vcycle_bytes(levels):
-    """Algorithmic bytes of one AMG V-cycle.  Per level with a coarser one (n rows, nnz
+    """Algorithmic bytes of one AMG cycle: one pass over every level (the second cycle that
+    large cases run on their shared-memory levels reads no global memory).  Per level with a
+    coarser one (n rows, nnz
     entries, nc coarse rows): pre-smoothing + residual 12 nnz + 36 n, restriction 12 n + 12 nc,
     prolongation + post-smoothing 12 nnz + 40 n + 8 nc; coarsest level: dense inverse
     8 nc^2 + 16 nc."""
@@ -498,7 +501,7 @@ def krylov_bytes(its_row, turb, n, nnz, restart=30, levels=None, poly=0):
     """Algorithmic bytes of each Krylov launch of one iteration (solve slots in call order).
 
     CG iteration: reads A (12 nnz + 4 (n+1)), p, z, r, w, x, D^-1 (48 n); writes p, w, x, r, z
-    (40 n); with the AMG preconditioner one V-cycle (vcycle_bytes) replaces D^-1.
+    (40 n); with the AMG preconditioner one cycle (vcycle_bytes) replaces D^-1.
     GMRES Arnoldi step j: SpMV + Jacobi (12 nnz + 4 (n+1) + 24 n), CGS dots (8 n (j+2)) and update
     (8 n (j+1) + 16 n); per restart cycle: initial residual (12 nnz + 4 (n+1) + 40 n) and the
     solution update (8 n (m_used + 2)).  A Jacobi-Neumann preconditioner of degree `poly` adds
@@ -539,7 +542,7 @@ def krylov_fp64_flops(its_row, turb, n, nnz, restart=30, poly=0):
     update (4 n (j+1)) and the norm (2 n); per restart cycle the residual (2 nnz + 4 n) and the
     solution update (2 n m_used).  A Jacobi-Neumann preconditioner of degree `poly` adds
     2 nnz + 3 n per stage to every step and restart, and its application to D^-1 b once per
-    solve.  CG slots are left out (their V-cycle is FP32)."""
+    solve.  CG slots are left out (their AMG cycle is FP32)."""
     stage = 2 * nnz + 3 * n
     kinds = ["gmres", "gmres", "gmres", "cg"] + (["gmres", "gmres"] if turb else [])
     out = []
@@ -745,7 +748,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peak()
     launches = max(1, per_sys_launch[dom])
     achieved = (per_sys_bytes[dom] / launches) / (sys_ms[dom] / launches / 1e3) / 1e9 if sys_ms[dom] > 0 else 0.0
-    # FP64 roofline of the GMRES system with the larger share (the CG's V-cycle is FP32)
+    # FP64 roofline of the GMRES system with the larger share (the CG's AMG cycle is FP32)
     gdom = "gmres_vel" if sys_ms["gmres_vel"] >= sys_ms["gmres_scalar"] else "gmres_scalar"
     flops = sum(f for row in hist["ksp_its"] for slot, f in krylov_fp64_flops(row, turb, n, nnz, poly=GMRES_POLY)
                 if (slot < 3) == (gdom == "gmres_vel"))
@@ -817,13 +820,13 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "cells": n, "faces": case.nfac, "nnz": nnz,
                        "parallelism": f"replicas{world}", "l2": "working set > 129 MB L2, no flush",
                        "krylov": "GMRES(30) with the Jacobi-Neumann polynomial preconditioner of degree %d "
-                                 "(u,v,w,k,eps), CG+AMG V-cycle (p'), reference tolerances" % GMRES_POLY,
+                                 "(u,v,w,k,eps), CG+AMG cycle (p'), reference tolerances" % GMRES_POLY,
                        "krylov_its_last_step": [int(x) for x in hist["ksp_its"][-1]],
                        "amg_levels_rows": [int(x) for x in levels[0]],
                        "amg_levels_nnz": [int(x) for x in levels[1]]},
             "e2e": {"value": e2e_value, "unit": "cell-iters/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
-            "roofline": {"bound": "hbm", "kernel": {"cg": "k_cg_amg (pressure correction: CG + AMG V-cycle)",
+            "roofline": {"bound": "hbm", "kernel": {"cg": "k_cg_amg (pressure correction: CG + AMG cycle)",
                                                     "gmres_vel": "k_gmres_ms<3> (u, v, w in lockstep)",
                                                     "gmres_scalar": "k_gmres_ms<1> (k, epsilon)"}[dom],
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",

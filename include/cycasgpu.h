@@ -268,6 +268,24 @@ int cycas_simple_iteration_io(cycas_ctx* c, int32_t nin, const char* const* in_n
 int cycas_simple_iterations(cycas_ctx* ctx, int32_t n, double* res_hist, double* resmax, int32_t* its,
                             int32_t* reasons);
 
+/* The steady branch of NSSolve (NS/navier.cpp:52-145, IfSteady): SIMPLE-C iterations until
+ * ResMax < residual_steady (the reference's stop test, navier.cpp:141-145) or max_step of them
+ * ran.  *n_iter receives the iterations run; iteration k < cap reports res_hist[10k..],
+ * resmax[k], its[8k..] and reasons[8k..] as cycas_simple_iterations does (any of them may be
+ * null).  The result files of NSSolve's output cadence are the caller's (cycas_dump_begin).  A
+ * failed Krylov solve ends the loop with its status, as ConvergeError ends the reference's. */
+int cycas_solve_steady(cycas_ctx* ctx, int32_t max_step, double residual_steady, int32_t cap, int32_t* n_iter,
+                       double* res_hist, double* resmax, int32_t* its, int32_t* reasons);
+
+/* An in-HBM restart point (no counterpart in the reference, whose restart goes through the
+ * res.sav file of WriteBackupFile/ReadBackupFile, navierIO.cpp:370-404): SAVE copies every
+ * field of the context (cell and boundary fields, face fluxes, gradients, systems, previous
+ * time levels) and the clock into one device buffer, allocated on the first save; RESTORE puts
+ * them back.  Device-to-device copies queued on the context's stream. */
+#define CYCAS_RESTART_SAVE 0
+#define CYCAS_RESTART_RESTORE 1
+int cycas_restart_point(cycas_ctx* ctx, int32_t op);
+
 /* Individual stages for parity tests: bc_velocity bc_pressure bc_deltap grad_uvwp grad_deltap
  * build_velocity ruface2 build_pressure correct_cells correct_ruface calculate_velocity
  * calculate_pressure keps build_te (the k rows of keps) build_ed (the epsilon rows, on the

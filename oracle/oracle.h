@@ -138,6 +138,11 @@ struct Case {
   std::vector<double> Rnp, Unp, Vnp, Wnp, Tnp, TEp, EDp;
   std::vector<double> Rnp2, Unp2, Vnp2, Wnp2, Tnp2, TEp2, EDp2;
   double cur_time = 0.;
+
+  // TE^1.5 of the wall function: 0 = the mathematical value rounded once (pow15, what the GPU
+  // computes), 1 = the C library's std::pow, as the reference's own build calls it
+  // (navier_bc.cpp:279); the two differ by one ulp on a small share of arguments.
+  int libm_pow = 0;
 };
 
 // setup (mesh + params + init), following main.cpp:38-65 at one rank

@@ -241,6 +241,13 @@ int orc_set_ksp(void* hp, int which, int pc, int restart, double rtol_override, 
   return 0;
 }
 
+// TE^1.5 of the wall function: 0 rounded once (default, as the GPU), 1 the C library's pow (as
+// the reference's own build)
+int orc_set_libm_pow(void* hp, int flag) {
+  ((Handle*)hp)->cs.libm_pow = flag ? 1 : 0;
+  return 0;
+}
+
 int orc_set_ksp_perm(void* hp, int which, const int* perm, long n) {
   Case& cs = ((Handle*)hp)->cs;
   if (n == 0) cs.ksp[which].perm.clear();

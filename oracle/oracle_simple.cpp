@@ -687,7 +687,8 @@ void keps_build_te(Case& cs) {
     if (yplus < 11.) utau = std::sqrt(tauw / cs.Rn[ic]);
     else utau = Cmu25 * std::sqrt(cs.TE[ic]);
     Prod[ic] = tauw * utau / (kappa * dist);
-    double eps = std::pow(Cmu, 0.75) * pow15(cs.TE[ic]) / (kappa * dist);
+    double te15 = cs.libm_pow ? std::pow(cs.TE[ic], 1.5) : pow15(cs.TE[ic]);
+    double eps = std::pow(Cmu, 0.75) * te15 / (kappa * dist);
     TES[ic] = Prod[ic] * vol;
     ApTE[ic] -= cs.Rn[ic] * cs.ED[ic] / cs.TE[ic] * vol;
     ApTE[ic] += cs.Rn[ic] * eps / cs.TE[ic] * vol;

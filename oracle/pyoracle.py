@@ -45,6 +45,7 @@ def lib():
         L.orc_set_ksp.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
         L.orc_set_ksp_type.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_set_ksp_perm.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_long]
+        L.orc_set_libm_pow.argtypes = [C.c_void_p, C.c_int]
         L.orc_stage.argtypes = [C.c_void_p, C.c_char_p]
         L.orc_iterate.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_physics.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -135,6 +136,11 @@ class OracleCase:
         if perm is not None:
             p = np.ascontiguousarray(perm, dtype=np.int32)
             lib().orc_set_ksp_perm(self.h, which, _ptr(p), p.size)
+
+    def set_libm_pow(self, flag=True):
+        """TE^1.5 of the wall function through the C library's pow, as the reference's own build
+        computes it, instead of the once-rounded value the GPU computes."""
+        lib().orc_set_libm_pow(self.h, 1 if flag else 0)
 
     def stage(self, name):
         rc = lib().orc_stage(self.h, name.encode())

@@ -90,7 +90,7 @@ EXPORTS = (
     "cycas_dump_begin", "cycas_dump_wait",
     "cycas_create", "cycas_create_from_case", "cycas_destroy",
     "cycas_get_field", "cycas_set_field", "cycas_get_int", "cycas_simple_iteration", "cycas_simple_iteration_io", "cycas_simple_iterations",
-    "cycas_time_step", "cycas_case_physics", "cycas_set_fields", "cycas_get_fields", "cycas_solve_velocity", "cycas_solve_pressure", "cycas_solve_scalar",
+    "cycas_solve_steady", "cycas_restart_point", "cycas_time_step", "cycas_case_physics", "cycas_set_fields", "cycas_get_fields", "cycas_solve_velocity", "cycas_solve_pressure", "cycas_solve_scalar",
     "cycas_run_stage", "cycas_csr_solve", "cycas_get_stream", "cycas_set_profiling", "cycas_get_profile",
     "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels", "cycas_batch_create",
     "cycas_batch_size", "cycas_batch_offsets", "cycas_batch_iteration", "cycas_batch_residuals",
@@ -156,6 +156,8 @@ def load(build_if_missing: bool = True):
     L.cycas_simple_iteration_io.argtypes = [_P, C.c_int32, _P, _P, _P, C.c_int32, _P, _P, _P, _F64P, _F64P,
                                             C.POINTER(IterStats)]
     L.cycas_simple_iterations.argtypes = [_P, C.c_int32, _P, _P, _P, _P]
+    L.cycas_solve_steady.argtypes = [_P, C.c_int32, C.c_double, C.c_int32, C.POINTER(C.c_int32), _P, _P, _P, _P]
+    L.cycas_restart_point.argtypes = [_P, C.c_int32]
     L.cycas_run_stage.argtypes = [_P, C.c_char_p]
     L.cycas_solve_velocity.argtypes = [_P, C.c_double, C.c_int32, _P, _P, _P, C.POINTER(IterStats)]
     L.cycas_solve_pressure.argtypes = [_P, C.c_double, C.c_int32, _P, C.c_int32, C.POINTER(IterStats)]

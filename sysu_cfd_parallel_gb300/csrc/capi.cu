@@ -128,6 +128,8 @@ struct cycas_ctx {
   std::vector<void*> allocs;
   std::map<std::string, std::pair<double*, long>> dfields;
   std::map<std::string, std::pair<int*, long>> ifields;
+  double* restart_point = nullptr;   // copy of every named field (cycas_restart_point), or null
+  double restart_time = 0.0;         // the clock at the restart point
   // measurement
   long long launches_base = 0;   // g_launch_count at the last profile reset
   bool profiling = false;
@@ -1675,6 +1677,57 @@ int cycas_simple_iterations(cycas_ctx* c, int32_t n, double* res_hist, double* r
       }
       if (rc != CYCAS_OK) return rc;
     }
+    return CYCAS_OK;
+  });
+}
+
+int cycas_solve_steady(cycas_ctx* c, int32_t max_step, double residual_steady, int32_t cap, int32_t* n_iter,
+                       double* res_hist, double* resmax, int32_t* its, int32_t* reasons) {
+  return guard([&]() -> int {
+    require(c != nullptr && max_step >= 0 && cap >= 0 && n_iter != nullptr, "bad argument");
+    require(!c->is_batch && c->tc.scheme == 0, "cycas_solve_steady needs a steady single-case context");
+    *n_iter = 0;
+    for (int step = 1; step <= max_step; step++) {
+      cycas_iter_stats st;
+      double res[10], rm;
+      run_iteration(*c);
+      int rc = finish_iteration(*c, res, &rm, &st);
+      const int k = step - 1;
+      if (k < cap) {
+        if (res_hist) std::memcpy(res_hist + 10L * k, res, sizeof res);
+        if (resmax) resmax[k] = rm;
+        for (int q = 0; q < 8; q++) {
+          if (its) its[8L * k + q] = st.its[q];
+          if (reasons) reasons[8L * k + q] = st.reason[q];
+        }
+      }
+      *n_iter = step;
+      if (rc != CYCAS_OK) return rc;
+      if (rm < residual_steady) break;  // navier.cpp:141-145
+    }
+    return CYCAS_OK;
+  });
+}
+
+int cycas_restart_point(cycas_ctx* c, int32_t op) {
+  return guard([&]() -> int {
+    require(c != nullptr && (op == CYCAS_RESTART_SAVE || op == CYCAS_RESTART_RESTORE), "bad argument");
+    long total = 0;
+    for (const auto& kv : c->dfields) total += kv.second.second;
+    if (op == CYCAS_RESTART_SAVE && !c->restart_point) c->restart_point = c->alloc<double>(total);
+    require(c->restart_point != nullptr, "no restart point saved");
+    long off = 0;
+    for (const auto& kv : c->dfields) {  // std::map: the same order on save and restore
+      double* f = kv.second.first;
+      const size_t bytes = sizeof(double) * (size_t)kv.second.second;
+      double* r = c->restart_point + off;
+      if (bytes)
+        CK(cudaMemcpyAsync(op == CYCAS_RESTART_SAVE ? r : f, op == CYCAS_RESTART_SAVE ? f : r, bytes,
+                           cudaMemcpyDeviceToDevice, c->stream));
+      off += kv.second.second;
+    }
+    if (op == CYCAS_RESTART_RESTORE) c->cur_time = c->restart_time;
+    else c->restart_time = c->cur_time;
     return CYCAS_OK;
   });
 }

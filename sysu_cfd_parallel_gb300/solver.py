@@ -234,6 +234,31 @@ class NavierStokesSolver:
         self.step += n
         return {"residual": res, "resmax": rm, "ksp_its": its, "ksp_reason": rs}
 
+    def solve_steady(self, max_step: int | None = None, residual_steady: float | None = None):
+        """The steady loop of NSSolve without its result files (cycas_solve_steady): iterations
+        until ResMax < residual_steady or max_step of them; returns dict(iterations, residual
+        [n,10], resmax [n], ksp_its [n,8], ksp_reason [n,8]).  A failed solve raises as
+        ``iterate`` does, after the iterations that ran are counted."""
+        max_step = self.case.max_step if max_step is None else max_step
+        tol = self.case.residual_steady if residual_steady is None else residual_steady
+        res = np.zeros((max_step, 10)); rm = np.zeros(max_step)
+        its = np.zeros((max_step, 8), dtype=np.int32); rs = np.zeros((max_step, 8), dtype=np.int32)
+        n = C.c_int32(0)
+        rc = capi.load().cycas_solve_steady(self._h, max_step, tol, max_step, C.byref(n), capi.ptr(res),
+                                            capi.ptr(rm), capi.ptr(its), capi.ptr(rs))
+        k = n.value
+        self.step += k
+        capi.check(rc)
+        return {"iterations": k, "residual": res[:k], "resmax": rm[:k], "ksp_its": its[:k], "ksp_reason": rs[:k]}
+
+    def save_restart_point(self) -> None:
+        """Keeps a device copy of the whole state (cycas_restart_point SAVE)."""
+        capi.check(capi.load().cycas_restart_point(self._h, 0))
+
+    def restore_restart_point(self) -> None:
+        """Returns to the state of the last save_restart_point (device-to-device copies)."""
+        capi.check(capi.load().cycas_restart_point(self._h, 1))
+
     # ---- DataPartition::solve* (MPIStructure.h:224-228) on the last assembled systems; the
     # arrays are solved in place, as the reference writes into the caller's arrays
     def _solved(self, rc, st, name):

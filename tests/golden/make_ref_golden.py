@@ -1,0 +1,119 @@
+"""Regenerates the fixtures of this directory that come from the reference's own code.
+
+``oracle/refpin`` builds the reference's unmodified solver sources (NS/*.cpp, read where they lie)
+against a single-rank stand-in for MPI, PETSc, METIS and CGNS whose Krylov solves are the
+oracle's (see oracle/refpin/include/petscksp.h).  ``oracle/_ref/cycas_ref`` then runs the
+reference's own start-up sequence and NSSolve on a case and writes what it built and computed.
+This script runs it on the committed case inputs and stores, per case and preconditioner,
+``ref_<pc>.npz``:
+
+* the integer topology and geometry the reference built (CreateFaces / CellFaceInfo);
+* the residual vector NSSolve reduced in every outer iteration (navier.cpp:94);
+* every Krylov solve's iteration count and converged reason;
+* the fields after the run (for ``cavity20`` only u, v, w and p, besides the residual history
+  and the Krylov log).
+
+The cases are those of make_golden.py (run for ``golden_steps`` iterations or time steps) plus
+``cavity20``, the plain-method cavity (20^3 hexahedra, Re 100) for its configured 200 iterations
+with GMRES(30) rtol 1e-8 on every system (-ksp_type gmres -ksp_rtol 1e-8), as the configuration
+runs the reference.  Preconditioners: ``ilu`` (PETSc's default, ILU(0)) and ``jacobi``.
+
+Needs the reference tree (REF, default /root/reference) and g++.  Run from the repository root:
+    python tests/golden/make_ref_golden.py
+"""
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+REF = os.environ.get("REF", "/root/reference")
+BINARY = os.path.join(ROOT, "oracle", "_ref", "cycas_ref")
+
+# name -> (golden steps, extra reference options)
+RUNS = {
+    "cavity5j": (8, []),
+    "channel_tiny": (6, []),
+    "cavity5g_dual": (3, []),
+    "channel_tiny_tr": (3, []),
+    "cavity20": (200, ["-ksp_type", "gmres", "-ksp_rtol", "1e-8"]),
+}
+GEOMETRY_INT = ["face_cell1", "face_cell2", "face_bnd", "face_vertices", "cell_nface", "cell_rid", "cell_face",
+                "cell_cell", "cell_vertices", "cell_globalidx", "bnd_face", "bnd_rid", "bnd_vertices"]
+GEOMETRY = ["face_x", "face_n", "face_xpac", "face_xnac", "face_area", "face_lambda", "face_rlencos", "cell_vol",
+            "cell_x", "bnd_distance", "vert"]
+FIELDS = ["U", "V", "W", "P", "R", "T", "VisTur", "RUFace", "deltaP", "Apr", "TE", "ED"]
+
+
+def build():
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "refpin"), "REF=" + REF], check=True)
+    return BINARY
+
+
+def load_outputs(out):
+    d = {}
+    with open(os.path.join(out, "manifest.txt")) as f:
+        for line in f:
+            nm, dt, n = line.split()
+            d[nm] = np.fromfile(os.path.join(out, nm + ".bin"), dtype={"f8": np.float64, "i4": np.int32}[dt])
+    return d
+
+
+def run_reference(case_dir, steps, options=()):
+    """Runs the reference build on a copy of case_dir; returns its outputs as arrays."""
+    with tempfile.TemporaryDirectory() as tmp:
+        work = os.path.join(tmp, "case")
+        os.makedirs(work)
+        for f in ("case.msh", "param.in"):
+            shutil.copy(os.path.join(case_dir, f), work)
+        out = os.path.join(tmp, "out")
+        os.makedirs(out)
+        r = subprocess.run([BINARY, work, out, "--iters", str(steps), *options], stdin=subprocess.DEVNULL,
+                           stdout=subprocess.PIPE, stderr=subprocess.STDOUT, env=dict(os.environ, TERM="dumb"))
+        if r.returncode != 0:
+            raise RuntimeError(r.stdout.decode(errors="replace")[-3000:])
+        return load_outputs(out)
+
+
+def pack(o, steps, options, geometry=True):
+    keep = {nm: o[nm] for nm in GEOMETRY_INT + GEOMETRY if nm in o} if geometry else {}
+    keep.update({nm: o[nm] for nm in (FIELDS if geometry else ["U", "V", "W", "P"]) if nm in o})
+    keep["residual"] = o["residual"].reshape(-1, 10)
+    keep["ksp"] = o["ksp"].reshape(-1, 4)
+    keep["info"] = o["info"]
+    keep["steps"] = np.array(steps)
+    keep["options"] = np.array(" ".join(options))
+    return keep
+
+
+def write_cavity20(d):
+    """The 20^3 cavity's inputs (uniform mesh, no random numbers: meshgen writes the same bytes
+    every time, so only the fixtures are committed)."""
+    from sysu_cfd_parallel_gb300 import meshgen
+    return os.path.dirname(meshgen.write_case(d, "cavity", n=20, steps=200))
+
+
+def main():
+    build()
+    tmp = tempfile.mkdtemp()
+    os.makedirs(os.path.join(HERE, "cavity20"), exist_ok=True)
+    for name, (steps, opts) in RUNS.items():
+        d = write_cavity20(tmp) if name == "cavity20" else os.path.join(HERE, name)
+        out_dir = os.path.join(HERE, name)
+        for pc in ("ilu", "jacobi"):
+            options = list(opts) + (["-pc_type", "jacobi"] if pc == "jacobi" else [])
+            o = run_reference(d, steps, options)
+            # the long run keeps its residual history, Krylov log and velocity / pressure only
+            np.savez_compressed(os.path.join(out_dir, "ref_%s.npz" % pc),
+                                **pack(o, steps, options, name != "cavity20"))
+            print(name, pc, "iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
+    shutil.rmtree(tmp, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -291,6 +291,7 @@ def guarded(fn, *a, **kw):
 
 
 def measure_mixed_solve(param, local, steps, ref_fields, fp64_ms, fp64_iters):
+    # fp64_ms: the FP64 solve's time per step (ms)
     """The headline solve with mixed-precision GMRES (FP32 Arnoldi cycles in FP64 iterative
     refinement) to the same stop test: time to converged against FP64 and the relative-L2 error of
     every field at convergence against the FP64 solve's."""
@@ -307,7 +308,7 @@ def measure_mixed_solve(param, local, steps, ref_fields, fp64_ms, fp64_iters):
     s.close()
     return {"value": case.ncel * iters / (ms / 1e3), "ms_per_step": ms / steps,
             "iterations_to_converge": last["iterations"], "fp64_iterations_to_converge": fp64_iters,
-            "time_to_converged_speedup_vs_fp64": fp64_ms / ms,
+            "time_to_converged_speedup_vs_fp64": fp64_ms / (ms / steps),
             "krylov": "GMRES systems: FP32 Arnoldi cycles (inner rtol 1e-4) in FP64 iterative refinement",
             "field_rel_l2_vs_fp64_at_convergence": err}
 
@@ -690,12 +691,17 @@ def krylov_fp64_flops(its_row, turb, n, nnz, restart=30, poly=0):
 
 
 def measure_fp_rates():
-    """FP64 / FP32 FMA throughput of this GPU in TFLOP/s (cycas_measure_fp_rates)."""
+    """FP64 / FP32 FMA throughput of this GPU in TFLOP/s, from the bench-only probe library
+    (csrc/rate_probe.cu, built beside libcycasgpu.so but not part of it)."""
     import ctypes as C
-    from sysu_cfd_parallel_gb300 import capi
-    a, b = C.c_double(), C.c_double()
-    capi.check(capi.load().cycas_measure_fp_rates(C.byref(a), C.byref(b)))
-    return a.value, b.value
+    from sysu_cfd_parallel_gb300 import build as b
+    lib = C.CDLL(b.PROBE_LIB)
+    lib.cycas_measure_fp_rates.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    x, y = C.c_double(), C.c_double()
+    rc = lib.cycas_measure_fp_rates(C.byref(x), C.byref(y))
+    if rc != 0:
+        raise RuntimeError("FMA-rate probe failed (%d)" % rc)
+    return x.value, y.value
 
 
 def measured_peak():
@@ -1136,6 +1142,42 @@ def run_channel(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile(args):
+    """Profiling leg (for ncu and per-system timings): `--steps` SIMPLE iterations of a generated
+    case after `--warmup` untimed ones, with the per-system Krylov timing of the library on; prints
+    one JSON line with the Krylov iteration counts and the profile."""
+    from sysu_cfd_parallel_gb300 import capi, meshgen
+    from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
+    d = tempfile.mkdtemp(prefix="cycas_prof_")
+    iters = args.steps + args.warmup
+    if args.kind == "channel":
+        kw = {"jitter": args.jitter, "seed": 2026} if args.jitter > 0 else {}
+        param = meshgen.write_case(d, "channel", nx=args.nx, ny=args.ny, nz=args.nz, steps=iters, **kw)
+    else:
+        kw = {"jitter": args.jitter, "seed": 1000} if args.jitter > 0 else {}
+        param = meshgen.write_case(d, "cavity", n=args.side, steps=iters, **kw)
+    opt = capi.default_options(pc=capi.PC_JACOBI)
+    opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG if args.pressure_pc == "amg" else capi.PC_JACOBI
+    opt.mixed = 1 if args.mixed else 0
+    opt.amg_omega = args.amg_omega
+    opt.amg_gamma = args.amg_gamma
+    gpc = {"jacobi": capi.PC_JACOBI, "poly1": capi.PC_POLY1, "poly2": capi.PC_POLY2, "poly3": capi.PC_POLY3,
+           "poly4": capi.PC_POLY4, "poly5": capi.PC_POLY5}[args.gmres_pc]
+    opt.ksp[capi.SYS_VELOCITY].pc = gpc
+    opt.ksp[capi.SYS_SCALAR].pc = gpc
+    s = NavierStokesSolver(Case(param), opt)
+    if args.warmup:
+        s.iterate(args.warmup)
+    s.set_profiling(True)
+    s.reset_profile()
+    t0 = time.time()
+    r = s.iterate(args.steps)
+    dt = time.time() - t0
+    print(json.dumps({"workload": "profile", "cells": s.case.ncel, "iters": args.steps, "seconds": dt,
+                      "ksp_its": r["ksp_its"].tolist(), "profile": s.profile()}), flush=True)
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1145,7 +1187,8 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=15)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision and batched lines")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "channel", "serve", "precision", "transient"])
+    ap.add_argument("--workload", default="cavity",
+                    choices=["cavity", "channel", "serve", "precision", "transient", "profile"])
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--drain", type=float, default=120.0)
@@ -1157,8 +1200,21 @@ def main():
     ap.add_argument("--mixed", action="store_true")
     ap.add_argument("--serve-seed", type=int, default=5)
     ap.add_argument("--outer-rtol", type=float, default=1e-10, help="precision workload: rtol of every system")
+    # --workload profile: the generated case and its solver options
+    ap.add_argument("--kind", default="cavity", choices=["channel", "cavity"])
+    ap.add_argument("--nx", type=int, default=100)
+    ap.add_argument("--ny", type=int, default=10)
+    ap.add_argument("--nz", type=int, default=10)
+    ap.add_argument("--side", type=int, default=CAVITY_N, help="cavity cells per side")
+    ap.add_argument("--pressure-pc", default="amg", choices=["amg", "jacobi"])
+    ap.add_argument("--gmres-pc", default="poly5", choices=["jacobi", "poly1", "poly2", "poly3", "poly4", "poly5"])
+    ap.add_argument("--amg-omega", type=float, default=0.0, help="AMG smoother weight (0: library default)")
+    ap.add_argument("--amg-gamma", type=int, default=0, help="AMG cycles at the first shared-memory level")
+    ap.add_argument("--jitter", type=float, default=0.0, help="interior node jitter (fraction of h)")
     args = ap.parse_args()
-    if args.workload == "serve":
+    if args.workload == "profile":
+        run_profile(args)
+    elif args.workload == "serve":
         run_serve(args)
     elif args.workload == "precision":
         run_precision(args)

@@ -320,9 +320,6 @@ int cycas_set_graph(cycas_ctx* ctx, int32_t on);
 int cycas_set_profiling(cycas_ctx* ctx, int32_t on);
 int cycas_get_profile(cycas_ctx* ctx, cycas_profile* out);
 int cycas_reset_profile(cycas_ctx* ctx);
-/* FP64 and FP32 FMA throughput of the current device in TFLOP/s (one CTA of 1024 threads per
- * SM, eight independent FMA chains per thread); the bench's FP64 ceiling. */
-int cycas_measure_fp_rates(double* fp64_tflops, double* fp32_tflops);
 /* Sizes of the pressure AMG hierarchy (0 levels unless CYCAS_PC_AMG is in use): *nlev levels,
  * rows[l] and stored entries nnz[l] for the first max_levels of them, fine to coarse. */
 int cycas_get_amg_levels(cycas_ctx* ctx, int32_t max_levels, int32_t* nlev, int32_t* rows, int32_t* nnz);
@@ -463,8 +460,12 @@ int cycas_server_stats(cycas_server* s, double* out);
  * other than NONE/JACOBI and Krylov types other than DEFAULT/GMRES.  Work is issued on
  * `stream` (a cudaStream_t; NULL = the legacy default stream) and the call returns after the
  * stream has finished it.  The first call on a device looks the array's address up with that
- * device current: make it before any stream capture.  All calls on a device share the array:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * device current, and under lazy module loading (CUDA's default) that lookup is also what loads
+ * the library's device code and places the static array -- the one device allocation and
+ * synchronisation this entry point makes, once per device and process.  So make one warm-up call
+ * per device at start-up (n = 1 will do), before any stream capture and before the phase that
+ * must not allocate.  All calls on a device share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
 int cycas_csr_solve_noalloc(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
                             const double* b, double* x, const cycas_ksp_options* ksp, double rtol, int32_t maxit,
                             int32_t guess_zero, void* stream, cycas_solve_stats* stats);

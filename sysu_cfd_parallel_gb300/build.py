@@ -38,8 +38,11 @@ UNITS = [
     ("noalloc.cu", "nvcc", []),
     ("server.cpp", "cxx", []),
     ("result_io.cpp", "cxx", ["-ffp-contract=off"]),
-    ("rate_probe.cu", "nvcc", []),
 ]
+# bench-only: the FP64/FP32 FMA-rate probe bench.py uses for the FP64 roofline of the channel
+# workload, built as its own library so that the product library does not carry it
+PROBE_SRC = "rate_probe.cu"
+PROBE_LIB = os.path.join(BUILD, "libcycas_rate_probe.so")
 
 
 def _cuda_home() -> str:
@@ -55,7 +58,7 @@ def _cuda_home() -> str:
 
 def _sources_digest() -> str:
     h = hashlib.sha256()
-    for name in sorted(os.listdir(CSRC)):
+    for name in sorted(os.listdir(CSRC)):  # the product units and the bench-only probe
         with open(os.path.join(CSRC, name), "rb") as f:
             h.update(name.encode())
             h.update(f.read())
@@ -100,6 +103,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
+    probe = [NVCC, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", os.path.join(CSRC, PROBE_SRC), "-o",
+             PROBE_LIB]
+    r = subprocess.run(probe, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("rate probe build failed:\n" + r.stdout.decode(errors="replace"))
     with open(stamp, "w") as f:
         f.write(digest)
     return LIB

@@ -97,7 +97,7 @@ EXPORTS = (
     "cycas_batch_copy_case", "cycas_batch_case_field", "cycas_server_create", "cycas_server_destroy",
     "cycas_server_clock", "cycas_server_submit", "cycas_server_step", "cycas_server_poll",
     "cycas_server_result_field", "cycas_server_last_error", "cycas_server_stats", "cycas_footprint_estimate",
-    "cycas_measure_fp_rates", "cycas_set_graph", "cycas_batch_autotune",
+    "cycas_set_graph", "cycas_batch_autotune",
 )
 
 _lib = None
@@ -187,7 +187,6 @@ def load(build_if_missing: bool = True):
     L.cycas_server_step.argtypes = [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.cycas_server_poll.argtypes = [_P, C.POINTER(RequestResult), C.c_int32, C.POINTER(C.c_int32)]
     L.cycas_server_result_field.argtypes = [_P, C.c_int64, C.c_char_p, _P, C.c_int64]
-    L.cycas_measure_fp_rates.argtypes = [_F64P, _F64P]
     L.cycas_set_graph.argtypes = [_P, C.c_int32]
     L.cycas_batch_autotune.argtypes = [_P, C.c_int32, C.POINTER(C.c_int32), _F64P, _F64P]
     L.cycas_footprint_estimate.argtypes = [_P]

@@ -24,8 +24,10 @@
 // Synchronisation is the cost on a 152-SM grid, so each level above the tail takes one grid
 // barrier down (smoothing and restriction fused per coarse row block: x_l is recomputed from
 // r_l where it is needed instead of stored) and one up; the coarsest levels (the "tail",
-// chosen so that their matrices fit in shared memory) are loaded into CTA 0's shared memory
-// once per solve and cycled there with block barriers only.  CG itself is the
+// chosen so that their matrices, with 16-bit columns, fit in shared memory) are loaded into
+// every CTA's shared memory once per solve and cycled there by every CTA at once, with block
+// barriers only: each CTA then holds the whole coarse correction, so the first prolongation
+// follows the tail without a grid barrier and no CTA waits while another works alone.  CG itself is the
 // Chronopoulos-Gear form: w = A u and the inner products (r,u), (w,u), (u,u), (u,s) come out
 // of one pass and one grid reduction, and p, s = A p, x, r are updated locally, so an
 // iteration costs two grid barriers plus the V-cycle's.
@@ -174,11 +176,16 @@ __device__ __forceinline__ T* at(unsigned char* sb, int off) {
   return reinterpret_cast<T*>(sb + off);
 }
 
-// rank 0 of a team: the tail levels of its case (matrices, transfer lists, the coarsest
-// inverse) into shared memory; level 0 is renumbered from the system's rows to the case's
+// every member of a team: the tail levels of its case (matrices with 16-bit columns, transfer
+// lists, the coarsest inverse) into its own shared memory; level 0 is renumbered from the
+// system's rows to the case's
 template <class T>
 __device__ __forceinline__ void copy_in(T* dst, const T* src, int cnt, T shift = T(0)) {
   for (int i = threadIdx.x; i < cnt; i += kGmThreads) dst[i] = src[i] - shift;
+}
+// columns of a tail level: local indices below 65536 (tail_layout checks), stored in 16 bits
+__device__ __forceinline__ void copy_cols(unsigned short* dst, const int* src, int cnt, int shift) {
+  for (int i = threadIdx.x; i < cnt; i += kGmThreads) dst[i] = (unsigned short)(src[i] - shift);
 }
 __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, const float* coarse_inv, int lo,
                           unsigned char* sb) {
@@ -187,10 +194,17 @@ __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, c
     const TailLevelOff& o = T.lv[l];
     const int row0 = l == 0 ? lo : 0;
     if (l + 1 < nlev) {
+      // the matrix in SELL-32 layout; values gathered from the level's CSR values (level 0:
+      // the case's entries start at the system's row pointer of its first row)
       const int k0 = l == 0 ? __ldg(F.rowptr + lo) : 0;
-      copy_in(at<int>(sb, o.rowptr), F.rowptr + row0, F.n + 1, k0);
-      copy_in(at<int>(sb, o.col), F.col + k0, F.nnz, row0);
-      copy_in(at<float>(sb, o.val), (const float*)F.val + k0, F.nnz);
+      const int ns = (F.n + 31) / 32;
+      copy_in(at<int>(sb, o.rowptr), F.sell_ptr, ns + 1);
+      copy_in(at<unsigned short>(sb, o.col), F.sell_col, F.sell_len);
+      float* va = at<float>(sb, o.val);
+      for (int e = threadIdx.x; e < F.sell_len; e += kGmThreads) {
+        const int src = __ldg(F.sell_src + e);
+        va[e] = src >= 0 ? F.val[k0 + src] : 0.0f;
+      }
       copy_in(at<float>(sb, o.wdinv), (const float*)F.wdinv + row0, F.n);
       copy_in(at<int>(sb, o.agg), F.agg + row0, F.n);
       copy_in(at<int>(sb, o.ptptr), F.ptptr, L[l + 1].n + 1);
@@ -202,26 +216,29 @@ __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, c
   __syncthreads();
 }
 
-// Tail levels in shared memory, cycled by rank 0 of a team.  Per level l: R (residual in),
+// Tail levels in shared memory, cycled by every member of a team.  Per level l: R (residual in),
 // X (correction out), T (scratch); R_l is read-only while a cycle runs through level l.
 
-// sum over the shared-memory CSR row i of va[k] * f(cl[k]) in column order; the loads of up to
-// eight entries are issued together, so a row costs a few shared-memory round trips rather
-// than two per entry
+// sum over row i of a shared-memory SELL-32 matrix (slice offsets sp, columns cl, values va)
+// of va * f(column), in the row's CSR order followed by its zero padding.  The rows of a warp
+// are 32 consecutive rows of one slice, so every load of a column or value is one
+// conflict-free shared-memory access; the loads of up to eight entries are issued together.
 template <class F>
-__device__ __forceinline__ float smem_row(const int* rp, const int* cl, const float* va, int i, F f) {
-  const int k0 = rp[i], k1 = rp[i + 1];
+__device__ __forceinline__ float sell_row(const int* sp, const unsigned short* cl, const float* va, int i, F f) {
+  const int sl = i >> 5;
+  const int b0 = sp[sl] + (i & 31), w = (sp[sl + 1] - sp[sl]) >> 5;
   float s = 0.0f;
-  for (int b = k0; b < k1; b += 8) {
+  for (int k0 = 0; k0 < w; k0 += 8) {
     int c[8];
     float v[8], x[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-      c[q] = b + q < k1 ? cl[b + q] : 0;
-      v[q] = b + q < k1 ? va[b + q] : 0.0f;
+      const bool ok = k0 + q < w;
+      c[q] = ok ? (int)cl[b0 + 32 * (k0 + q)] : 0;
+      v[q] = ok ? va[b0 + 32 * (k0 + q)] : 0.0f;
     }
 #pragma unroll
-    for (int q = 0; q < 8; q++) x[q] = b + q < k1 ? f(c[q]) : 0.0f;
+    for (int q = 0; q < 8; q++) x[q] = k0 + q < w ? f(c[q]) : 0.0f;
 #pragma unroll
     for (int q = 0; q < 8; q++) s += v[q] * x[q];
   }
@@ -235,7 +252,7 @@ __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned ch
   const TailLevelOff& o = T.lv[l];
   const int n = L[l].n, nc = L[l + 1].n;
   const int* rp = at<int>(sb, o.rowptr);
-  const int* cl = at<int>(sb, o.col);
+  const unsigned short* cl = at<unsigned short>(sb, o.col);
   const float* va = at<float>(sb, o.val);
   const float* wd = at<float>(sb, o.wdinv);
   const float* R = at<float>(sb, o.R);
@@ -244,7 +261,7 @@ __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned ch
   for (int i = tid; i < n; i += kGmThreads) {
     const float ri = R[i];
     X[i] = wd[i] * ri;
-    Tt[i] = ri - smem_row(rp, cl, va, i, [&](int j) { return wd[j] * R[j]; });
+    Tt[i] = ri - sell_row(rp, cl, va, i, [&](int j) { return wd[j] * R[j]; });
   }
   __syncthreads();
   const int* pp = at<int>(sb, o.ptptr);
@@ -288,7 +305,7 @@ __device__ void tail_up(const AmgDevLevel* L, const TailLayout& T, float alpha, 
   const TailLevelOff& o = T.lv[l];
   const int n = L[l].n;
   const int* rp = at<int>(sb, o.rowptr);
-  const int* cl = at<int>(sb, o.col);
+  const unsigned short* cl = at<unsigned short>(sb, o.col);
   const float* va = at<float>(sb, o.val);
   const float* wd = at<float>(sb, o.wdinv);
   const int* ag = at<int>(sb, o.agg);
@@ -299,7 +316,7 @@ __device__ void tail_up(const AmgDevLevel* L, const TailLayout& T, float alpha, 
   for (int i = tid; i < n; i += kGmThreads) Y[i] = X[i] + alpha * Xc[ag[i]];
   __syncthreads();
   for (int i = tid; i < n; i += kGmThreads) {
-    const float acc = smem_row(rp, cl, va, i, [&](int j) { return Y[j]; });
+    const float acc = sell_row(rp, cl, va, i, [&](int j) { return Y[j]; });
     X[i] = Y[i] + wd[i] * (R[i] - acc);
   }
   __syncthreads();
@@ -312,15 +329,17 @@ __device__ void tail_v(const AmgDevLevel* L, int nlev, const TailLayout& T, floa
   for (int l = nlev - 2; l >= s; l--) tail_up(L, T, alpha, sb, l);
 }
 
-// rank 0 of a team: the cycle from level T.tail down, in shared memory.  Its input residual
-// is the tail level's r, its correction goes to the tail level's t (or, when the tail is the
-// whole hierarchy, to rows [lo, hi) of the FP64 vector z).  The first coarse level of the tail
-// (g = max(tail, 1)) is solved by gamma cycles, x <- x + V(r_g - A_g x) (a W-cycle for
-// gamma 2): the tail levels are cheap, with no grid barrier, and a more accurate coarse
-// correction cuts the outer CG iterations.  `buf` holds the accumulated x and the original
-// r_g (2 n_g floats).
+// every member of a team: the cycle from level T.tail down, in its own shared memory (the
+// members compute the same values in the same order, so each holds the whole coarse correction
+// and the prolongation below needs no barrier).  The input residual is the tail level's r; the
+// correction stays in shared memory (X of the tail level) or, when the tail is the whole
+// hierarchy, the member's share of rows [lo, hi) goes to the FP64 vector z.  The first coarse
+// level of the tail (g = max(tail, 1)) is solved by gamma cycles, x <- x + V(r_g - A_g x) (a
+// W-cycle for gamma 2): the tail levels are cheap, with no grid barrier, and a more accurate
+// coarse correction cuts the outer CG iterations.  `buf` holds the accumulated x and the
+// original r_g (2 n_g floats).
 __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma,
-                           unsigned char* sb, float* buf, int lo, double* z) {
+                                        unsigned char* sb, float* buf, int r0, int r1, int lo, double* z) {
   const int tid = threadIdx.x;
   const int t0 = T.tail;
   {
@@ -335,7 +354,7 @@ __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const Ta
     const TailLevelOff& o = T.lv[g];
     const int n = L[g].n;
     const int* rp = at<int>(sb, o.rowptr);
-    const int* cl = at<int>(sb, o.col);
+    const unsigned short* cl = at<unsigned short>(sb, o.col);
     const float* va = at<float>(sb, o.val);
     float* R = at<float>(sb, o.R);
     float* X = at<float>(sb, o.X);
@@ -348,7 +367,7 @@ __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const Ta
         if (rep == 1) Q[i] = R[i];
       }
       __syncthreads();
-      for (int i = tid; i < n; i += kGmThreads) R[i] = Q[i] - smem_row(rp, cl, va, i, [&](int j) { return S[j]; });
+      for (int i = tid; i < n; i += kGmThreads) R[i] = Q[i] - sell_row(rp, cl, va, i, [&](int j) { return S[j]; });
       __syncthreads();
       tail_v(L, nlev, T, alpha, sb, g);
     }
@@ -358,14 +377,9 @@ __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const Ta
   } else {
     tail_v(L, nlev, T, alpha, sb, t0);
   }
-  {
-    const float* X = at<float>(sb, T.lv[t0].X);
-    if (t0 == 0) {
-      for (int i = tid; i < L[0].n; i += kGmThreads) z[lo + i] = (double)X[i];
-    } else {
-      float* out = L[t0].t;
-      for (int i = tid; i < L[t0].n; i += kGmThreads) out[i] = X[i];
-    }
+  if (t0 == 0) {
+    const float* X = at<float>(sb, T.lv[0].X);
+    for (int r = r0 + tid; r < r1; r += kGmThreads) z[r] = (double)X[r - lo];
   }
 }
 
@@ -399,8 +413,10 @@ __device__ __forceinline__ void grid_down(const AmgDevLevel& F, const AmgDevLeve
 }
 
 // prolongation of the coarse correction and post-smoothing on rows rw of a level:
-// out = y + w D^-1 (r - A y),  y = w D^-1 r + a P x_C; level 0 writes the FP64 z
-__device__ __forceinline__ void grid_up(const AmgDevLevel& F, const float* xc, float alpha, Rows rw, float* outf,
+// out = y + w D^-1 (r - A y),  y = w D^-1 r + a P x_C; level 0 writes the FP64 z.  xc(I) reads
+// the coarse correction of coarse row I (from global memory, or from the tail in shared memory)
+template <class XC>
+__device__ __forceinline__ void grid_up(const AmgDevLevel& F, XC xc, float alpha, Rows rw, float* outf,
                                         double* outd) {
   const float* rl = F.r;
   const float* wd = F.wdinv;
@@ -408,9 +424,9 @@ __device__ __forceinline__ void grid_up(const AmgDevLevel& F, const float* xc, f
   for (int i = rw.r0 + threadIdx.x; i < rw.r1; i += kGmThreads) {
     const float ri = ldcgf(rl + i);
     const float wi = __ldg(wd + i);
-    const float y = wi * ri + alpha * ldcgf(xc + __ldg(agg + i));
+    const float y = wi * ri + alpha * xc(__ldg(agg + i));
     float acc = row_gather_f<8>(F.rowptr, F.col, F.val, i, [&](int j) {
-      return __ldg(wd + j) * ldcgf(rl + j) + alpha * ldcgf(xc + __ldg(agg + j));
+      return __ldg(wd + j) * ldcgf(rl + j) + alpha * xc(__ldg(agg + j));
     });
     const float o = y + wi * (ri - acc);
     if (outd) outd[i] = (double)o;
@@ -419,7 +435,8 @@ __device__ __forceinline__ void grid_up(const AmgDevLevel& F, const float* xc, f
 }
 
 // z = M r for the case's rows [lo, hi) of the residual held in L[0].r; false after a barrier
-// timeout
+// timeout.  Barriers: one per grid level down, none between the tail and the first level up
+// (every member holds the tail's correction), one per grid level up.
 __device__ bool vcycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma, unsigned char* sb,
                        float* buf, int lo, int hi, double* z, const Team& Tm, int* err) {
   const int t0 = T.tail;
@@ -427,11 +444,20 @@ __device__ bool vcycle(const AmgDevLevel* L, int nlev, const TailLayout& T, floa
     grid_down(L[l], L[l + 1], Tm, buf);
     if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   }
-  if (Tm.rank == 0) tail_cycle(L, nlev, T, alpha, gamma, sb, buf, lo, z);
-  if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
+  const Rows own = share(lo, hi, Tm);
+  tail_cycle(L, nlev, T, alpha, gamma, sb, buf, own.r0, own.r1, lo, z);
+  if (t0 == 0) return grid_barrier(Tm.bar, Tm.size, err);
+  const float* Xs = at<float>(sb, T.lv[t0].X);
   for (int l = t0 - 1; l >= 0; l--) {
-    const Rows rw = l == 0 ? share(lo, hi, Tm) : share(0, L[l].n, Tm);
-    grid_up(L[l], L[l + 1].t, alpha, rw, l == 0 ? nullptr : L[l].t, l == 0 ? z : nullptr);
+    const Rows rw = l == 0 ? own : share(0, L[l].n, Tm);
+    float* outf = l == 0 ? nullptr : L[l].t;
+    double* outd = l == 0 ? z : nullptr;
+    if (l == t0 - 1) {
+      grid_up(L[l], [&](int I) { return Xs[I]; }, alpha, rw, outf, outd);
+    } else {
+      const float* xc = L[l + 1].t;
+      grid_up(L[l], [&](int I) { return ldcgf(xc + I); }, alpha, rw, outf, outd);
+    }
     if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   }
   return true;
@@ -464,7 +490,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
   __syncthreads();
   unsigned char* sb = s_dyn;
   float* buf = reinterpret_cast<float*>(s_dyn + s_tl.bytes);
-  if (Tm.rank == 0) tail_load(s_lv, nlev, s_tl, cd->coarse_inv, lo, sb);
+  tail_load(s_lv, nlev, s_tl, cd->coarse_inv, lo, sb);
   const Rows own = share(lo, hi, Tm);
   const int stride = kPartStride;
   double* mypart = Tm.part + (long)Tm.rank * stride;

@@ -147,18 +147,57 @@ namespace {
 
 int align16(long b) { return (int)((b + 15) / 16 * 16); }
 
-// tail = the shortest suffix of levels ending at the coarsest whose arrays fit the budget
-TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz) {
+// SELL-32 copy of a level's pattern (AmgDevLevel::sell_*)
+struct Sell {
+  std::vector<int> ptr, src;
+  std::vector<unsigned short> col;
+};
+Sell sell32(const AmgHostLevel& L) {
+  Sell S;
+  const int ns = (L.n + 31) / 32;
+  S.ptr.assign(ns + 1, 0);
+  for (int s = 0; s < ns; s++) {
+    int w = 0;
+    for (int i = 32 * s; i < std::min(L.n, 32 * s + 32); i++) w = std::max(w, L.rowptr[i + 1] - L.rowptr[i]);
+    S.ptr[s + 1] = S.ptr[s] + 32 * w;
+  }
+  S.col.assign(S.ptr[ns], 0);
+  S.src.assign(S.ptr[ns], -1);
+  for (int s = 0; s < ns; s++) {
+    const int w = (S.ptr[s + 1] - S.ptr[s]) / 32;
+    for (int lane = 0; lane < 32; lane++) {
+      const int i = 32 * s + lane;
+      if (i >= L.n) continue;
+      const int len = L.rowptr[i + 1] - L.rowptr[i];
+      for (int k = 0; k < w; k++) {
+        const int e = S.ptr[s] + 32 * k + lane;
+        if (k < len) {
+          S.col[e] = (unsigned short)L.col[L.rowptr[i] + k];
+          S.src[e] = L.rowptr[i] + k;
+        } else {
+          S.col[e] = (unsigned short)i;  // padding: the row's own column, value 0
+        }
+      }
+    }
+  }
+  return S;
+}
+
+// tail = the shortest suffix of levels ending at the coarsest whose arrays fit the budget;
+// columns are stored in 16 bits, so a tail level has fewer than 65536 rows.  sell[l]: entries of
+// level l's SELL-32 layout
+TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz, const std::vector<int>& sell) {
   TailLayout T{};
   const int L = (int)n.size();
   auto level_bytes = [&](int l) -> long {
     if (l == L - 1) return align16(4L * n[l] * n[l]) + 2L * align16(4L * n[l]);
-    return align16(4L * (n[l] + 1)) + 2L * align16(4L * nnz[l]) + align16(4L * n[l]) + align16(4L * n[l]) +
-           align16(4L * (n[l + 1] + 1)) + align16(4L * n[l]) + 3L * align16(4L * n[l]);
+    const long ns = (n[l] + 31) / 32;
+    return align16(4L * (ns + 1)) + align16(2L * sell[l]) + align16(4L * sell[l]) + align16(4L * n[l]) +
+           align16(4L * n[l]) + align16(4L * (n[l + 1] + 1)) + align16(4L * n[l]) + 3L * align16(4L * n[l]);
   };
   long total = level_bytes(L - 1);
   int t = L - 1;
-  while (t > 0 && total + level_bytes(t - 1) <= kAmgTailBudget) total += level_bytes(--t);
+  while (t > 0 && n[t - 1] < 65536 && total + level_bytes(t - 1) <= kAmgTailBudget) total += level_bytes(--t);
   T.tail = t;
   int off = 0;
   auto take = [&](long b) {
@@ -170,9 +209,9 @@ TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz) {
   for (int l = t; l < L; l++) {
     TailLevelOff& o = T.lv[l];
     if (l + 1 < L) {
-      o.rowptr = take(4L * (n[l] + 1));
-      o.col = take(4L * nnz[l]);
-      o.val = take(4L * nnz[l]);
+      o.rowptr = take(4L * ((n[l] + 31) / 32 + 1));
+      o.col = take(2L * sell[l]);
+      o.val = take(4L * sell[l]);
       o.wdinv = take(4L * n[l]);
       o.agg = take(4L * n[l]);
       o.ptptr = take(4L * (n[l + 1] + 1));
@@ -362,18 +401,35 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
   v.coarse_inv = up.alloc_float(std::max(1L, ninv));
   int tail_max = 0;
   for (int c = 0; c < nc; c++) {
-    std::vector<int> ln, lz;
+    std::vector<int> ln, lz, ls;
+    std::vector<Sell> sells;
     for (const AmgHostLevel& L : H(c).lv) {
       ln.push_back(L.n);
       lz.push_back(L.nnz);
+      // the SELL copy only matters for levels small enough to be in the tail
+      sells.push_back(L.n < 65536 ? sell32(L) : Sell{});
+      ls.push_back(L.n < 65536 ? (int)sells.back().col.size() : L.nnz);
     }
     AmgCaseDesc& cd = v.cases[c];
     cd.lo = lo[c];
     cd.hi = hi[c];
     cd.nlev = (int)H(c).lv.size();
     cd.coarse_inv = v.coarse_inv + inv_off[c];
+    cd.tl = tail_layout(ln, lz, ls);
+    for (int l = 0; l < cd.nlev; l++) {
+      AmgDevLevel& e = v.levels[c][l];
+      e.sell_ptr = nullptr;
+      e.sell_col = nullptr;
+      e.sell_src = nullptr;
+      e.sell_len = 0;
+      if (l < cd.tl.tail || l + 1 >= cd.nlev) continue;
+      const Sell& S = sells[l];
+      e.sell_ptr = up.upload_int(S.ptr.data(), (long)S.ptr.size());
+      e.sell_col = (const unsigned short*)up.upload_bytes(S.col.data(), 2L * (long)S.col.size());
+      e.sell_src = up.upload_int(S.src.data(), (long)S.src.size());
+      e.sell_len = (int)S.col.size();
+    }
     cd.levels = (const AmgDevLevel*)up.upload_bytes(v.levels[c].data(), sizeof(AmgDevLevel) * cd.nlev);
-    cd.tl = tail_layout(ln, lz);
     cd.gamma = v.gamma > 0 ? v.gamma : (hi[c] - lo[c] >= kAmgWRows ? 2 : 1);
     tail_max = std::max(tail_max, cd.tl.bytes);
     if (c == 0) {

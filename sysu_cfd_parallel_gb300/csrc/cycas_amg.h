@@ -17,11 +17,13 @@ namespace cycas {
 constexpr int kAmgMaxLevels = 12;
 constexpr int kAmgCoarseMax = 64;            // the coarsest level is inverted densely by one CTA
 constexpr int kAmgDownBuf = 8192;            // floats of the per-CTA restriction buffer
-constexpr int kAmgTailBudget = 160 * 1024;   // shared-memory bytes for a case's tail levels
+// shared-memory bytes for a case's tail levels: with the restriction buffer and the kernel's
+// static shared memory this stays within the 227 KB a CTA can have
+constexpr int kAmgTailBudget = 188 * 1024;
 // Cases with at least this many pressure rows solve the tail's first level by two cycles (a
-// W-cycle there).  The second cycle runs on one CTA, a fixed cost per CG iteration that the
-// saved iterations repay only on large cases: measured on GB300 per 10 SIMPLE iterations,
-// 480k-tet channel -7.5 %, 104k -4 %, 60k +8 %, 4k-cell cavity +5 %.
+// W-cycle there).  The second cycle is a fixed cost per CG iteration (in shared memory, no grid
+// barrier) that the saved iterations repay only on large cases: measured on GB300 per 10 SIMPLE
+// iterations, 480k-tet channel -7.5 %, 104k -4 %, 60k +8 %, 4k-cell cavity +5 %.
 constexpr int kAmgWRows = 80000;
 
 struct AmgHostLevel {
@@ -54,14 +56,24 @@ struct AmgDevLevel {
   const int* ptrow;   // rows of each aggregate (level 0: global rows)
   float* r;           // residual (level 0: FP32 copy of the CG residual, global rows)
   float* t;           // correction returned to the finer level (levels >= 1)
+  // levels of the shared-memory tail (else null): the pattern in SELL-32 layout -- rows in
+  // slices of 32, a slice column-major and padded to its longest row, so the 32 lanes of a warp
+  // read entry k of 32 consecutive rows from consecutive addresses (no bank conflicts).  Padding
+  // entries have the row's own column and take the value 0; the real entries keep the CSR
+  // order, so a row sums in the same order as in CSR.
+  const int* sell_ptr;             // [ceil(n/32)+1] first entry of each slice
+  const unsigned short* sell_col;  // [sell_len] local columns
+  const int* sell_src;             // [sell_len] the entry's position in this level's CSR values, -1 for padding
+  int sell_len;
 };
 
-// byte offsets of one tail level's arrays in dynamic shared memory
+// byte offsets of one tail level's arrays in dynamic shared memory: rowptr/col/val hold the
+// SELL-32 slice offsets, 16-bit columns and values of the level's matrix
 struct TailLevelOff {
   int rowptr, col, val, wdinv, agg, ptptr, ptrow, R, X, T;
 };
 
-// the coarsest levels of a case, cycled by one CTA out of shared memory
+// the coarsest levels of a case, cycled out of shared memory by every CTA that solves the case
 struct TailLayout {
   int tail;   // first level of the tail (levels tail..nlev-1)
   int bytes;  // dynamic shared memory taken by the tail (multiple of 16)

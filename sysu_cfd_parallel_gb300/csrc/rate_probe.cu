@@ -1,4 +1,5 @@
-// Measurement hook: the FP64 and FP32 FMA throughput of the current device.
+// Bench-only measurement probe (built as libcycas_rate_probe.so, not part of libcycasgpu.so):
+// the FP64 and FP32 FMA throughput of the current device.
 //
 // The SIMPLE path's FP64 loops are bounded by the FP64 issue rate on GB300 (a small fraction of
 // the FP32 rate), so the bench reports their arithmetic against this measured peak beside the

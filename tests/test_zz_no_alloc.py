@@ -1,14 +1,18 @@
-"""cycas_csr_solve_noalloc (device buffers, static scratch) against cycas_csr_solve.
+"""cycas_csr_solve_noalloc (device buffers, static scratch) against cycas_csr_solve and the oracle.
 
-Both run the same persistent GMRES kernel; the no-allocation entry point only takes its
-scratch from a static device array instead of cudaMalloc.  Collected last so that it also
-runs after every other GPU test has used the device.
+Both library entry points run the same persistent GMRES kernel; the no-allocation one only
+takes its scratch from a static device array instead of cudaMalloc.  Its results are compared
+with the allocating entry point and with the oracle's restatement of PETSc's GMRES, and its
+no-allocation property is checked directly: after the warm-up call, further calls leave the
+device's free memory unchanged.  Collected last so that it also runs after every other GPU test
+has used the device.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
+import pyoracle as po
 from sysu_cfd_parallel_gb300 import capi
 from sysu_cfd_parallel_gb300.solver import csr_solve
 
@@ -67,6 +71,42 @@ def test_noalloc_matches_allocating_solve_on_consecutive_calls(pc):
         assert st.reason > 0 and reason_r > 0
         assert abs(st.its - its_r) <= 1, (st.its, its_r)
         assert _rel_l2(x, xr) < 1e-12
+        # the oracle's GMRES(m): classical Gram-Schmidt, left preconditioning, PETSc's test
+        xo, its_o, reason_o, _ = po.csr_solve(rowptr, col, val, b, pc={capi.PC_JACOBI: po.PC_JACOBI,
+                                                                        capi.PC_NONE: po.PC_NONE}[pc],
+                                              restart=restart, rtol=1e-10)
+        assert reason_o > 0 and abs(st.its - its_o) <= 1, (st.its, its_o)
+        assert _rel_l2(x, xo) < 1e-12
+
+
+def test_noalloc_allocates_nothing_after_warm_up():
+    """After one warm-up call (which may load the module and place the static array), solves of
+    the largest size leave cudaMemGetInfo's free bytes unchanged."""
+    import torch
+
+    rowptr, col, val, b = _banded(MAX_ROWS, 6)
+    dev = torch.device("cuda:0")
+    bufs = [torch.from_numpy(a).to(dev) for a in (rowptr, col, val, b)]
+    x = torch.zeros(b.size, dtype=torch.float64, device=dev)
+    k = capi.KspOptions(type=capi.KSP_GMRES, restart=30, pc=capi.PC_JACOBI, rtol=0.0, maxit=0)
+    st = capi.SolveStats()
+    lib = capi.load()
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def call():
+        x.zero_()
+        return lib.cycas_csr_solve_noalloc(b.size, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(),
+                                           bufs[3].data_ptr(), x.data_ptr(), C.byref(k), 1e-10, 1000, 1, stream,
+                                           C.byref(st))
+
+    assert call() == capi.CYCAS_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    for _ in range(3):
+        assert call() == capi.CYCAS_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_initial_guess():

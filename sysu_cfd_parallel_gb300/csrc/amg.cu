@@ -176,6 +176,14 @@ __device__ __forceinline__ T* at(unsigned char* sb, int off) {
   return reinterpret_cast<T*>(sb + off);
 }
 
+// the kernel's dynamic shared memory, named at file scope so that the tail functions (one of
+// them out of line) address it as shared memory rather than through generic pointers
+extern __shared__ __align__(16) unsigned char amg_smem[];
+template <class T>
+__device__ __forceinline__ T* sat(int off) {
+  return reinterpret_cast<T*>(amg_smem + off);
+}
+
 // every member of a team: the tail levels of its case (matrices with 16-bit columns, transfer
 // lists, the coarsest inverse) into its own shared memory; level 0 is renumbered from the
 // system's rows to the case's
@@ -183,10 +191,7 @@ template <class T>
 __device__ __forceinline__ void copy_in(T* dst, const T* src, int cnt, T shift = T(0)) {
   for (int i = threadIdx.x; i < cnt; i += kGmThreads) dst[i] = src[i] - shift;
 }
-// columns of a tail level: local indices below 65536 (tail_layout checks), stored in 16 bits
-__device__ __forceinline__ void copy_cols(unsigned short* dst, const int* src, int cnt, int shift) {
-  for (int i = threadIdx.x; i < cnt; i += kGmThreads) dst[i] = (unsigned short)(src[i] - shift);
-}
+
 __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, const float* coarse_inv, int lo,
                           unsigned char* sb) {
   for (int l = T.tail; l < nlev; l++) {
@@ -198,19 +203,20 @@ __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, c
       // the case's entries start at the system's row pointer of its first row)
       const int k0 = l == 0 ? __ldg(F.rowptr + lo) : 0;
       const int ns = (F.n + 31) / 32;
-      copy_in(at<int>(sb, o.rowptr), F.sell_ptr, ns + 1);
-      copy_in(at<unsigned short>(sb, o.col), F.sell_col, F.sell_len);
-      float* va = at<float>(sb, o.val);
+      copy_in(sat<int>(o.rowptr), F.sell_ptr, ns + 1);
+      copy_in(sat<unsigned short>(o.col), F.sell_col, F.sell_len);
+      copy_in(sat<unsigned short>(o.perm), F.sell_row, 32 * ns);
+      float* va = sat<float>(o.val);
       for (int e = threadIdx.x; e < F.sell_len; e += kGmThreads) {
         const int src = __ldg(F.sell_src + e);
         va[e] = src >= 0 ? F.val[k0 + src] : 0.0f;
       }
-      copy_in(at<float>(sb, o.wdinv), (const float*)F.wdinv + row0, F.n);
-      copy_in(at<int>(sb, o.agg), F.agg + row0, F.n);
-      copy_in(at<int>(sb, o.ptptr), F.ptptr, L[l + 1].n + 1);
-      copy_in(at<int>(sb, o.ptrow), F.ptrow, F.n, row0);
+      copy_in(sat<float>(o.wdinv), (const float*)F.wdinv + row0, F.n);
+      copy_in(sat<int>(o.agg), F.agg + row0, F.n);
+      copy_in(sat<int>(o.ptptr), F.ptptr, L[l + 1].n + 1);
+      copy_in(sat<int>(o.ptrow), F.ptrow, F.n, row0);
     } else {
-      copy_in(at<float>(sb, T.inv), coarse_inv, F.n * F.n);
+      copy_in(sat<float>(T.inv), coarse_inv, F.n * F.n);
     }
   }
   __syncthreads();
@@ -219,14 +225,15 @@ __device__ void tail_load(const AmgDevLevel* L, int nlev, const TailLayout& T, c
 // Tail levels in shared memory, cycled by every member of a team.  Per level l: R (residual in),
 // X (correction out), T (scratch); R_l is read-only while a cycle runs through level l.
 
-// sum over row i of a shared-memory SELL-32 matrix (slice offsets sp, columns cl, values va)
-// of va * f(column), in the row's CSR order followed by its zero padding.  The rows of a warp
-// are 32 consecutive rows of one slice, so every load of a column or value is one
-// conflict-free shared-memory access; the loads of up to eight entries are issued together.
+// sum over the row at SELL-32 position p of a shared-memory matrix (slice offsets sp, columns
+// cl, values va) of va * f(column), in the row's CSR order followed by its zero padding.  The
+// positions of a warp are 32 consecutive positions of one slice, so every load of a column or
+// value is one conflict-free shared-memory access; the loads of up to eight entries are issued
+// together.
 template <class F>
-__device__ __forceinline__ float sell_row(const int* sp, const unsigned short* cl, const float* va, int i, F f) {
-  const int sl = i >> 5;
-  const int b0 = sp[sl] + (i & 31), w = (sp[sl + 1] - sp[sl]) >> 5;
+__device__ __forceinline__ float sell_row(const int* sp, const unsigned short* cl, const float* va, int p, F f) {
+  const int sl = p >> 5;
+  const int b0 = sp[sl] + (p & 31), w = (sp[sl + 1] - sp[sl]) >> 5;
   float s = 0.0f;
   for (int k0 = 0; k0 < w; k0 += 8) {
     int c[8];
@@ -251,22 +258,24 @@ __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned ch
   const int tid = threadIdx.x;
   const TailLevelOff& o = T.lv[l];
   const int n = L[l].n, nc = L[l + 1].n;
-  const int* rp = at<int>(sb, o.rowptr);
-  const unsigned short* cl = at<unsigned short>(sb, o.col);
-  const float* va = at<float>(sb, o.val);
-  const float* wd = at<float>(sb, o.wdinv);
-  const float* R = at<float>(sb, o.R);
-  float* X = at<float>(sb, o.X);
-  float* Tt = at<float>(sb, o.T);
-  for (int i = tid; i < n; i += kGmThreads) {
+  const int* rp = sat<int>(o.rowptr);
+  const unsigned short* cl = sat<unsigned short>(o.col);
+  const float* va = sat<float>(o.val);
+  const float* wd = sat<float>(o.wdinv);
+  const float* R = sat<float>(o.R);
+  float* X = sat<float>(o.X);
+  float* Tt = sat<float>(o.T);
+  const unsigned short* pm = sat<unsigned short>(o.perm);
+  for (int p = tid; p < n; p += kGmThreads) {
+    const int i = pm[p];
     const float ri = R[i];
     X[i] = wd[i] * ri;
-    Tt[i] = ri - sell_row(rp, cl, va, i, [&](int j) { return wd[j] * R[j]; });
+    Tt[i] = ri - sell_row(rp, cl, va, p, [&](int j) { return wd[j] * R[j]; });
   }
   __syncthreads();
-  const int* pp = at<int>(sb, o.ptptr);
-  const int* pr = at<int>(sb, o.ptrow);
-  float* Rn = at<float>(sb, T.lv[l + 1].R);
+  const int* pp = sat<int>(o.ptptr);
+  const int* pr = sat<int>(o.ptrow);
+  float* Rn = sat<float>(T.lv[l + 1].R);
   for (int I = tid; I < nc; I += kGmThreads) {
     const int q0 = pp[I], q1 = pp[I + 1];
     float s = 0.0f;
@@ -286,9 +295,9 @@ __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned ch
 __device__ void tail_coarsest(const AmgDevLevel* L, int nlev, const TailLayout& T, unsigned char* sb) {
   const int tid = threadIdx.x;
   const int n = L[nlev - 1].n;
-  const float* inv = at<float>(sb, T.inv);
-  const float* R = at<float>(sb, T.lv[nlev - 1].R);
-  float* X = at<float>(sb, T.lv[nlev - 1].X);
+  const float* inv = sat<float>(T.inv);
+  const float* R = sat<float>(T.lv[nlev - 1].R);
+  float* X = sat<float>(T.lv[nlev - 1].X);
   const int lane = tid & 31, wid = tid >> 5;
   for (int i = wid; i < n; i += kGmWarps) {
     float s = 0.0f;
@@ -304,19 +313,21 @@ __device__ void tail_up(const AmgDevLevel* L, const TailLayout& T, float alpha, 
   const int tid = threadIdx.x;
   const TailLevelOff& o = T.lv[l];
   const int n = L[l].n;
-  const int* rp = at<int>(sb, o.rowptr);
-  const unsigned short* cl = at<unsigned short>(sb, o.col);
-  const float* va = at<float>(sb, o.val);
-  const float* wd = at<float>(sb, o.wdinv);
-  const int* ag = at<int>(sb, o.agg);
-  const float* R = at<float>(sb, o.R);
-  float* X = at<float>(sb, o.X);
-  float* Y = at<float>(sb, o.T);
-  const float* Xc = at<float>(sb, T.lv[l + 1].X);
+  const int* rp = sat<int>(o.rowptr);
+  const unsigned short* cl = sat<unsigned short>(o.col);
+  const float* va = sat<float>(o.val);
+  const float* wd = sat<float>(o.wdinv);
+  const int* ag = sat<int>(o.agg);
+  const float* R = sat<float>(o.R);
+  float* X = sat<float>(o.X);
+  float* Y = sat<float>(o.T);
+  const float* Xc = sat<float>(T.lv[l + 1].X);
   for (int i = tid; i < n; i += kGmThreads) Y[i] = X[i] + alpha * Xc[ag[i]];
   __syncthreads();
-  for (int i = tid; i < n; i += kGmThreads) {
-    const float acc = sell_row(rp, cl, va, i, [&](int j) { return Y[j]; });
+  const unsigned short* pm = sat<unsigned short>(o.perm);
+  for (int p = tid; p < n; p += kGmThreads) {
+    const int i = pm[p];
+    const float acc = sell_row(rp, cl, va, p, [&](int j) { return Y[j]; });
     X[i] = Y[i] + wd[i] * (R[i] - acc);
   }
   __syncthreads();
@@ -336,30 +347,35 @@ __device__ void tail_v(const AmgDevLevel* L, int nlev, const TailLayout& T, floa
 // hierarchy, the member's share of rows [lo, hi) goes to the FP64 vector z.  The first coarse
 // level of the tail (g = max(tail, 1)) is solved by gamma cycles, x <- x + V(r_g - A_g x) (a
 // W-cycle for gamma 2): the tail levels are cheap, with no grid barrier, and a more accurate
-// coarse correction cuts the outer CG iterations.  `buf` holds the accumulated x and the
-// original r_g (2 n_g floats).
+// coarse correction cuts the outer CG iterations; g moves further down while its level has
+// more than kAmgWLevelRows rows.  `buf` holds the accumulated x and the original r_g (2 n_g
+// floats).
 __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma,
                                         unsigned char* sb, float* buf, int r0, int r1, int lo, double* z) {
   const int tid = threadIdx.x;
   const int t0 = T.tail;
   {
-    float* R = at<float>(sb, T.lv[t0].R);
+    float* R = sat<float>(T.lv[t0].R);
     const float* rin = t0 == 0 ? L[0].r + lo : L[t0].r;
     for (int i = tid; i < L[t0].n; i += kGmThreads) R[i] = ldcgf(rin + i);
   }
   __syncthreads();
-  const int g = t0 > 1 ? t0 : 1;
+  // the W-cycle's level: the first tail level below level 0 small enough for the second cycle
+  // to be cheap (each tail pass runs on one SM's shared memory)
+  int g = t0 > 1 ? t0 : 1;
+  while (g < nlev - 1 && L[g].n > kAmgWLevelRows) g++;
   if (gamma > 1 && g < nlev - 1 && 2 * L[g].n <= kAmgDownBuf) {
     for (int l = t0; l < g; l++) tail_down(L, T, sb, l);
     const TailLevelOff& o = T.lv[g];
     const int n = L[g].n;
-    const int* rp = at<int>(sb, o.rowptr);
-    const unsigned short* cl = at<unsigned short>(sb, o.col);
-    const float* va = at<float>(sb, o.val);
-    float* R = at<float>(sb, o.R);
-    float* X = at<float>(sb, o.X);
-    float* S = buf;      // accumulated correction
-    float* Q = buf + n;  // the level's original residual
+    const int* rp = sat<int>(o.rowptr);
+    const unsigned short* cl = sat<unsigned short>(o.col);
+    const float* va = sat<float>(o.val);
+    float* R = sat<float>(o.R);
+    float* X = sat<float>(o.X);
+    float* S = sat<float>(T.bytes);  // accumulated correction (the restriction buffer)
+    float* Q = S + n;                // the level's original residual
+    const unsigned short* pm = sat<unsigned short>(o.perm);
     tail_v(L, nlev, T, alpha, sb, g);
     for (int rep = 1; rep < gamma; rep++) {
       for (int i = tid; i < n; i += kGmThreads) {
@@ -367,7 +383,10 @@ __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const Ta
         if (rep == 1) Q[i] = R[i];
       }
       __syncthreads();
-      for (int i = tid; i < n; i += kGmThreads) R[i] = Q[i] - sell_row(rp, cl, va, i, [&](int j) { return S[j]; });
+      for (int p = tid; p < n; p += kGmThreads) {
+        const int i = pm[p];
+        R[i] = Q[i] - sell_row(rp, cl, va, p, [&](int j) { return S[j]; });
+      }
       __syncthreads();
       tail_v(L, nlev, T, alpha, sb, g);
     }
@@ -378,7 +397,7 @@ __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const Ta
     tail_v(L, nlev, T, alpha, sb, t0);
   }
   if (t0 == 0) {
-    const float* X = at<float>(sb, T.lv[0].X);
+    const float* X = sat<float>(T.lv[0].X);
     for (int r = r0 + tid; r < r1; r += kGmThreads) z[r] = (double)X[r - lo];
   }
 }
@@ -447,7 +466,7 @@ __device__ bool vcycle(const AmgDevLevel* L, int nlev, const TailLayout& T, floa
   const Rows own = share(lo, hi, Tm);
   tail_cycle(L, nlev, T, alpha, gamma, sb, buf, own.r0, own.r1, lo, z);
   if (t0 == 0) return grid_barrier(Tm.bar, Tm.size, err);
-  const float* Xs = at<float>(sb, T.lv[t0].X);
+  const float* Xs = sat<float>(T.lv[t0].X);
   for (int l = t0 - 1; l >= 0; l--) {
     const Rows rw = l == 0 ? own : share(0, L[l].n, Tm);
     float* outf = l == 0 ? nullptr : L[l].t;

@@ -147,31 +147,34 @@ namespace {
 
 int align16(long b) { return (int)((b + 15) / 16 * 16); }
 
-// SELL-32 copy of a level's pattern (AmgDevLevel::sell_*)
+// SELL-32 copy of a level's pattern (AmgDevLevel::sell_*): rows ordered by length (longest
+// first, ties in row order), slices of 32 consecutive positions padded to their longest row
 struct Sell {
   std::vector<int> ptr, src;
-  std::vector<unsigned short> col;
+  std::vector<unsigned short> col, row;
 };
 Sell sell32(const AmgHostLevel& L) {
   Sell S;
   const int ns = (L.n + 31) / 32;
+  auto len = [&](int i) { return L.rowptr[i + 1] - L.rowptr[i]; };
+  std::vector<int> order(L.n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return len(a) > len(b); });
+  S.row.assign(32L * ns, 0);
+  for (int p = 0; p < L.n; p++) S.row[p] = (unsigned short)order[p];
   S.ptr.assign(ns + 1, 0);
-  for (int s = 0; s < ns; s++) {
-    int w = 0;
-    for (int i = 32 * s; i < std::min(L.n, 32 * s + 32); i++) w = std::max(w, L.rowptr[i + 1] - L.rowptr[i]);
-    S.ptr[s + 1] = S.ptr[s] + 32 * w;
-  }
+  for (int s = 0; s < ns; s++) S.ptr[s + 1] = S.ptr[s] + 32 * len(order[32 * s]);  // the slice's first row is its longest
   S.col.assign(S.ptr[ns], 0);
   S.src.assign(S.ptr[ns], -1);
   for (int s = 0; s < ns; s++) {
     const int w = (S.ptr[s + 1] - S.ptr[s]) / 32;
     for (int lane = 0; lane < 32; lane++) {
-      const int i = 32 * s + lane;
-      if (i >= L.n) continue;
-      const int len = L.rowptr[i + 1] - L.rowptr[i];
+      const int p = 32 * s + lane;
+      if (p >= L.n) continue;
+      const int i = order[p];
       for (int k = 0; k < w; k++) {
         const int e = S.ptr[s] + 32 * k + lane;
-        if (k < len) {
+        if (k < len(i)) {
           S.col[e] = (unsigned short)L.col[L.rowptr[i] + k];
           S.src[e] = L.rowptr[i] + k;
         } else {
@@ -192,7 +195,8 @@ TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz, c
   auto level_bytes = [&](int l) -> long {
     if (l == L - 1) return align16(4L * n[l] * n[l]) + 2L * align16(4L * n[l]);
     const long ns = (n[l] + 31) / 32;
-    return align16(4L * (ns + 1)) + align16(2L * sell[l]) + align16(4L * sell[l]) + align16(4L * n[l]) +
+    return align16(4L * (ns + 1)) + align16(2L * sell[l]) + align16(4L * sell[l]) + align16(64L * ns) +
+           align16(4L * n[l]) +
            align16(4L * n[l]) + align16(4L * (n[l + 1] + 1)) + align16(4L * n[l]) + 3L * align16(4L * n[l]);
   };
   long total = level_bytes(L - 1);
@@ -205,13 +209,14 @@ TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz, c
     off += align16(b);
     return o;
   };
-  for (int l = 0; l < kAmgMaxLevels; l++) T.lv[l] = TailLevelOff{-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  for (int l = 0; l < kAmgMaxLevels; l++) T.lv[l] = TailLevelOff{-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
   for (int l = t; l < L; l++) {
     TailLevelOff& o = T.lv[l];
     if (l + 1 < L) {
       o.rowptr = take(4L * ((n[l] + 31) / 32 + 1));
       o.col = take(2L * sell[l]);
       o.val = take(4L * sell[l]);
+      o.perm = take(64L * ((n[l] + 31) / 32));
       o.wdinv = take(4L * n[l]);
       o.agg = take(4L * n[l]);
       o.ptptr = take(4L * (n[l + 1] + 1));
@@ -421,12 +426,14 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
       e.sell_ptr = nullptr;
       e.sell_col = nullptr;
       e.sell_src = nullptr;
+      e.sell_row = nullptr;
       e.sell_len = 0;
       if (l < cd.tl.tail || l + 1 >= cd.nlev) continue;
       const Sell& S = sells[l];
       e.sell_ptr = up.upload_int(S.ptr.data(), (long)S.ptr.size());
       e.sell_col = (const unsigned short*)up.upload_bytes(S.col.data(), 2L * (long)S.col.size());
       e.sell_src = up.upload_int(S.src.data(), (long)S.src.size());
+      e.sell_row = (const unsigned short*)up.upload_bytes(S.row.data(), 2L * (long)S.row.size());
       e.sell_len = (int)S.col.size();
     }
     cd.levels = (const AmgDevLevel*)up.upload_bytes(v.levels[c].data(), sizeof(AmgDevLevel) * cd.nlev);

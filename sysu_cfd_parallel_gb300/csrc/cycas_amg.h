@@ -25,6 +25,11 @@ constexpr int kAmgTailBudget = 188 * 1024;
 // barrier) that the saved iterations repay only on large cases: measured on GB300 per 10 SIMPLE
 // iterations, 480k-tet channel -7.5 %, 104k -4 %, 60k +8 %, 4k-cell cavity +5 %.
 constexpr int kAmgWRows = 80000;
+// The second cycle runs on the first tail level (below level 0) with at most this many rows:
+// every tail pass streams the level's matrix through one SM's shared memory, so a second cycle
+// on a level of ~1000 rows costs more than the CG iterations it saves (48^3 cavity: 20 CG
+// iterations of 67 us with the W-cycle on its 1244-row level against 23 of 58 us without).
+constexpr int kAmgWLevelRows = 512;
 
 struct AmgHostLevel {
   int n = 0, nnz = 0;
@@ -56,21 +61,23 @@ struct AmgDevLevel {
   const int* ptrow;   // rows of each aggregate (level 0: global rows)
   float* r;           // residual (level 0: FP32 copy of the CG residual, global rows)
   float* t;           // correction returned to the finer level (levels >= 1)
-  // levels of the shared-memory tail (else null): the pattern in SELL-32 layout -- rows in
-  // slices of 32, a slice column-major and padded to its longest row, so the 32 lanes of a warp
-  // read entry k of 32 consecutive rows from consecutive addresses (no bank conflicts).  Padding
+  // levels of the shared-memory tail (else null): the pattern in SELL-32 layout -- rows ordered
+  // by length (longest first) and cut into slices of 32 positions, a slice column-major and
+  // padded to its longest row, so the 32 lanes of a warp read entry k of 32 rows from
+  // consecutive addresses (no bank conflicts) and the ordering keeps the padding small.  Padding
   // entries have the row's own column and take the value 0; the real entries keep the CSR
   // order, so a row sums in the same order as in CSR.
   const int* sell_ptr;             // [ceil(n/32)+1] first entry of each slice
   const unsigned short* sell_col;  // [sell_len] local columns
   const int* sell_src;             // [sell_len] the entry's position in this level's CSR values, -1 for padding
+  const unsigned short* sell_row;  // [32 ceil(n/32)] the row at each position
   int sell_len;
 };
 
 // byte offsets of one tail level's arrays in dynamic shared memory: rowptr/col/val hold the
 // SELL-32 slice offsets, 16-bit columns and values of the level's matrix
 struct TailLevelOff {
-  int rowptr, col, val, wdinv, agg, ptptr, ptrow, R, X, T;
+  int rowptr, col, val, wdinv, agg, ptptr, ptrow, R, X, T, perm;  // perm: the row at each SELL position
 };
 
 // the coarsest levels of a case, cycled out of shared memory by every CTA that solves the case

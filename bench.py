@@ -519,6 +519,9 @@ def run_serve(args):
     opt = gmres_pc(batch_options(device=local), BATCH_POLY)
     opt.mixed = 1 if args.mixed else 0
     srv = Server(hbm_budget_gb=args.budget_gb, residual_tol=args.tol, max_iters=args.max_iters, options=opt)
+    srv.set_graph(True)
+    if args.max_cells > 0:
+        srv.set_max_cells(args.max_cells)
     t0 = Server.clock()
     k = 0
     steps = 0
@@ -547,9 +550,11 @@ def run_serve(args):
         "converged": len(conv), "server_steps": steps, "wall_s": wall,
         "cell_iters_per_s": cell_iters / wall, "n_gpus": 1, "dtype": "f64" if not args.mixed else "mixed",
         "data": "synthetic", "loop": srv.stats(),
+        "active_at_end": int(active), "queued_at_end": int(queued), "submitted": int(k),
         "config": {"workload": f"Poisson {args.rate}/s for {args.duration}s; cavities n={args.cavity_n}, "
                                f"channels m={args.channel_m}; tol {args.tol}; cap {args.max_iters} iterations; "
-                               f"budget {args.budget_gb} GB; drain {args.drain}s",
+                               f"budget {args.budget_gb} GB; active-cell cap {args.max_cells:g}; "
+                               f"drain {args.drain}s",
                    "mixed": bool(args.mixed)},
     }
     print(json.dumps(line), flush=True)
@@ -1142,6 +1147,101 @@ def run_channel(args):
         torch.distributed.destroy_process_group()
 
 
+def run_batch256(args):
+    """The batching workload as configured: 256 lid-driven cavities (n^3 hexahedra, n uniform in
+    {8..40}, node jitter 0.1h, Re log-uniform in [10, 1000], lid speed 1), every one solved to a
+    1e-6 residual (ResMax / cell volume sum, the cube's volume being 1).  Three legs:
+      * batched: all cases submitted at once to the continuous-batching server, FP64, every
+        batch iteration replayed as one CUDA graph; a case leaves the batch when it converges;
+      * batched + mixed: the same with mixed-precision GMRES (FP32 Arnoldi cycles in FP64
+        iterative refinement);
+      * one at a time: each case alone through cycas_solve_steady, plain FP64 with the
+        headline's preconditioners (the plain FP64 GPU path).
+    value: cell-iterations/s of the batched + mixed leg (every case's iterations to convergence
+    over the wall time from submission to the last retirement)."""
+    import numpy as np
+    import torch
+    from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver, Server
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    params = batch_cases(args.batch_cases)
+    ncel = [Case(p).ncel for p in params]
+    cells = sum(ncel)
+
+    def served(mixed):
+        opt = gmres_pc(batch_options_local(local), BATCH_POLY)
+        opt.mixed = 1 if mixed else 0
+        srv = Server(hbm_budget_gb=args.budget_gb, residual_tol=args.tol, max_iters=args.max_iters, options=opt)
+        srv.set_graph(True)
+        t0 = Server.clock()
+        ids = [srv.submit(p) for p in params]
+        steps = 0
+        while True:
+            active, queued = srv.step()
+            steps += 1
+            if active == 0 and queued == 0:
+                break
+        wall = Server.clock() - t0
+        res = [srv.results[i] for i in ids]
+        st = srv.stats()
+        srv.close()
+        its = np.array([r["iterations"] for r in res])
+        conv = sum(r["status"] == 1 for r in res)
+        lat = np.array([r["t_done"] - r["t_arrival"] for r in res])
+        return {"wall_s": wall, "value": float(np.dot(its, ncel)) / wall, "converged": int(conv),
+                "cases": len(res), "iterations": its.tolist(), "server_steps": steps,
+                "time_to_converged_p50_s": float(np.percentile(lat, 50)),
+                "time_to_converged_p99_s": float(np.percentile(lat, 99)), "loop": st}
+
+    out = {"batched": guarded(served, False), "batched_mixed": guarded(served, True)}
+
+    def alone():
+        from sysu_cfd_parallel_gb300 import capi
+        total_ms, its, fails = 0.0, [], 0
+        for p in params:
+            s = NavierStokesSolver(Case(p), headline_options(local))
+            stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            try:
+                r = s.solve_steady(args.max_iters, args.tol)
+                its.append(r["iterations"])
+                fails += 0 if r["resmax"][-1] < args.tol else 1
+            except capi.CycasError:
+                its.append(-1)
+                fails += 1
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+            s.close()
+        good = np.array([max(0, i) for i in its])
+        return {"device_s": total_ms / 1e3, "value": float(np.dot(good, ncel)) / (total_ms / 1e3),
+                "iterations": its, "not_converged": fails}
+
+    if not args.no_variants:
+        out["one_at_a_time_plain_fp64"] = guarded(alone)
+    bm = out["batched_mixed"]
+    line = {"metric": "cell-iters/s to 1e-6 resid (256 cavities, batched + mixed vs plain FP64 one at a time)",
+            "value": bm.get("value"), "unit": "cell-iters/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "mixed", "data": "synthetic", "cells": cells,
+            "config": {"workload": "%d cavities n~U{8..40}^3 hexahedra, jitter 0.1h, Re~logU[10,1000], each to "
+                                   "1e-6; continuous-batching server, CUDA graph per batch iteration" % len(params),
+                       "budget_gb": args.budget_gb, "max_iters": args.max_iters},
+            **out}
+    a = out.get("one_at_a_time_plain_fp64") or {}
+    for k in ("batched", "batched_mixed"):
+        if "wall_s" in out[k] and "device_s" in a:
+            out[k]["speedup_vs_one_at_a_time_plain_fp64"] = a["device_s"] / out[k]["wall_s"]
+    print(json.dumps(line), flush=True)
+
+
+def batch_options_local(local):
+    from sysu_cfd_parallel_gb300.solver import batch_options
+    return batch_options(device=local)
+
+
 def run_profile(args):
     """Profiling leg (for ncu and per-system timings): `--steps` SIMPLE iterations of a generated
     case after `--warmup` untimed ones, with the per-system Krylov timing of the library on; prints
@@ -1188,7 +1288,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision and batched lines")
     ap.add_argument("--workload", default="cavity",
-                    choices=["cavity", "channel", "serve", "precision", "transient", "profile"])
+                    choices=["cavity", "channel", "serve", "precision", "transient", "profile", "batch256"])
+    ap.add_argument("--batch-cases", type=int, default=256, help="batch256 workload: number of cavities")
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--drain", type=float, default=120.0)
@@ -1197,6 +1298,8 @@ def main():
     ap.add_argument("--cavity-n", default="16,64")
     ap.add_argument("--channel-m", default="10,25")
     ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--max-cells", type=float, default=4e6,
+                    help="serve workload: cap on the active requests' cells (0: HBM budget only)")
     ap.add_argument("--mixed", action="store_true")
     ap.add_argument("--serve-seed", type=int, default=5)
     ap.add_argument("--outer-rtol", type=float, default=1e-10, help="precision workload: rtol of every system")
@@ -1214,6 +1317,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "profile":
         run_profile(args)
+    elif args.workload == "batch256":
+        run_batch256(args)
     elif args.workload == "serve":
         run_serve(args)
     elif args.workload == "precision":

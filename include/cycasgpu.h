@@ -435,6 +435,16 @@ double cycas_footprint_estimate(const cycas_case* c);
 int cycas_server_create(const cycas_options* opt, double hbm_budget_bytes, double residual_tol, int32_t max_iters,
                         int32_t keep_fields, cycas_server** out);
 void cycas_server_destroy(cycas_server* s);
+/* Replay each batch's SIMPLE-C iterations as one CUDA graph (cycas_set_graph on every batch the
+ * server builds; a batch is captured on its first iteration after a rebuild).  No counterpart in
+ * the reference. */
+int cycas_server_set_graph(cycas_server* s, int32_t on);
+/* Admission by compute as well as by memory: requests join only while the cells of the active
+ * requests stay within max_cells (0: no cap; a request larger than the cap runs alone once
+ * nothing else is active).  When requests arrive faster than the GPU finishes them, the cap keeps
+ * each step short and lets admitted requests finish in arrival order instead of every request
+ * advancing slowly in one huge batch.  No counterpart in the reference. */
+int cycas_server_set_max_cells(cycas_server* s, double max_cells);
 double cycas_server_clock(void);
 /* queues a request; CYCAS_ERR_UNSUPPORTED for transient, energy or perfect-gas cases (batches
  * hold steady, isothermal, constant-density cases) */

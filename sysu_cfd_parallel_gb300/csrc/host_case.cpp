@@ -18,6 +18,9 @@
 // reference's per-vertex std::set search and per-face realloc; it reproduces the same face
 // indices, owner/neighbour and per-cell face slots for conforming meshes.
 #include <algorithm>
+#include <sys/stat.h>
+#include <mutex>
+#include <memory>
 #include <cctype>
 #include <cerrno>
 #include <climits>
@@ -613,6 +616,90 @@ void init_fields(HostCase& hc) {
   }
 }
 
+namespace {
+
+// Parsed meshes (gmsh ingest + face discovery), shared by every case that loads the same file:
+// a request server loads many cases that differ only in their param.in (Reynolds number, inlet
+// velocity) over a few dozen meshes.  Keyed by the file's path, size, inode and modification
+// time, so a rewritten file is parsed again; bounded in bytes, least recently used first out.
+struct MeshEntry {
+  std::shared_ptr<const HostCase> mesh;  // only the mesh arrays are filled
+  size_t bytes = 0;
+  uint64_t used = 0;
+};
+std::mutex g_mesh_mu;
+std::map<std::string, MeshEntry> g_meshes;
+uint64_t g_mesh_clock = 0;
+size_t g_mesh_bytes = 0;
+constexpr size_t kMeshCacheBytes = size_t(4) << 30;
+
+template <class T>
+size_t vbytes(const std::vector<T>& v) { return v.size() * sizeof(T); }
+
+size_t mesh_bytes(const HostCase& h) {
+  return vbytes(h.vert) + vbytes(h.cell_vertices) + vbytes(h.cell_rid) + vbytes(h.cell_nface) +
+         vbytes(h.cell_face) + vbytes(h.cell_cell) + vbytes(h.bnd_vertices) + vbytes(h.bnd_rid) +
+         vbytes(h.bnd_face) + vbytes(h.face_cell1) + vbytes(h.face_cell2) + vbytes(h.face_bnd) +
+         vbytes(h.face_vertices);
+}
+
+void copy_mesh(HostCase& dst, const HostCase& src) {
+  dst.ncel = src.ncel;
+  dst.nfac = src.nfac;
+  dst.nbnd = src.nbnd;
+  dst.nvrt = src.nvrt;
+  dst.vert = src.vert;
+  dst.cell_vertices = src.cell_vertices;
+  dst.cell_rid = src.cell_rid;
+  dst.cell_nface = src.cell_nface;
+  dst.cell_face = src.cell_face;
+  dst.cell_cell = src.cell_cell;
+  dst.bnd_vertices = src.bnd_vertices;
+  dst.bnd_rid = src.bnd_rid;
+  dst.bnd_face = src.bnd_face;
+  dst.face_cell1 = src.face_cell1;
+  dst.face_cell2 = src.face_cell2;
+  dst.face_bnd = src.face_bnd;
+  dst.face_vertices = src.face_vertices;
+}
+
+// the mesh arrays of `grid` into hc, parsed once per file version
+void load_mesh_cached(HostCase& hc, const std::string& grid, bool binary) {
+  struct stat st;
+  if (stat(grid.c_str(), &st) != 0) throw IoError("cant find grid file " + grid);
+  const std::string key = grid + "|" + std::to_string((long long)st.st_size) + "|" +
+                          std::to_string((unsigned long long)st.st_ino) + "|" +
+                          std::to_string((long long)st.st_mtim.tv_sec) + "." +
+                          std::to_string((long long)st.st_mtim.tv_nsec) + (binary ? "|b" : "|a");
+  {
+    std::lock_guard<std::mutex> lk(g_mesh_mu);
+    auto it = g_meshes.find(key);
+    if (it != g_meshes.end()) {
+      it->second.used = ++g_mesh_clock;
+      copy_mesh(hc, *it->second.mesh);
+      return;
+    }
+  }
+  auto m = std::make_shared<HostCase>();
+  load_gmsh(*m, grid, binary);
+  build_faces(*m);
+  copy_mesh(hc, *m);
+  const size_t b = mesh_bytes(*m);
+  std::lock_guard<std::mutex> lk(g_mesh_mu);
+  if (b > kMeshCacheBytes || g_meshes.count(key)) return;
+  while (g_mesh_bytes + b > kMeshCacheBytes && !g_meshes.empty()) {
+    auto lru = g_meshes.begin();
+    for (auto it = g_meshes.begin(); it != g_meshes.end(); ++it)
+      if (it->second.used < lru->second.used) lru = it;
+    g_mesh_bytes -= lru->second.bytes;
+    g_meshes.erase(lru);
+  }
+  g_meshes[key] = MeshEntry{m, b, ++g_mesh_clock};
+  g_mesh_bytes += b;
+}
+
+}  // namespace
+
 void load_case(HostCase& hc, const std::string& paramPath, bool msh_binary) {
   load_params(hc, paramPath);
   std::string grid = hc.gridfile;
@@ -621,8 +708,7 @@ void load_case(HostCase& hc, const std::string& paramPath, bool msh_binary) {
     size_t sl = paramPath.find_last_of('/');
     if (sl != std::string::npos) grid = paramPath.substr(0, sl + 1) + grid;
   }
-  load_gmsh(hc, grid, msh_binary);
-  build_faces(hc);
+  load_mesh_cached(hc, grid, msh_binary);
   size_t sl = paramPath.find_last_of('/');
   hc.backup_path = (sl == std::string::npos ? std::string() : paramPath.substr(0, sl + 1)) + "res.sav";
   init_fields(hc);

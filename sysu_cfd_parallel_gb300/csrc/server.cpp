@@ -4,14 +4,23 @@
 //   1. admits queued requests while the estimated device footprint of the active cases stays
 //      within the HBM budget (first come, first served: a request that does not fit blocks the
 //      ones behind it, so large cases are not starved; one larger than the whole budget runs
-//      alone);
+//      alone; with cycas_server_set_max_cells also while the active requests' cells stay within
+//      a cap, which bounds the time of one step when more work arrives than the GPU does) -- at
+//      once when the server is idle, otherwise once the iterations since the last
+//      admission have taken as long as the batch rebuild that admission cost (a rebuild of a
+//      batch of millions of cells costs about a second of host time; admitting at every step
+//      of a busy server would spend most of its time rebuilding);
 //   2. rebuilds the batch of every physics class whose membership changed (cases of one batch
 //      share the turbulence model and relaxation factors), moving the state of the cases that
 //      stay from the old batch to the new one on the device;
 //   3. advances every active case by one SIMPLE-C iteration (one batch iteration per class);
 //   4. retires every case whose residual, max_i localRes[i] divided by the case's volume, is
 //      at or below the tolerance, that reached the iteration cap, or whose fields stopped being
-//      finite, recording its times.
+//      finite, recording its times (and fields).  A retired case leaves its batch at the next
+//      rebuild, which comes when new requests join the class or when retired cases hold a
+//      quarter of the batch's cells: rebuilding a batch of millions of cells costs about a
+//      second of host time, so rebuilding at every retirement would cost more than iterating
+//      the retired cases along (their results are taken at retirement and no longer change).
 // A case's iterations are exactly those it would do alone; only the Krylov inner products
 // sum in another order (see the batch contexts).
 #include <algorithm>
@@ -65,13 +74,18 @@ struct cycas_server {
   double budget = 0.0, tol = 1e-6;
   int max_iters = 10000;
   int keep_fields = 0;
+  int graph = 0;  // replay every batch's iterations as one CUDA graph (cycas_server_set_graph)
+  double max_cells = 0.0;  // cap on the cells of the active requests (0: none), cycas_server_set_max_cells
+  double active_cells = 0.0;
   int64_t next_id = 1;
   std::deque<std::unique_ptr<Request>> queue;
   struct Class {
     std::vector<std::unique_ptr<Request>> active;
     cycas_ctx* ctx = nullptr;
-    std::vector<Request*> members;  // case order of ctx
+    std::vector<Request*> members;  // case order of ctx (retired members stay until the next rebuild)
     bool dirty = false;
+    double cells = 0.0, retired_cells = 0.0;  // of the batch, and of its retired members
+    double retired_footprint = 0.0;           // released from the budget at the next rebuild
   };
   std::map<int, Class> classes;  // by turbulence model
   std::vector<std::unique_ptr<Request>> finished;
@@ -79,6 +93,9 @@ struct cycas_server {
   std::string err;
   // host wall time of the loop's parts (cycas_server_stats)
   double t_rebuild = 0.0, t_iterate = 0.0, t_admin = 0.0;
+  // admission is held back while the iterations since the last admission rebuild have taken
+  // less time than that rebuild, so rebuild time stays at most about half of the loop
+  double last_admit_rebuild_s = 0.0, iterate_since_admit_s = 0.0;
   int64_t n_rebuild = 0, n_steps = 0;
 };
 
@@ -105,6 +122,10 @@ int rebuild(cycas_server* s, cycas_server::Class& K) {
     }
     int rc = cycas_batch_create(cases.data(), (int32_t)cases.size(), &s->opt, &K.ctx);
     if (rc != CYCAS_OK) return fail(s, rc);
+    if (s->graph) {
+      rc = cycas_set_graph(K.ctx, 1);  // captured on the batch's first iteration
+      if (rc != CYCAS_OK) return fail(s, rc);
+    }
     // continuing cases keep their state
     for (size_t k = 0; k < K.members.size(); k++) {
       auto it = std::find(old_members.begin(), old_members.end(), K.members[k]);
@@ -127,6 +148,11 @@ int rebuild(cycas_server* s, cycas_server::Class& K) {
   }
   if (old) cycas_destroy(old);
   K.dirty = false;
+  K.cells = 0.0;
+  for (Request* r : K.members) K.cells += (double)r->dims[0];
+  K.retired_cells = 0.0;
+  s->in_use -= K.retired_footprint;
+  K.retired_footprint = 0.0;
   return CYCAS_OK;
 }
 
@@ -146,6 +172,23 @@ int cycas_server_create(const cycas_options* opt, double hbm_budget_bytes, doubl
   s->max_iters = max_iters;
   s->keep_fields = keep_fields;
   *out = s;
+  return CYCAS_OK;
+}
+
+int cycas_server_set_max_cells(cycas_server* s, double max_cells) {
+  if (!s || max_cells < 0.0) return CYCAS_ERR_INVALID;
+  s->max_cells = max_cells;
+  return CYCAS_OK;
+}
+
+int cycas_server_set_graph(cycas_server* s, int32_t on) {
+  if (!s) return CYCAS_ERR_INVALID;
+  s->graph = on ? 1 : 0;
+  for (auto& kv : s->classes)
+    if (kv.second.ctx) {
+      int rc = cycas_set_graph(kv.second.ctx, s->graph);
+      if (rc != CYCAS_OK) return fail(s, rc);
+    }
   return CYCAS_OK;
 }
 
@@ -199,14 +242,40 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
       if (!kv.second.active.empty()) return false;
     return true;
   };
-  while (!s->queue.empty() && (s->in_use + s->queue.front()->footprint <= s->budget || idle())) {
+  // the budget still counts retired cases until their batch is rebuilt: when the first queued
+  // request does not fit, rebuild the batches that hold retired cases to release them
+  if (!s->queue.empty() && s->in_use + s->queue.front()->footprint > s->budget) {
+    for (auto& kv : s->classes) {
+      auto& K = kv.second;
+      if (K.retired_footprint <= 0.0) continue;
+      const double t0 = now_s();
+      int rc = rebuild(s, K);
+      s->t_rebuild += now_s() - t0;
+      s->n_rebuild++;
+      if (rc != CYCAS_OK) return rc;
+    }
+  }
+  const bool was_idle = idle();
+  const bool admit = was_idle || s->iterate_since_admit_s >= s->last_admit_rebuild_s;
+  std::map<int, bool> admitted;  // classes that took new requests this step
+  auto fits = [&](const Request& r) {
+    return s->in_use + r.footprint <= s->budget &&
+           (s->max_cells <= 0.0 || s->active_cells + (double)r.dims[0] <= s->max_cells);
+  };
+  while (admit && !s->queue.empty() && (fits(*s->queue.front()) || idle())) {
     std::unique_ptr<Request> r = std::move(s->queue.front());
     s->queue.pop_front();
     r->t_admit = now_s();
     s->in_use += r->footprint;
+    s->active_cells += (double)r->dims[0];
     auto& K = s->classes[r->turb];
+    admitted[r->turb] = true;
     K.active.push_back(std::move(r));
     K.dirty = true;
+  }
+  if (!admitted.empty()) {
+    s->last_admit_rebuild_s = 0.0;
+    s->iterate_since_admit_s = 0.0;
   }
   // 2-4. per class: rebuild if needed, one iteration, retire
   for (auto& kv : s->classes) {
@@ -214,8 +283,10 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
     if (K.dirty) {
       const double t0 = now_s();
       int rc = rebuild(s, K);
-      s->t_rebuild += now_s() - t0;
+      const double dt = now_s() - t0;
+      s->t_rebuild += dt;
       s->n_rebuild++;
+      if (admitted.count(kv.first)) s->last_admit_rebuild_s += dt;
       if (rc != CYCAS_OK) return rc;
     }
     if (K.members.empty()) continue;
@@ -225,11 +296,13 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
     const double t0 = now_s();
     int rc = cycas_batch_iteration(K.ctx, resmax.data(), its.data(), reasons.data());
     s->t_iterate += now_s() - t0;
+    s->iterate_since_admit_s += now_s() - t0;
     // per-case outcomes are judged below; only errors of the batch itself stop the server
     if (rc != CYCAS_OK && rc != CYCAS_NOT_CONVERGED && rc != CYCAS_NAN_DETECTED) return fail(s, rc);
     std::vector<int> retire;
     for (int k = 0; k < nc; k++) {
       Request* r = K.members[k];
+      if (r->status != 0) continue;  // retired earlier, iterated along until the next rebuild
       r->iterations++;
       r->resmax = resmax[k] / (r->volume > 0.0 ? r->volume : 1.0);
       // a Krylov solve that stops short (iteration cap, breakdown near a converged field) does
@@ -260,7 +333,9 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
       std::vector<std::unique_ptr<Request>> keep;
       for (auto& r : K.active) {
         if (r->status != 0) {
-          s->in_use -= r->footprint;
+          K.retired_footprint += r->footprint;
+          K.retired_cells += (double)r->dims[0];
+          s->active_cells -= (double)r->dims[0];
           cycas_case_free(r->cs);
           r->cs = nullptr;
           s->finished.push_back(std::move(r));
@@ -269,7 +344,7 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
         }
       }
       K.active.swap(keep);
-      K.dirty = true;
+      if (K.active.empty() || K.retired_cells >= 0.25 * K.cells) K.dirty = true;
     }
   }
   int act = 0;

@@ -570,6 +570,15 @@ class Server:
     def clock() -> float:
         return capi.load().cycas_server_clock()
 
+    def set_graph(self, on: bool) -> None:
+        """Replay each batch's iterations as one CUDA graph (cycas_server_set_graph)."""
+        capi.check(capi.load().cycas_server_set_graph(self._h, 1 if on else 0))
+
+    def set_max_cells(self, max_cells: float) -> None:
+        """Admit requests only while the active requests' cells stay within max_cells (0: no
+        cap; cycas_server_set_max_cells)."""
+        capi.check(capi.load().cycas_server_set_max_cells(self._h, float(max_cells)))
+
     def submit(self, param_path: str) -> int:
         i = C.c_int64()
         rc = capi.load().cycas_server_submit(self._h, param_path.encode(), C.byref(i))

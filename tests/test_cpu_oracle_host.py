@@ -278,3 +278,24 @@ def test_defaults_follow_reference():
     capi.load().cycas_options_default(C.byref(o))
     assert [o.ksp[s].type for s in range(3)] in ([capi.KSP_DEFAULT] * 3, [capi.KSP_GMRES, capi.KSP_CG, capi.KSP_GMRES])
     assert all(o.ksp[s].restart == 30 for s in range(3))
+
+
+def test_mesh_cache_reuses_and_invalidates(tmp_path):
+    """The loader parses a mesh file once per version: a second case over the same file gets
+    the same arrays with its own parameters, and a rewritten file is parsed again."""
+    d = tmp_path / "mc"
+    p = meshgen.write_case(str(d), "cavity", n=5, jitter=0.1, seed=3, steps=5)
+    a = Case(p)
+    text = open(p).read().replace("0.01", "0.05")
+    p2 = str(d / "param2.in")
+    open(p2, "w").write(text)
+    b = Case(p2)
+    for nm in HOST_INT + ["cell_rid", "bnd_rid", "bnd_vertices"]:
+        assert np.array_equal(a.get_int(nm), b.get_int(nm)), nm
+    assert np.array_equal(a.get_field("VisLam") * 5.0, b.get_field("VisLam"))
+    meshgen.write_case(str(d), "cavity", n=6, steps=5)  # same path, another mesh
+    c = Case(p)
+    assert c.ncel == 216 and a.ncel == 125
+    o = po.OracleCase(p)
+    for nm in HOST_INT:
+        assert np.array_equal(c.get_int(nm), o.geti(nm)), nm

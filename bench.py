@@ -290,8 +290,9 @@ def guarded(fn, *a, **kw):
     return out
 
 
-def measure_mixed_solve(param, local, steps, ref_fields, fp64_ms, fp64_iters):
-    # fp64_ms: the FP64 solve's time per step (ms)
+def measure_mixed_solve(param, local, steps, ref_fields, fp64_ms, fp64_iters, level=1):
+    # fp64_ms: the FP64 solve's time per step (ms); level 1: FP32 Arnoldi cycles, 2: also FP32
+    # assembly (gradients, momentum rows, Rhie-Chow flux)
     """The headline solve with mixed-precision GMRES (FP32 Arnoldi cycles in FP64 iterative
     refinement) to the same stop test: time to converged against FP64 and the relative-L2 error of
     every field at convergence against the FP64 solve's."""
@@ -299,7 +300,9 @@ def measure_mixed_solve(param, local, steps, ref_fields, fp64_ms, fp64_iters):
     import torch
     from sysu_cfd_parallel_gb300.solver import Case, NavierStokesSolver
     case = Case(param)
-    s = NavierStokesSolver(case, headline_options(local, mixed=True))
+    opt = headline_options(local, mixed=True)
+    opt.mixed = level
+    s = NavierStokesSolver(case, opt)
     s.save_restart_point()
     stream = torch.cuda.ExternalStream(s.stream_handle(), device=local)
     solve_from_restart(s)
@@ -310,6 +313,7 @@ def measure_mixed_solve(param, local, steps, ref_fields, fp64_ms, fp64_iters):
             "iterations_to_converge": last["iterations"], "fp64_iterations_to_converge": fp64_iters,
             "time_to_converged_speedup_vs_fp64": fp64_ms / (ms / steps),
             "krylov": "GMRES systems: FP32 Arnoldi cycles (inner rtol 1e-4) in FP64 iterative refinement",
+            "assembly": "FP32 gradients, momentum rows and Rhie-Chow flux" if level == 2 else "FP64",
             "field_rel_l2_vs_fp64_at_convergence": err}
 
 
@@ -937,6 +941,9 @@ def run_gpu(args):
         output = guarded(measure_output_solve, s, stream, ms / args.steps)
         mixed = guarded(measure_mixed_solve, param, local, max(1, min(args.steps, 3)), ref_fields, ms / args.steps,
                         its_per_solve)
+        if isinstance(mixed, dict) and "error" not in mixed:
+            mixed["fp32_assembly"] = guarded(measure_mixed_solve, param, local, max(1, min(args.steps, 3)),
+                                             ref_fields, ms / args.steps, its_per_solve, 2)
         batched = guarded(measure_batched, local, BATCH_SAMPLE, 10)
 
     cpu = None

@@ -187,7 +187,14 @@ typedef struct {
                                for the GMRES systems (momentum, k, epsilon): FP32 Arnoldi cycles
                                wrapped in FP64 iterative refinement, each cycle ending at a
                                relative drop of inner_rtol, convergence tested on the FP64 true
-                               residual to the system's rtol (no counterpart in the reference) */
+                               residual to the system's rtol (no counterpart in the reference).
+                               2: as 1, and the gradients, momentum rows and Rhie-Chow face flux
+                               computed in FP32 (FP64 storage; the pressure-correction rows, their
+                               FP64 mass-imbalance sum, the corrections and the residuals stay
+                               FP64).  Level 2 shifts the discrete solution by about 1e-5
+                               relative (48^3 cavity at ResMax 1e-6: u 4.5e-6, v 1.6e-5, w 6.5e-6,
+                               p 4.9e-6 against FP64) and floors the residual between 1e-6 and
+                               1e-8; level 1 stays within 1e-8 of FP64. */
   double inner_rtol;        /* <= 0: 1e-4 */
   /* pressure AMG cycle (CYCAS_PC_AMG; no counterpart in the reference, whose pressure PC is
    * PETSc's ILU(0)); 0 selects the default */

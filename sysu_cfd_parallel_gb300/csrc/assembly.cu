@@ -10,6 +10,8 @@
 // are bit-identical to the reference arithmetic evaluated without contraction.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "cycas_device.h"
 
 namespace cycas {
@@ -33,6 +35,25 @@ __device__ __forceinline__ double vdot3(const double* a, double b0, double b1, d
 }
 __device__ __forceinline__ double vdot3v(double a0, double a1, double a2, double b0, double b1, double b2) {
   double s = 0.;
+  s += a0 * b0;
+  s += a1 * b1;
+  s += a2 * b2;
+  return s;
+}
+// the same sums in the arithmetic type T of an assembly kernel (double: the functions above)
+template <class T>
+__device__ __forceinline__ T tmin(T x, T y) { return x < y ? x : y; }
+template <class T>
+__device__ __forceinline__ T tdot3(const T* a, T b0, T b1, T b2) {
+  T s = T(0);
+  s += a[0] * b0;
+  s += a[1] * b1;
+  s += a[2] * b2;
+  return s;
+}
+template <class T>
+__device__ __forceinline__ T tdot3v(T a0, T a1, T a2, T b0, T b1, T b2) {
+  T s = T(0);
   s += a0 * b0;
   s += a1 * b1;
   s += a2 * b2;
@@ -312,27 +333,38 @@ struct GradArgs {
 // Green-Gauss (navier_gradient.cpp:12-74, limiter 0): the reference loops over faces and
 // scatters +-pf*n to both cells; per cell that is a sum over its faces in ascending face
 // index, which is the order c_gface holds.
-template <int NF>
+// T is the arithmetic type: double in the FP64 path (bit-exact with the reference), float in
+// mixed-precision contexts (loads are rounded to float once, results widened back).
+template <class T, int NF>
 __global__ void k_gradient(int ncel, const int* __restrict__ c_nface, const int* __restrict__ c_gface,
                            const int* __restrict__ f_c1, const int* __restrict__ f_c2,
                            const int* __restrict__ f_bnd, const double* __restrict__ f_lambda,
                            const double* __restrict__ f_n, const double* __restrict__ c_vol, GradArgs<NF> a) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ncel) return;
-  double g[NF][3];
+  T g[NF][3];
 #pragma unroll
-  for (int q = 0; q < NF; q++) g[q][0] = g[q][1] = g[q][2] = 0.;
+  for (int q = 0; q < NF; q++) g[q][0] = g[q][1] = g[q][2] = T(0);
   int nf = c_nface[i];
   for (int k = 0; k < nf; k++) {
     int fid = c_gface[(long)k * ncel + i];
     int c1 = f_c1[fid], c2 = f_c2[fid];
-    double n0 = f_n[3 * (long)fid], n1 = f_n[3 * (long)fid + 1], n2 = f_n[3 * (long)fid + 2];
+    T n0 = (T)f_n[3 * (long)fid], n1 = (T)f_n[3 * (long)fid + 1], n2 = (T)f_n[3 * (long)fid + 2];
     if (c2 >= 0) {
-      double lam = f_lambda[fid];
+      T lam = (T)f_lambda[fid];
       bool own = (c1 == i);
 #pragma unroll
       for (int q = 0; q < NF; q++) {
-        double pf = lam * __ldg(a.phi[q] + c1) + (1. - lam) * __ldg(a.phi[q] + c2);
+        T pf;
+        if constexpr (std::is_same<T, float>::value) {
+          // FP32: the face value relative to the cell's own, lambda-weighted difference of the
+          // FP64 values (the cell's normals sum to zero, so the sum is the same while the large
+          // face values no longer cancel in FP32)
+          const double d = __ldg(a.phi[q] + (own ? c2 : c1)) - __ldg(a.phi[q] + i);
+          pf = own ? (T(1) - lam) * (T)d : lam * (T)d;
+        } else {
+          pf = lam * (T)__ldg(a.phi[q] + c1) + (T(1) - lam) * (T)__ldg(a.phi[q] + c2);
+        }
         if (own) {
           g[q][0] += pf * n0;
           g[q][1] += pf * n1;
@@ -347,17 +379,19 @@ __global__ void k_gradient(int ncel, const int* __restrict__ c_nface, const int*
       int b = f_bnd[fid];
 #pragma unroll
       for (int q = 0; q < NF; q++) {
-        double pf = __ldg(a.bphi[q] + b);
+        T pf;
+        if constexpr (std::is_same<T, float>::value) pf = (T)(__ldg(a.bphi[q] + b) - __ldg(a.phi[q] + i));
+        else pf = (T)__ldg(a.bphi[q] + b);
         g[q][0] += pf * n0;
         g[q][1] += pf * n1;
         g[q][2] += pf * n2;
       }
     }
   }
-  double vol = c_vol[i];
+  T vol = (T)c_vol[i];
 #pragma unroll
   for (int q = 0; q < NF; q++)
-    for (int d = 0; d < 3; d++) a.grad[q][3 * (long)i + d] = g[q][d] / vol;
+    for (int d = 0; d < 3; d++) a.grad[q][3 * (long)i + d] = (double)(g[q][d] / vol);
 }
 
 // ------------------------------------------------------------------ momentum
@@ -377,59 +411,61 @@ struct MomArgs {
 };
 
 // BuildVelocityMatrix cell loop (navier_velocity.cpp:100-383)
+// T as for k_gradient: double (bit-exact) or float (mixed-precision contexts).
+template <class T>
 __global__ void __launch_bounds__(kThreads) k_momentum(MomArgs a) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.ncel) return;
   const long N = a.ncel;
-  double Ui = a.U[i], Vi = a.V[i], Wi = a.W[i];
-  double xi0 = a.c_x[3 * i], xi1 = a.c_x[3 * i + 1], xi2 = a.c_x[3 * i + 2];
-  double visi = a.VisLam[i] + a.VisTur[i];
-  double gu[3] = {a.dU[3 * i], a.dU[3 * i + 1], a.dU[3 * i + 2]};
-  double gv[3] = {a.dV[3 * i], a.dV[3 * i + 1], a.dV[3 * i + 2]};
-  double gw[3] = {a.dW[3 * i], a.dW[3 * i + 1], a.dW[3 * i + 2]};
-  double app = 0., su = 0., sv = 0., sw = 0.;
+  T Ui = (T)a.U[i], Vi = (T)a.V[i], Wi = (T)a.W[i];
+  T xi0 = (T)a.c_x[3 * i], xi1 = (T)a.c_x[3 * i + 1], xi2 = (T)a.c_x[3 * i + 2];
+  T visi = (T)a.VisLam[i] + (T)a.VisTur[i];
+  T gu[3] = {(T)a.dU[3 * i], (T)a.dU[3 * i + 1], (T)a.dU[3 * i + 2]};
+  T gv[3] = {(T)a.dV[3 * i], (T)a.dV[3 * i + 1], (T)a.dV[3 * i + 2]};
+  T gw[3] = {(T)a.dW[3 * i], (T)a.dW[3 * i + 1], (T)a.dW[3 * i + 2]};
+  T app = T(0), su = T(0), sv = T(0), sw = T(0);
   if (a.scheme != 0) {  // unsteady terms (navier_velocity.cpp:108-123)
-    double coef = a.R[i] / a.dt * a.c_vol[i];
-    double un = a.Unp[i], vn = a.Vnp[i], wn = a.Wnp[i];
+    T coef = (T)a.R[i] / (T)a.dt * (T)a.c_vol[i];
+    T un = (T)a.Unp[i], vn = (T)a.Vnp[i], wn = (T)a.Wnp[i];
     if (a.scheme == 1) {
       app += coef;
       su += coef * un;
       sv += coef * vn;
       sw += coef * wn;
     } else {  // both previous levels hold the same values (SaveTransientOldData)
-      app += 1.5 * coef;
-      su += coef * (2 * un - 0.5 * un);
-      sv += coef * (2 * vn - 0.5 * vn);
-      sw += coef * (2 * wn - 0.5 * wn);
+      app += T(1.5) * coef;
+      su += coef * (T(2) * un - T(0.5) * un);
+      sv += coef * (T(2) * vn - T(0.5) * vn);
+      sw += coef * (T(2) * wn - T(0.5) * wn);
     }
   }
   int nf = a.c_nface[i];
   for (int j = 0; j < nf; j++) {
     int iface = a.c_face[j * N + i];
     int ip = a.f_c1[iface], in = a.f_c2[iface];
-    double fde0, fde1, fde2, fdi0, fdi1, fdi2, fcs0, fcs1, fcs2;
+    T fde0, fde1, fde2, fdi0, fdi1, fdi2, fcs0, fcs1, fcs2;
     const double* fn = a.f_n + 3 * (long)iface;
     const double* fx = a.f_x + 3 * (long)iface;
     if (in < 0) {
       int bnd = a.f_bnd[iface];
       int t = a.b_type[bnd];
-      double s1 = fn[0], s2 = fn[1], s3 = fn[2];
-      double RUn = a.RUFace[iface];
-      double Visc = visi;
-      double dudx = gu[0], dudy = gu[1], dudz = gu[2];
-      double dvdx = gv[0], dvdy = gv[1], dvdz = gv[2];
-      double dwdx = gw[0], dwdy = gw[1], dwdz = gw[2];
-      double dxc0 = fx[0] - xi0, dxc1 = fx[1] - xi1, dxc2 = fx[2] - xi2;
-      double val = Visc * a.f_rlencos[iface];
+      T s1 = (T)fn[0], s2 = (T)fn[1], s3 = (T)fn[2];
+      T RUn = (T)a.RUFace[iface];
+      T Visc = visi;
+      T dudx = gu[0], dudy = gu[1], dudz = gu[2];
+      T dvdx = gv[0], dvdy = gv[1], dvdz = gv[2];
+      T dwdx = gw[0], dwdy = gw[1], dwdz = gw[2];
+      T dxc0 = (T)fx[0] - xi0, dxc1 = (T)fx[1] - xi1, dxc2 = (T)fx[2] - xi2;
+      T val = Visc * (T)a.f_rlencos[iface];
       app += val;
       if (t == 1) {
-        double sh0 = (dudx + dudx) * s1 + (dudy + dvdx) * s2 + (dudz + dwdx) * s3;
-        double sh1 = (dvdx + dudy) * s1 + (dvdy + dvdy) * s2 + (dvdz + dwdy) * s3;
-        double sh2 = (dwdx + dudz) * s1 + (dwdy + dvdz) * s2 + (dwdz + dwdz) * s3;
+        T sh0 = (dudx + dudx) * s1 + (dudy + dvdx) * s2 + (dudz + dwdx) * s3;
+        T sh1 = (dvdx + dudy) * s1 + (dvdy + dvdy) * s2 + (dvdz + dwdy) * s3;
+        T sh2 = (dwdx + dudz) * s1 + (dwdy + dvdz) * s2 + (dwdz + dwdz) * s3;
         sh0 *= Visc;
         sh1 *= Visc;
         sh2 *= Visc;
-        double Pi = a.P[i];
+        T Pi = (T)a.P[i];
         sh0 += Pi * s1;
         sh1 += Pi * s2;
         sh2 += Pi * s3;
@@ -442,7 +478,7 @@ __global__ void __launch_bounds__(kThreads) k_momentum(MomArgs a) {
         fdi0 = val * Ui;
         fdi1 = val * Vi;
         fdi2 = val * Wi;
-        fcs0 = fcs1 = fcs2 = 0.;
+        fcs0 = fcs1 = fcs2 = T(0);
       } else {
         fde0 = (dudx + dudx) * s1 + (dudy + dvdx) * s2 + (dudz + dwdx) * s3;
         fde1 = (dvdx + dudy) * s1 + (dvdy + dvdy) * s2 + (dvdz + dwdy) * s3;
@@ -450,15 +486,15 @@ __global__ void __launch_bounds__(kThreads) k_momentum(MomArgs a) {
         fde0 *= Visc;
         fde1 *= Visc;
         fde2 *= Visc;
-        double bu = a.BU[bnd], bv = a.BV[bnd], bw = a.BW[bnd];
+        T bu = (T)a.BU[bnd], bv = (T)a.BV[bnd], bw = (T)a.BW[bnd];
         fdi0 = val * (dudx * dxc0 + dudy * dxc1 + dudz * dxc2 - bu);
         fdi1 = val * (dvdx * dxc0 + dvdy * dxc1 + dvdz * dxc2 - bv);
         fdi2 = val * (dwdx * dxc0 + dwdy * dxc1 + dwdz * dxc2 - bw);
         if (t == 4) {
-          fcs0 = fcs1 = fcs2 = 0.;
+          fcs0 = fcs1 = fcs2 = T(0);
         } else {  // 2 inlet, 3 outlet
-          if (t == 2 && RUn > 0) atomicAdd(a.warn, 1);
-          double fl = dmin(RUn, 0.0);
+          if (t == 2 && RUn > T(0)) atomicAdd(a.warn, 1);
+          T fl = tmin<T>(RUn, T(0));
           app -= fl;
           fcs0 = fl * bu;
           fcs1 = fl * bv;
@@ -466,70 +502,84 @@ __global__ void __launch_bounds__(kThreads) k_momentum(MomArgs a) {
         }
       }
     } else {
-      double s1, s2, s3, RUn, lam;
-      double fl0 = a.f_lambda[iface];
+      T s1, s2, s3, RUn, lam;
+      T fl0 = (T)a.f_lambda[iface];
       if (i != ip) {
         in = ip;
-        s1 = -fn[0];
-        s2 = -fn[1];
-        s3 = -fn[2];
-        RUn = -a.RUFace[iface];
-        lam = 1. - fl0;
+        s1 = -(T)fn[0];
+        s2 = -(T)fn[1];
+        s3 = -(T)fn[2];
+        RUn = -(T)a.RUFace[iface];
+        lam = T(1) - fl0;
       } else {
-        s1 = fn[0];
-        s2 = fn[1];
-        s3 = fn[2];
-        RUn = a.RUFace[iface];
+        s1 = (T)fn[0];
+        s2 = (T)fn[1];
+        s3 = (T)fn[2];
+        RUn = (T)a.RUFace[iface];
         lam = fl0;
       }
-      double lam2 = 1. - lam;
-      double visn = a.VisLam[in] + a.VisTur[in];
-      double Visc = lam * visi + lam2 * visn;
-      double nu0 = a.dU[3 * (long)in], nu1 = a.dU[3 * (long)in + 1], nu2 = a.dU[3 * (long)in + 2];
-      double nv0 = a.dV[3 * (long)in], nv1 = a.dV[3 * (long)in + 1], nv2 = a.dV[3 * (long)in + 2];
-      double nw0 = a.dW[3 * (long)in], nw1 = a.dW[3 * (long)in + 1], nw2 = a.dW[3 * (long)in + 2];
-      double dudx = lam * gu[0] + lam2 * nu0, dudy = lam * gu[1] + lam2 * nu1, dudz = lam * gu[2] + lam2 * nu2;
-      double dvdx = lam * gv[0] + lam2 * nv0, dvdy = lam * gv[1] + lam2 * nv1, dvdz = lam * gv[2] + lam2 * nv2;
-      double dwdx = lam * gw[0] + lam2 * nw0, dwdy = lam * gw[1] + lam2 * nw1, dwdz = lam * gw[2] + lam2 * nw2;
-      double apn = 0.;
-      if (RUn < 0.) {
+      T lam2 = T(1) - lam;
+      T visn = (T)a.VisLam[in] + (T)a.VisTur[in];
+      T Visc = lam * visi + lam2 * visn;
+      T nu0 = (T)a.dU[3 * (long)in], nu1 = (T)a.dU[3 * (long)in + 1], nu2 = (T)a.dU[3 * (long)in + 2];
+      T nv0 = (T)a.dV[3 * (long)in], nv1 = (T)a.dV[3 * (long)in + 1], nv2 = (T)a.dV[3 * (long)in + 2];
+      T nw0 = (T)a.dW[3 * (long)in], nw1 = (T)a.dW[3 * (long)in + 1], nw2 = (T)a.dW[3 * (long)in + 2];
+      T dudx = lam * gu[0] + lam2 * nu0, dudy = lam * gu[1] + lam2 * nu1, dudz = lam * gu[2] + lam2 * nu2;
+      T dvdx = lam * gv[0] + lam2 * nv0, dvdy = lam * gv[1] + lam2 * nv1, dvdz = lam * gv[2] + lam2 * nv2;
+      T dwdx = lam * gw[0] + lam2 * nw0, dwdy = lam * gw[1] + lam2 * nw1, dwdz = lam * gw[2] + lam2 * nw2;
+      T apn = T(0);
+      if (RUn < T(0)) {
         apn += RUn;
         app -= RUn;
       }
-      double val = Visc * a.f_rlencos[iface];
+      T val = Visc * (T)a.f_rlencos[iface];
       app += val;
       apn += -val;
       a.A[a.c_slot[j * N + i]] = apn;
-      double Un = a.U[in], Vn = a.V[in], Wn = a.W[in];
-      double xn0 = a.c_x[3 * (long)in], xn1 = a.c_x[3 * (long)in + 1], xn2 = a.c_x[3 * (long)in + 2];
-      double ufi, vfi, wfi, ufh, vfh, wfh;
-      if (RUn > 0.) {
+      T Un = (T)a.U[in], Vn = (T)a.V[in], Wn = (T)a.W[in];
+      T xn0 = (T)a.c_x[3 * (long)in], xn1 = (T)a.c_x[3 * (long)in + 1], xn2 = (T)a.c_x[3 * (long)in + 2];
+      T ufi, vfi, wfi, ufh, vfh, wfh, cu, cv, cw;
+      if (RUn > T(0)) {
         ufi = Ui;
         vfi = Vi;
         wfi = Wi;
-        double dx0 = fx[0] - xi0, dx1 = fx[1] - xi1, dx2 = fx[2] - xi2;
-        ufh = Ui + vdot3(gu, dx0, dx1, dx2);
-        vfh = Vi + vdot3(gv, dx0, dx1, dx2);
-        wfh = Wi + vdot3(gw, dx0, dx1, dx2);
+        T dx0 = (T)fx[0] - xi0, dx1 = (T)fx[1] - xi1, dx2 = (T)fx[2] - xi2;
+        cu = tdot3<T>(gu, dx0, dx1, dx2);
+        cv = tdot3<T>(gv, dx0, dx1, dx2);
+        cw = tdot3<T>(gw, dx0, dx1, dx2);
+        ufh = Ui + cu;
+        vfh = Vi + cv;
+        wfh = Wi + cw;
       } else {
         ufi = Un;
         vfi = Vn;
         wfi = Wn;
-        double dx0 = fx[0] - xn0, dx1 = fx[1] - xn1, dx2 = fx[2] - xn2;
-        ufh = Un + vdot3v(nu0, nu1, nu2, dx0, dx1, dx2);
-        vfh = Vn + vdot3v(nv0, nv1, nv2, dx0, dx1, dx2);
-        wfh = Wn + vdot3v(nw0, nw1, nw2, dx0, dx1, dx2);
+        T dx0 = (T)fx[0] - xn0, dx1 = (T)fx[1] - xn1, dx2 = (T)fx[2] - xn2;
+        cu = tdot3v<T>(nu0, nu1, nu2, dx0, dx1, dx2);
+        cv = tdot3v<T>(nv0, nv1, nv2, dx0, dx1, dx2);
+        cw = tdot3v<T>(nw0, nw1, nw2, dx0, dx1, dx2);
+        ufh = Un + cu;
+        vfh = Vn + cv;
+        wfh = Wn + cw;
       }
-      fcs0 = RUn * (ufh - ufi);
-      fcs1 = RUn * (vfh - vfi);
-      fcs2 = RUn * (wfh - wfi);
+      if constexpr (std::is_same<T, float>::value) {
+        // FP32: the high-order correction itself (ufh - ufi is exactly the gradient term, whose
+        // digits the FP32 subtraction from ufh would lose)
+        fcs0 = RUn * cu;
+        fcs1 = RUn * cv;
+        fcs2 = RUn * cw;
+      } else {
+        fcs0 = RUn * (ufh - ufi);
+        fcs1 = RUn * (vfh - vfi);
+        fcs2 = RUn * (wfh - wfi);
+      }
       fde0 = (dudx + dudx) * s1 + (dudy + dvdx) * s2 + (dudz + dwdx) * s3;
       fde1 = (dvdx + dudy) * s1 + (dvdy + dvdy) * s2 + (dvdz + dwdy) * s3;
       fde2 = (dwdx + dudz) * s1 + (dwdy + dvdz) * s2 + (dwdz + dwdz) * s3;
       fde0 *= Visc;
       fde1 *= Visc;
       fde2 *= Visc;
-      double dxc0 = xn0 - xi0, dxc1 = xn1 - xi1, dxc2 = xn2 - xi2;
+      T dxc0 = xn0 - xi0, dxc1 = xn1 - xi1, dxc2 = xn2 - xi2;
       fdi0 = val * (dudx * dxc0 + dudy * dxc1 + dudz * dxc2);
       fdi1 = val * (dvdx * dxc0 + dvdy * dxc1 + dvdz * dxc2);
       fdi2 = val * (dwdx * dxc0 + dwdy * dxc1 + dwdz * dxc2);
@@ -538,23 +588,24 @@ __global__ void __launch_bounds__(kThreads) k_momentum(MomArgs a) {
     sv += fde1 - fdi1 - fcs1;
     sw += fde2 - fdi2 - fcs2;
   }
-  app /= a.urf0;
-  double apr = 1. / (app);
+  app /= (T)a.urf0;
+  T apr = T(1) / (app);
   a.Apr[i] = apr;
   a.dinv[i] = apr;
   a.A[a.c_diag[i]] = app;
-  double vol = a.c_vol[i];
-  double Ri = a.R[i];
-  a.bu[i] = su + (1. - a.urf0) * app * Ui + (-a.dP[3 * i] + Ri * a.g0) * vol;
-  a.bv[i] = sv + (1. - a.urf0) * app * Vi + (-a.dP[3 * i + 1] + Ri * a.g1) * vol;
-  a.bw[i] = sw + (1. - a.urf0) * app * Wi + (-a.dP[3 * i + 2] + Ri * a.g2) * vol;
-  a.old[i] = Ui;
-  a.old[N + i] = Vi;
-  a.old[2 * N + i] = Wi;
+  T vol = (T)a.c_vol[i];
+  T Ri = (T)a.R[i];
+  a.bu[i] = su + (T(1) - (T)a.urf0) * app * Ui + (-(T)a.dP[3 * i] + Ri * (T)a.g0) * vol;
+  a.bv[i] = sv + (T(1) - (T)a.urf0) * app * Vi + (-(T)a.dP[3 * i + 1] + Ri * (T)a.g1) * vol;
+  a.bw[i] = sw + (T(1) - (T)a.urf0) * app * Wi + (-(T)a.dP[3 * i + 2] + Ri * (T)a.g2) * vol;
+  a.old[i] = a.U[i];  // the FP64 field itself (the residual compares with it exactly)
+  a.old[N + i] = a.V[i];
+  a.old[2 * N + i] = a.W[i];
 }
 
 // ------------------------------------------------------------------ Rhie-Chow
-// CalRUFace2 (navier_velocity.cpp:425-477)
+// CalRUFace2 (navier_velocity.cpp:425-477); T as for k_gradient
+template <class T>
 __global__ void k_ruface2(int nfac, const int* __restrict__ f_c1, const int* __restrict__ f_c2,
                           const int* __restrict__ f_bnd, const double* __restrict__ f_n,
                           const double* __restrict__ f_area, const double* __restrict__ f_lambda,
@@ -569,38 +620,48 @@ __global__ void k_ruface2(int nfac, const int* __restrict__ f_c1, const int* __r
   if (i >= nfac) return;
   int c1 = f_c1[i], c2 = f_c2[i];
   const double* n = f_n + 3 * (long)i;
+  const T n0 = (T)n[0], n1 = (T)n[1], n2 = (T)n[2];
   if (c2 < 0) {
     int b = f_bnd[i];
-    double ro = BRo[b];
-    double ruf = BU[b] * ro, rvf = BV[b] * ro, rwf = BW[b] * ro;
-    RUFace[i] = ruf * n[0] + rvf * n[1] + rwf * n[2];
+    T ro = (T)BRo[b];
+    T ruf = (T)BU[b] * ro, rvf = (T)BV[b] * ro, rwf = (T)BW[b] * ro;
+    RUFace[i] = (double)(ruf * n0 + rvf * n1 + rwf * n2);
     return;
   }
-  double lam = f_lambda[i], lam2 = 1. - lam;
-  double R1 = R[c1], R2 = R[c2];
-  double rf = lam * R1 + lam2 * R2;
-  double ruf = lam * R1 * U[c1] + lam2 * R2 * U[c2];
-  double rvf = lam * R1 * V[c1] + lam2 * R2 * V[c2];
-  double rwf = lam * R1 * W[c1] + lam2 * R2 * W[c2];
-  double ru = ruf * n[0] + rvf * n[1] + rwf * n[2];
+  T lam = (T)f_lambda[i], lam2 = T(1) - lam;
+  T R1 = (T)R[c1], R2 = (T)R[c2];
+  T rf = lam * R1 + lam2 * R2;
+  T ruf = lam * R1 * (T)U[c1] + lam2 * R2 * (T)U[c2];
+  T rvf = lam * R1 * (T)V[c1] + lam2 * R2 * (T)V[c2];
+  T rwf = lam * R1 * (T)W[c1] + lam2 * R2 * (T)W[c2];
+  T ru = ruf * n0 + rvf * n1 + rwf * n2;
   const double* xp = f_xpac + 3 * (long)i;
   const double* xn = f_xnac + 3 * (long)i;
   const double* x1 = c_x + 3 * (long)c1;
   const double* x2 = c_x + 3 * (long)c2;
-  const double* g1 = dP + 3 * (long)c1;
-  const double* g2 = dP + 3 * (long)c2;
-  double P1 = P[c1] + vdot3(g1, xp[0] - x1[0], xp[1] - x1[1], xp[2] - x1[2]);
-  double P2 = P[c2] + vdot3(g2, xn[0] - x2[0], xn[1] - x2[1], xn[2] - x2[2]);
-  double dx0 = xn[0] - xp[0], dx1 = xn[1] - xp[1], dx2 = xn[2] - xp[2];
-  double d12 = sqrt(vdot3v(dx0, dx1, dx2, dx0, dx1, dx2));
-  double aprf = lam * Apr[c1] + lam2 * Apr[c2];
-  double vol = lam * c_vol[c1] + lam2 * c_vol[c2];
-  double dpx = lam * g1[0] + lam2 * g2[0];
-  double dpy = lam * g1[1] + lam2 * g2[1];
-  double dpz = lam * g1[2] + lam2 * g2[2];
-  double dpn = dpx * dx0 + dpy * dx1 + dpz * dx2;
-  ru -= rf * f_area[i] * aprf / d12 * vol * ((P2 - P1) - dpn);
-  RUFace[i] = ru;
+  const T g1[3] = {(T)dP[3 * (long)c1], (T)dP[3 * (long)c1 + 1], (T)dP[3 * (long)c1 + 2]};
+  const T g2[3] = {(T)dP[3 * (long)c2], (T)dP[3 * (long)c2 + 1], (T)dP[3 * (long)c2 + 2]};
+  const T xp0 = (T)xp[0], xp1 = (T)xp[1], xp2 = (T)xp[2], xn0 = (T)xn[0], xn1 = (T)xn[1], xn2 = (T)xn[2];
+  T P1, P2;
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32: the two face pressures relative to P[c1], the cell difference taken in FP64 (only
+    // P2 - P1 enters the flux, and P itself carries an offset that would swamp it in FP32)
+    P1 = tdot3<T>(g1, xp0 - (T)x1[0], xp1 - (T)x1[1], xp2 - (T)x1[2]);
+    P2 = (T)(P[c2] - P[c1]) + tdot3<T>(g2, xn0 - (T)x2[0], xn1 - (T)x2[1], xn2 - (T)x2[2]);
+  } else {
+    P1 = (T)P[c1] + tdot3<T>(g1, xp0 - (T)x1[0], xp1 - (T)x1[1], xp2 - (T)x1[2]);
+    P2 = (T)P[c2] + tdot3<T>(g2, xn0 - (T)x2[0], xn1 - (T)x2[1], xn2 - (T)x2[2]);
+  }
+  T dx0 = xn0 - xp0, dx1 = xn1 - xp1, dx2 = xn2 - xp2;
+  T d12 = sqrt(tdot3v<T>(dx0, dx1, dx2, dx0, dx1, dx2));
+  T aprf = lam * (T)Apr[c1] + lam2 * (T)Apr[c2];
+  T vol = lam * (T)c_vol[c1] + lam2 * (T)c_vol[c2];
+  T dpx = lam * g1[0] + lam2 * g2[0];
+  T dpy = lam * g1[1] + lam2 * g2[1];
+  T dpz = lam * g1[2] + lam2 * g2[2];
+  T dpn = dpx * dx0 + dpy * dx1 + dpz * dx2;
+  ru -= rf * (T)f_area[i] * aprf / d12 * vol * ((P2 - P1) - dpn);
+  RUFace[i] = (double)ru;
 }
 
 // ------------------------------------------------------------------ pressure correction
@@ -1205,8 +1266,9 @@ void launch_bc_deltap(const DevMesh& m, const DevFields& f, cudaStream_t s) {
   if (m.nbnd > 0) ++g_launch_count, k_bc_copy<<<blocks_for(m.nbnd), kThreads, 0, s>>>(m.nbnd, m.b_face, m.f_c1, f.dp, f.BPre);
 }
 
-void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
-                     double* const* grad, cudaStream_t s) {
+template <class T>
+void launch_gradient_t(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
+                       double* const* grad, cudaStream_t s) {
   if (nfield == 4) {
     GradArgs<4> a;
     for (int q = 0; q < 4; q++) {
@@ -1214,7 +1276,7 @@ void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, con
       a.bphi[q] = bphi[q];
       a.grad[q] = grad[q];
     }
-    ++g_launch_count, k_gradient<4><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2, m.f_bnd,
+    ++g_launch_count, k_gradient<T, 4><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2, m.f_bnd,
                                                           m.f_lambda, m.f_n, m.c_vol, a);
   } else {
     for (int q = 0; q < nfield; q++) {
@@ -1222,14 +1284,20 @@ void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, con
       a.phi[0] = phi[q];
       a.bphi[0] = bphi[q];
       a.grad[0] = grad[q];
-      ++g_launch_count, k_gradient<1><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2,
+      ++g_launch_count, k_gradient<T, 1><<<blocks_for(m.ncel), kThreads, 0, s>>>(m.ncel, m.c_nface, m.c_gface, m.f_c1, m.f_c2,
                                                             m.f_bnd, m.f_lambda, m.f_n, m.c_vol, a);
     }
   }
 }
 
+void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
+                     double* const* grad, cudaStream_t s, bool fp32) {
+  if (fp32) launch_gradient_t<float>(m, nfield, phi, bphi, grad, s);
+  else launch_gradient_t<double>(m, nfield, phi, bphi, grad, s);
+}
+
 void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, const double* gravity,
-                     DevStatus* st, cudaStream_t s, const TimeConf& tc) {
+                     DevStatus* st, cudaStream_t s, const TimeConf& tc, bool fp32) {
   MomArgs a;
   a.Unp = f.Unp;
   a.Vnp = f.Vnp;
@@ -1279,13 +1347,15 @@ void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, co
   a.g1 = gravity[1];
   a.g2 = gravity[2];
   a.warn = &st->warn_inlet;
-  ++g_launch_count, k_momentum<<<blocks_for(m.ncel), kThreads, 0, s>>>(a);
+  if (fp32) ++g_launch_count, k_momentum<float><<<blocks_for(m.ncel), kThreads, 0, s>>>(a);
+  else ++g_launch_count, k_momentum<double><<<blocks_for(m.ncel), kThreads, 0, s>>>(a);
 }
 
-void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s) {
-  ++g_launch_count, k_ruface2<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.f_n, m.f_area, m.f_lambda,
-                                                    m.f_xpac, m.f_xnac, m.c_x, m.c_vol, f.R, f.U, f.V, f.W, f.P,
-                                                    f.Apr, f.dPdX, f.BRo, f.BU, f.BV, f.BW, f.RUFace);
+void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s, bool fp32) {
+  auto k = fp32 ? k_ruface2<float> : k_ruface2<double>;
+  ++g_launch_count, k<<<blocks_for(m.nfac), kThreads, 0, s>>>(m.nfac, m.f_c1, m.f_c2, m.f_bnd, m.f_n, m.f_area, m.f_lambda,
+                                            m.f_xpac, m.f_xnac, m.c_x, m.c_vol, f.R, f.U, f.V, f.W, f.P, f.Apr,
+                                            f.dPdX, f.BRo, f.BU, f.BV, f.BW, f.RUFace);
 }
 
 void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s) {

@@ -145,8 +145,12 @@ struct cycas_ctx {
   bool use_graph = false;
   cudaGraphExec_t gexec = nullptr;
   long long graph_launches = 0;  // kernels of one replay
-  // mixed precision (GMRES systems): FP32 copies of the system being solved
+  // mixed precision: FP32 Arnoldi cycles in the GMRES systems, with FP32 copies of the system
+  // being solved; at level 2 also FP32 arithmetic in the gradients, the momentum rows and the
+  // Rhie-Chow face flux (storage stays FP64; the pressure-correction rows and their
+  // mass-imbalance sum, the corrections and the residuals stay FP64)
   bool mixed = false;
+  bool fp32_assembly = false;  // mixed level 2
   double inner_rtol = 1e-4;
   float* val32 = nullptr;   // [nnz]
   float* dinv32 = nullptr;  // [ncel]
@@ -574,7 +578,9 @@ void init_ctx(cycas_ctx& c, const cycas_params* p, const cycas_options* o) {
     c.ksp[s].rtol = k.rtol > 0 ? k.rtol : kRefRtol[s];
     c.ksp[s].maxit = k.maxit > 0 ? k.maxit : kRefMaxit[s];
   }
+  require(o->mixed >= 0 && o->mixed <= 2, "mixed must be 0, 1 or 2");
   c.mixed = o->mixed != 0;
+  c.fp32_assembly = o->mixed == 2;
   c.inner_rtol = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
   require(o->amg_omega <= 1.0f && o->amg_alpha <= 2.0f && o->amg_gamma >= 0 && o->amg_gamma <= 4,
           "AMG options out of range (omega <= 1, alpha <= 2, gamma 0..4)");
@@ -730,18 +736,18 @@ void grad_uvwp(cycas_ctx& c) {
   const double* phi[4] = {c.f.U, c.f.V, c.f.W, c.f.P};
   const double* bphi[4] = {c.f.BU, c.f.BV, c.f.BW, c.f.BPre};
   double* g[4] = {c.f.dUdX, c.f.dVdX, c.f.dWdX, c.f.dPdX};
-  launch_gradient(c.m, 4, phi, bphi, g, c.stream);
+  launch_gradient(c.m, 4, phi, bphi, g, c.stream, c.fp32_assembly);
 }
 
 void grad1(cycas_ctx& c, const double* phi, const double* bphi, double* g) {
-  launch_gradient(c.m, 1, &phi, &bphi, &g, c.stream);
+  launch_gradient(c.m, 1, &phi, &bphi, &g, c.stream, c.fp32_assembly);
 }
 
 // BuildVelocityMatrix (navier_velocity.cpp:63-393)
 void build_velocity(cycas_ctx& c) {
   bc_velocity(c, true);
   grad_uvwp(c);
-  launch_momentum(c.m, c.f, c.urf, c.gravity, c.st, c.stream, c.tc);
+  launch_momentum(c.m, c.f, c.urf, c.gravity, c.st, c.stream, c.tc, c.fp32_assembly);
 }
 
 // CalculateVelocity (navier_velocity.cpp:10-60)
@@ -767,7 +773,7 @@ void build_pressure(cycas_ctx& c) {
 // with the Jacobi preconditioner at the pressure system's tolerances.
 void calculate_pressure(cycas_ctx& c) {
   bc_velocity(c, false);
-  launch_ruface2(c.m, c.f, c.stream);
+  launch_ruface2(c.m, c.f, c.stream, c.fp32_assembly);
   build_pressure(c);
   if (c.density == 1) {
     KspConf k = c.ksp[CYCAS_SYS_PRESSURE];

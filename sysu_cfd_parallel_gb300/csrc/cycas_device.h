@@ -143,11 +143,13 @@ struct DevBatch {
 void launch_bc_velocity(const DevMesh& m, const DevFields& f, int density_model, bool set_pressure,
                         cudaStream_t s, const DevBatch* b = nullptr);
 void launch_bc_deltap(const DevMesh& m, const DevFields& f, cudaStream_t s);
+// fp32: the arithmetic in FP32 (mixed-precision contexts; storage stays FP64), else FP64 and
+// bit-exact with the reference
 void launch_gradient(const DevMesh& m, int nfield, const double* const* phi, const double* const* bphi,
-                     double* const* grad, cudaStream_t s);
+                     double* const* grad, cudaStream_t s, bool fp32 = false);
 void launch_momentum(const DevMesh& m, const DevFields& f, const double* urf, const double* gravity,
-                     DevStatus* st, cudaStream_t s, const TimeConf& tc = TimeConf());
-void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s);
+                     DevStatus* st, cudaStream_t s, const TimeConf& tc = TimeConf(), bool fp32 = false);
+void launch_ruface2(const DevMesh& m, const DevFields& f, cudaStream_t s, bool fp32 = false);
 void launch_pressure(const DevMesh& m, const DevFields& f, cudaStream_t s);
 // compressible (perfect-gas) pressure-correction rows (navier_pressure.cpp:106-224, DensityModel 1)
 void launch_pressure_gas(const DevMesh& m, const DevFields& f, const TimeConf& tc, cudaStream_t s);

@@ -7,7 +7,7 @@ mu 0.01, lid velocity (1,0,0), no-slip walls, Re 100, the reference's relaxation
 n = 48 (110,592 cells, 14x the 20^3 case), solved from the initial field until ResMax < 1e-6
 (NSSolve's stop test, navier.cpp:141-145; 213 iterations at 20^3, about 880 at 48^3).  FP64
 SIMPLE-C with the reference's Krylov tolerances: GMRES(30) rtol 1e-8 for u, v, w preconditioned
-by a Jacobi-Neumann polynomial of degree GMRES_POLY, CG rtol 1e-6 for the pressure correction
+by a Jacobi-Neumann polynomial of degree CAVITY_POLY, CG rtol 1e-6 for the pressure correction
 preconditioned by one aggregation-AMG cycle.  Every step starts from the same in-HBM restart
 point (cycas_restart_point), so the K steps are K identical solves.
 
@@ -53,7 +53,8 @@ HEADLINE_METRIC = "cell-iters/s to 1e-6 resid (steady SIMPLE-C, plain FP64, lid-
 # channel: degree 2 39.8, 3 34.6, 4 32.7, 5 31.3, 6 32.9); batches of small cases (the cavity
 # sample, the serving stream), whose systems converge in a few iterations anyway, at 1 to 3
 # (degrees 1/2/3/5 on the 32-cavity batch: 73.5/73.8/74.1/69.3 M cell-iters/s).
-GMRES_POLY = 5
+GMRES_POLY = 5    # the k-epsilon channel (and its precision workload)
+CAVITY_POLY = 2   # the cavity headline: measured 1826.7 ms per solve against 1896.1 ms for degree 5
 BATCH_POLY = 2
 
 
@@ -249,7 +250,7 @@ def cavity_case(n: int = CAVITY_N) -> str:
 
 def headline_options(local: int, mixed: bool = False):
     from sysu_cfd_parallel_gb300 import capi
-    opt = gmres_pc(capi.default_options(pc=capi.PC_JACOBI, device=local))
+    opt = gmres_pc(capi.default_options(pc=capi.PC_JACOBI, device=local), CAVITY_POLY)
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
     opt.mixed = 1 if mixed else 0
     return opt
@@ -943,7 +944,7 @@ def run_gpu(args):
     per_sys_bytes = {"cg": 0.0, "gmres_vel": 0.0, "gmres_scalar": 0.0}
     per_sys_launch = {"cg": 0, "gmres_vel": 0, "gmres_scalar": 0}
     for row in last["ksp_its"]:
-        for kind, slot, its, b in krylov_bytes(row, turb, n, nnz, levels=levels, poly=GMRES_POLY):
+        for kind, slot, its, b in krylov_bytes(row, turb, n, nnz, levels=levels, poly=CAVITY_POLY):
             key = "cg" if kind == "cg" else ("gmres_vel" if slot < 3 else "gmres_scalar")
             per_sys_bytes[key] += b * args.steps
             per_sys_launch[key] += args.steps
@@ -1014,7 +1015,7 @@ def run_gpu(args):
                        "final_resmax": float(last["resmax"][-1]),
                        "parallelism": f"replicas{world}", "l2": "solve working set < 129 MB L2 (L2-resident), no flush",
                        "krylov": "GMRES(30) rtol 1e-8 with the Jacobi-Neumann polynomial preconditioner of degree %d "
-                                 "(u,v,w), CG rtol 1e-6 + AMG cycle (p'), the reference's tolerances" % GMRES_POLY,
+                                 "(u,v,w), CG rtol 1e-6 + AMG cycle (p'), the reference's tolerances" % CAVITY_POLY,
                        "krylov_its_first_iteration": [int(x) for x in last["ksp_its"][0]],
                        "krylov_its_last_iteration": [int(x) for x in last["ksp_its"][-1]],
                        "amg_levels_rows": [int(x) for x in levels[0]]},
@@ -1322,7 +1323,8 @@ def run_profile(args):
     opt.amg_omega = args.amg_omega
     opt.amg_gamma = args.amg_gamma
     gpc = {"jacobi": capi.PC_JACOBI, "poly1": capi.PC_POLY1, "poly2": capi.PC_POLY2, "poly3": capi.PC_POLY3,
-           "poly4": capi.PC_POLY4, "poly5": capi.PC_POLY5}[args.gmres_pc]
+           "poly4": capi.PC_POLY4, "poly5": capi.PC_POLY5}[
+        args.gmres_pc or "poly%d" % (GMRES_POLY if args.kind == "channel" else CAVITY_POLY)]
     opt.ksp[capi.SYS_VELOCITY].pc = gpc
     opt.ksp[capi.SYS_SCALAR].pc = gpc
     s = NavierStokesSolver(Case(param), opt)
@@ -1371,7 +1373,8 @@ def main():
     ap.add_argument("--nz", type=int, default=10)
     ap.add_argument("--side", type=int, default=CAVITY_N, help="cavity cells per side")
     ap.add_argument("--pressure-pc", default="amg", choices=["amg", "jacobi"])
-    ap.add_argument("--gmres-pc", default="poly5", choices=["jacobi", "poly1", "poly2", "poly3", "poly4", "poly5"])
+    ap.add_argument("--gmres-pc", default=None, choices=["jacobi", "poly1", "poly2", "poly3", "poly4", "poly5"],
+                    help="profile workload: GMRES preconditioner (default: the workload's bench setting)")
     ap.add_argument("--amg-omega", type=float, default=0.0, help="AMG smoother weight (0: library default)")
     ap.add_argument("--amg-gamma", type=int, default=0, help="AMG cycles at the first shared-memory level")
     ap.add_argument("--jitter", type=float, default=0.0, help="interior node jitter (fraction of h)")

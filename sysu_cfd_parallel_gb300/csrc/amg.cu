@@ -252,8 +252,8 @@ __device__ __forceinline__ float sell_row(const int* sp, const unsigned short* c
   return s;
 }
 
-// pre-smoothing and restriction: X_l = w D^-1 R_l, T_l = R_l - A_l X_l, R_{l+1} = P^T T_l.  The
-// residual takes w D^-1 R of the neighbours directly, so X needs no pass (and sync) of its own.
+// pre-smoothing and restriction: X_l = w D^-1 R_l, T_l = R_l - A_l X_l, R_{l+1} = P^T T_l.  X is
+// written in a pass of its own, so the residual gathers one shared-memory value per entry.
 __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned char* sb, int l) {
   const int tid = threadIdx.x;
   const TailLevelOff& o = T.lv[l];
@@ -266,11 +266,11 @@ __device__ void tail_down(const AmgDevLevel* L, const TailLayout& T, unsigned ch
   float* X = sat<float>(o.X);
   float* Tt = sat<float>(o.T);
   const unsigned short* pm = sat<unsigned short>(o.perm);
-  for (int p = tid; p < n; p += kGmThreads) {
+  for (int i = tid; i < n; i += kGmThreads) X[i] = wd[i] * R[i];
+  __syncthreads();
+  for (int p = tid; p < n; p += kGmThreads) {  // one shared-memory gather per entry
     const int i = pm[p];
-    const float ri = R[i];
-    X[i] = wd[i] * ri;
-    Tt[i] = ri - sell_row(rp, cl, va, p, [&](int j) { return wd[j] * R[j]; });
+    Tt[i] = R[i] - sell_row(rp, cl, va, p, [&](int j) { return X[j]; });
   }
   __syncthreads();
   const int* pp = sat<int>(o.ptptr);

@@ -176,8 +176,8 @@ __device__ __forceinline__ T* at(unsigned char* sb, int off) {
   return reinterpret_cast<T*>(sb + off);
 }
 
-// the kernel's dynamic shared memory, named at file scope so that the tail functions (one of
-// them out of line) address it as shared memory rather than through generic pointers
+// the kernel's dynamic shared memory, named at file scope so that the tail functions address it
+// as shared memory rather than through generic pointers
 extern __shared__ __align__(16) unsigned char amg_smem[];
 template <class T>
 __device__ __forceinline__ T* sat(int off) {
@@ -350,7 +350,7 @@ __device__ void tail_v(const AmgDevLevel* L, int nlev, const TailLayout& T, floa
 // coarse correction cuts the outer CG iterations; g moves further down while its level has
 // more than kAmgWLevelRows rows.  `buf` holds the accumulated x and the original r_g (2 n_g
 // floats).
-__device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma,
+__device__ void tail_cycle(const AmgDevLevel* L, int nlev, const TailLayout& T, float alpha, int gamma,
                                         unsigned char* sb, float* buf, int r0, int r1, int lo, double* z) {
   const int tid = threadIdx.x;
   const int t0 = T.tail;
@@ -403,22 +403,25 @@ __device__ __noinline__ void tail_cycle(const AmgDevLevel* L, int nlev, const Ta
 }
 
 // level l -> l+1 on the team: each member takes a block of coarse rows, computes the smoothed
-// residual t_i = r_i - A_i (w D^-1 r) of their fine rows (in aggregate order) into shared
-// memory and sums each aggregate: r_{l+1} = P^T t.  Only r_l is read, so no barrier separates
-// smoothing from restriction.
-__device__ __forceinline__ void grid_down(const AmgDevLevel& F, const AmgDevLevel& C, const Team& Tm, float* buf) {
+// residual t_i = r_i - A_i (w D^-1 r) of their fine rows (in aggregate order; w D^-1 r is kept
+// per row, so an entry gathers one value) into shared memory and into F.sr (for the way up), and
+// sums each aggregate: r_{l+1} = P^T t, with w D^-1 r_{l+1} when level l+1 is cycled by the grid
+// too (c_grid).  Only r_l is read, so no barrier separates smoothing from restriction.
+__device__ __forceinline__ void grid_down(const AmgDevLevel& F, const AmgDevLevel& C, bool c_grid, const Team& Tm,
+                                          float* buf) {
   const Rows cr = share(0, C.n, Tm);
   const int G = max(1, kAmgDownBuf / max(1, F.maxagg));
   const float* rl = F.r;
-  const float* wd = F.wdinv;
+  const float* wr = F.wr;
   for (int I0 = cr.r0; I0 < cr.r1; I0 += G) {
     const int I1 = min(I0 + G, cr.r1);
     const int k0 = __ldg(F.ptptr + I0), k1 = __ldg(F.ptptr + I1);
     for (int k = k0 + threadIdx.x; k < k1; k += kGmThreads) {
       const int i = __ldg(F.ptrow + k);
       const float ri = ldcgf(rl + i);
-      float acc = row_gather_f<8>(F.rowptr, F.col, F.val, i, [&](int j) { return __ldg(wd + j) * ldcgf(rl + j); });
+      const float acc = row_gather_f<8>(F.rowptr, F.col, F.val, i, [&](int j) { return ldcgf(wr + j); });
       buf[k - k0] = ri - acc;
+      F.sr[i] = ri - acc;
     }
     __syncthreads();
     for (int I = I0 + threadIdx.x; I < I1; I += kGmThreads) {
@@ -426,28 +429,26 @@ __device__ __forceinline__ void grid_down(const AmgDevLevel& F, const AmgDevLeve
       float s = 0.0f;
       for (int q = q0; q < q1; q++) s += buf[q - k0];
       C.r[I] = s;
+      if (c_grid) C.wr[I] = __ldg(C.wdinv + I) * s;
     }
     __syncthreads();
   }
 }
 
 // prolongation of the coarse correction and post-smoothing on rows rw of a level:
-// out = y + w D^-1 (r - A y),  y = w D^-1 r + a P x_C; level 0 writes the FP64 z.  xc(I) reads
-// the coarse correction of coarse row I (from global memory, or from the tail in shared memory)
+// out = y + w D^-1 (r - A y),  y = w D^-1 r + a P x_C; level 0 writes the FP64 z.  With
+// t = r - A w D^-1 r kept from the way down (F.sr), r - A y = t - a A P x_C, so an entry gathers
+// only the coarse correction of its column's aggregate (F.aggcol).  xc(I) reads the coarse
+// correction of coarse row I (from global memory, or from the tail in shared memory)
 template <class XC>
 __device__ __forceinline__ void grid_up(const AmgDevLevel& F, XC xc, float alpha, Rows rw, float* outf,
                                         double* outd) {
-  const float* rl = F.r;
-  const float* wd = F.wdinv;
   const int* agg = F.agg;
   for (int i = rw.r0 + threadIdx.x; i < rw.r1; i += kGmThreads) {
-    const float ri = ldcgf(rl + i);
-    const float wi = __ldg(wd + i);
-    const float y = wi * ri + alpha * xc(__ldg(agg + i));
-    float acc = row_gather_f<8>(F.rowptr, F.col, F.val, i, [&](int j) {
-      return __ldg(wd + j) * ldcgf(rl + j) + alpha * xc(__ldg(agg + j));
-    });
-    const float o = y + wi * (ri - acc);
+    const float wi = __ldg(F.wdinv + i);
+    const float y = ldcgf(F.wr + i) + alpha * xc(__ldg(agg + i));
+    const float acc = row_gather_f<8>(F.rowptr, F.aggcol, F.val, i, [&](int J) { return xc(J); });
+    const float o = y + wi * (ldcgf(F.sr + i) - alpha * acc);
     if (outd) outd[i] = (double)o;
     else outf[i] = o;
   }
@@ -460,7 +461,7 @@ __device__ bool vcycle(const AmgDevLevel* L, int nlev, const TailLayout& T, floa
                        float* buf, int lo, int hi, double* z, const Team& Tm, int* err) {
   const int t0 = T.tail;
   for (int l = 0; l < t0; l++) {
-    grid_down(L[l], L[l + 1], Tm, buf);
+    grid_down(L[l], L[l + 1], l + 1 < t0, Tm, buf);
     if (!grid_barrier(Tm.bar, Tm.size, err)) return false;
   }
   const Rows own = share(lo, hi, Tm);
@@ -515,6 +516,8 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
   double* mypart = Tm.part + (long)Tm.rank * stride;
   const float alc = a.alpha;
   float* r32 = s_lv[0].r;
+  float* wr32 = s_lv[0].wr;
+  const float* wd32 = s_lv[0].wdinv;
 
   // initial residual r = b - A x (or b); the V-cycle input is its FP32 copy
   for (int r = own.r0 + tid; r < own.r1; r += kGmThreads) {
@@ -530,6 +533,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
     }
     a.r[r] = t;
     r32[r] = (float)br;
+    wr32[r] = wd32[r] * (float)br;
   }
   if (!grid_barrier(Tm.bar, Tm.size, a.err)) return;
   if (!a.guess_zero) {  // |M b| is the reference norm of a nonzero initial guess
@@ -539,6 +543,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
       const double zb = ldcg(a.u + r);
       acc[0] += zb * zb;
       r32[r] = (float)ldcg(a.r + r);
+      wr32[r] = wd32[r] * r32[r];
     }
     block_reduce<1>(acc, s_warp, s_red);
     if (tid == 0) mypart[kMaxRestart + 3] = s_red[0];
@@ -645,6 +650,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
         X[r0] = x0 + alpha * pn0;
         R[r0] = rn0;
         r32[r0] = (float)rn0;
+        wr32[r0] = wd32[r0] * (float)rn0;
         if (h1) {
           const double pn1 = u1 + beta * p1, sn1 = w1 + beta * s1, rn1 = q1 - alpha * sn1;
           P[r1] = pn1;
@@ -652,6 +658,7 @@ __device__ void cg_amg_team(const CgAmgArgs& a, const Team& Tm, int c) {
           X[r1] = x1 + alpha * pn1;
           R[r1] = rn1;
           r32[r1] = (float)rn1;
+          wr32[r1] = wd32[r1] * (float)rn1;
         }
       }
     }

@@ -353,6 +353,16 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
     d.wdinv = up.alloc_float(std::max(1, nrows[l]));
     float* d_r = up.alloc_float(std::max(1, nrows[l]));
     float* d_t = l == 0 ? nullptr : up.alloc_float(std::max(1, nrows[l]));
+    float* d_wr = up.alloc_float(std::max(1, nrows[l]));
+    float* d_sr = up.alloc_float(std::max(1, nrows[l]));
+    // agg[col[k]] of every entry of the depth (cases without a coarser level: unused zeros)
+    std::vector<int> ac(std::max(1, nnzs[l]), 0);
+    for (int c = 0; c < nc; c++) {
+      if ((int)H(c).lv.size() <= l + 1) continue;
+      const AmgHostLevel& L = H(c).lv[l];
+      for (int k = 0; k < L.nnz; k++) ac[nnz_off[l][c] + k] = L.agg[L.col[k]];
+    }
+    const int* d_ac = up.upload_int(ac.data(), (long)ac.size());
     const int* d_ag = up.upload_int(ag.data(), (long)ag.size());
     const int* d_pp = pp.empty() ? nullptr : up.upload_int(pp.data(), (long)pp.size());
     const int* d_pr = pr.empty() ? nullptr : up.upload_int(pr.data(), (long)pr.size());
@@ -379,6 +389,9 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
         e.agg = d_ag;
         e.r = d_r;
         e.t = nullptr;
+        e.wr = d_wr;
+        e.sr = d_sr;
+        e.aggcol = d_ac;
       } else {
         e.nnz_off = nnz_off[l][c];
         e.rowptr = d_rp + rp_off[l][c];
@@ -389,6 +402,9 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
         e.agg = d_ag + row_off[l][c];
         e.r = d_r + row_off[l][c];
         e.t = d_t + row_off[l][c];
+        e.wr = d_wr + row_off[l][c];
+        e.sr = d_sr + row_off[l][c];
+        e.aggcol = d_ac + nnz_off[l][c];
       }
       e.ptptr = pt_off[l][c] >= 0 ? d_pp + pt_off[l][c] : nullptr;
       e.ptrow = ptr_off[l][c] >= 0 ? d_pr + ptr_off[l][c] : nullptr;

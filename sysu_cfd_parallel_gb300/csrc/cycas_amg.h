@@ -61,6 +61,12 @@ struct AmgDevLevel {
   const int* ptrow;   // rows of each aggregate (level 0: global rows)
   float* r;           // residual (level 0: FP32 copy of the CG residual, global rows)
   float* t;           // correction returned to the finer level (levels >= 1)
+  // levels cycled by the grid (above the shared-memory tail): w D^-1 r of every row, the
+  // smoothed residual r - A w D^-1 r kept from the way down for the way up, and the next level's
+  // row of each entry's column (agg[col[k]]), so that each pass gathers one value per entry
+  float* wr;
+  float* sr;
+  const int* aggcol;  // level 0: by the system's entry positions
   // levels of the shared-memory tail (else null): the pattern in SELL-32 layout -- rows ordered
   // by length (longest first) and cut into slices of 32 positions, a slice column-major and
   // padded to its longest row, so the 32 lanes of a warp read entry k of 32 rows from

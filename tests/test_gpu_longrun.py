@@ -4,8 +4,9 @@
   GMRES(30) rtol 1e-8 on every system and Jacobi preconditioning, against the fixture the
   reference's own sources wrote (tests/golden/cavity20/ref_jacobi.npz): residual history to
   relative 1e-6, u, v, w, p to relative L2 1e-8, Krylov counts within one.
-* The same cavity with the headline's preconditioners (Jacobi-Neumann polynomial of degree 5 for
-  the momentum GMRES, CG + aggregation AMG for the pressure correction) against the oracle with
+* The same cavity with the headline's preconditioners (Jacobi-Neumann polynomial of degree 2 for
+  the momentum GMRES -- and degree 5, the channel's -- CG + aggregation AMG for the pressure
+  correction) against the oracle with
   the reference's ILU(0), every system solved tightly on both sides (rtol 1e-12; 1e-10 for the
   pressure correction, whose singular pure-Neumann system ILU(0)-CG cannot take further in FP64):
   with the Krylov error made negligible the SIMPLE iterations must coincide whatever the
@@ -60,13 +61,14 @@ def test_cavity20_configured_run_matches_reference_build(tmp_path):
     s.close()
 
 
-def test_cavity20_headline_preconditioners_match_oracle_ilu(tmp_path):
+@pytest.mark.parametrize("poly", [2, 5])
+def test_cavity20_headline_preconditioners_match_oracle_ilu(tmp_path, poly):
     param = _cavity20(tmp_path)
     o = po.OracleCase(param)
     rtol = {po.VELOCITY: 1e-12, po.PRESSURE: 1e-10, po.SCALAR: 1e-12}
     for w in (po.VELOCITY, po.PRESSURE, po.SCALAR):
         o.set_ksp(w, po.PC_ILU0, 30, rtol[w], 5000)
-    opt = capi.default_options(pc=capi.PC_POLY5)
+    opt = capi.default_options(pc={2: capi.PC_POLY2, 5: capi.PC_POLY5}[poly])
     opt.ksp[capi.SYS_PRESSURE].pc = capi.PC_AMG
     for k in range(3):
         opt.ksp[k].rtol = rtol[k]

@@ -580,6 +580,8 @@ def run_serve(args):
     opt.mixed = 1 if args.mixed else 0
     srv = Server(hbm_budget_gb=args.budget_gb, residual_tol=args.tol, max_iters=args.max_iters, options=opt)
     srv.set_graph(True)
+    # requests keep arriving: the next batch is built while the current one iterates
+    srv.set_async_rebuild(not args.sync_rebuild)
     if args.max_cells > 0:
         srv.set_max_cells(args.max_cells)
     t0 = Server.clock()
@@ -615,7 +617,7 @@ def run_serve(args):
                                f"channels m={args.channel_m}; tol {args.tol}; cap {args.max_iters} iterations; "
                                f"budget {args.budget_gb} GB; active-cell cap {args.max_cells:g}; "
                                f"drain {args.drain}s",
-                   "mixed": bool(args.mixed)},
+                   "mixed": bool(args.mixed), "batch_rebuilds": "in line" if args.sync_rebuild else "worker thread"},
     }
     print(json.dumps(line), flush=True)
     srv.close()
@@ -1376,6 +1378,8 @@ def main():
     ap.add_argument("--max-cells", type=float, default=4e6,
                     help="serve workload: cap on the active requests' cells (0: HBM budget only)")
     ap.add_argument("--mixed", action="store_true")
+    ap.add_argument("--sync-rebuild", action="store_true",
+                    help="serve workload: rebuild batches in line instead of on a worker thread")
     ap.add_argument("--serve-seed", type=int, default=5)
     ap.add_argument("--outer-rtol", type=float, default=1e-10, help="precision workload: rtol of every system")
     # --workload profile: the generated case and its solver options

@@ -452,6 +452,14 @@ int cycas_server_set_graph(cycas_server* s, int32_t on);
  * each step short and lets admitted requests finish in arrival order instead of every request
  * advancing slowly in one huge batch.  No counterpart in the reference. */
 int cycas_server_set_max_cells(cycas_server* s, double max_cells);
+/* Batch rebuilds on a worker thread (on = 1): while the next batch of a class is built, the
+ * current one keeps iterating its members, and the server switches at the first step after the
+ * build (newly admitted requests wait for it).  The build's kernels and copies then share the GPU
+ * with the iterations' cooperative kernels, which occupy every SM, so a build takes several
+ * times longer: worth it when requests keep arriving (the Poisson stream: 37.5 M instead of
+ * 28.5 M cell-iters/s), not for a fixed set submitted at once (256 cavities: 61.8 s instead of
+ * 50.6 s).  Default off.  No counterpart in the reference. */
+int cycas_server_set_async_rebuild(cycas_server* s, int32_t on);
 double cycas_server_clock(void);
 /* queues a request; CYCAS_ERR_UNSUPPORTED for transient, energy or perfect-gas cases (batches
  * hold steady, isothermal, constant-density cases) */

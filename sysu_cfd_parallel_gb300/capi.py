@@ -95,6 +95,7 @@ EXPORTS = (
     "cycas_reset_profile", "cycas_csr_solve_noalloc", "cycas_get_amg_levels", "cycas_batch_create",
     "cycas_batch_size", "cycas_batch_offsets", "cycas_batch_iteration", "cycas_batch_residuals",
     "cycas_batch_copy_case", "cycas_batch_case_field", "cycas_server_create", "cycas_server_destroy", "cycas_server_set_graph", "cycas_server_set_max_cells",
+    "cycas_server_set_async_rebuild",
     "cycas_server_clock", "cycas_server_submit", "cycas_server_step", "cycas_server_poll",
     "cycas_server_result_field", "cycas_server_last_error", "cycas_server_stats", "cycas_footprint_estimate",
     "cycas_set_graph", "cycas_batch_autotune",
@@ -181,6 +182,7 @@ def load(build_if_missing: bool = True):
     L.cycas_server_create.argtypes = [C.POINTER(Options), C.c_double, C.c_double, C.c_int32, C.c_int32, C.POINTER(_P)]
     L.cycas_server_set_graph.argtypes = [_P, C.c_int32]
     L.cycas_server_set_max_cells.argtypes = [_P, C.c_double]
+    L.cycas_server_set_async_rebuild.argtypes = [_P, C.c_int32]
     L.cycas_server_destroy.argtypes = [_P]
     L.cycas_server_destroy.restype = None
     L.cycas_server_clock.argtypes = []

@@ -12,7 +12,10 @@
 //      of a busy server would spend most of its time rebuilding);
 //   2. rebuilds the batch of every physics class whose membership changed (cases of one batch
 //      share the turbulence model and relaxation factors), moving the state of the cases that
-//      stay from the old batch to the new one on the device;
+//      stay from the old batch to the new one on the device.  With cycas_server_set_async_rebuild
+//      the new batch is built on a worker thread while the old one keeps iterating its members,
+//      and the server switches to it at the first step after it is ready (newly admitted cases
+//      start iterating then);
 //   3. advances every active case by one SIMPLE-C iteration (one batch iteration per class);
 //   4. retires every case whose residual, max_i localRes[i] divided by the case's volume, is
 //      at or below the tolerance, that reached the iteration cap, or whose fields stopped being
@@ -28,6 +31,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <future>
 #include <map>
 #include <memory>
 #include <numeric>
@@ -56,7 +60,19 @@ struct Request {
   double resmax = 0.0;
   int status = 0;  // CYCAS_REQ_*
   std::map<std::string, std::vector<double>> fields;
+  int in_build = 0;         // batches being built from this request's case
+  bool free_case = false;   // free cs once no build reads it
 };
+
+void release_case(Request* r) {
+  if (r->cs && r->in_build == 0) {
+    cycas_case_free(r->cs);
+    r->cs = nullptr;
+    r->free_case = false;
+  } else if (r->cs) {
+    r->free_case = true;
+  }
+}
 
 }  // namespace
 
@@ -75,6 +91,7 @@ struct cycas_server {
   int max_iters = 10000;
   int keep_fields = 0;
   int graph = 0;  // replay every batch's iterations as one CUDA graph (cycas_server_set_graph)
+  int async = 0;  // build new batches on a worker thread (cycas_server_set_async_rebuild)
   double max_cells = 0.0;  // cap on the cells of the active requests (0: none), cycas_server_set_max_cells
   double active_cells = 0.0;
   int64_t next_id = 1;
@@ -86,6 +103,16 @@ struct cycas_server {
     bool dirty = false;
     double cells = 0.0, retired_cells = 0.0;  // of the batch, and of its retired members
     double retired_footprint = 0.0;           // released from the budget at the next rebuild
+    // the next batch, built on a worker thread from a snapshot of the active cases
+    struct Build {
+      std::future<int> done;
+      cycas_ctx* ctx = nullptr;
+      std::vector<Request*> members;
+      double seconds = 0.0;  // host time of the build
+      std::string error;
+      bool admitted = false;  // started for newly admitted requests (admission pacing)
+    };
+    std::unique_ptr<Build> build;
   };
   std::map<int, Class> classes;  // by turbulence model
   std::vector<std::unique_ptr<Request>> finished;
@@ -106,54 +133,116 @@ int fail(cycas_server* s, int rc) {
   return rc;
 }
 
-// new batch of class K from its active cases; the state of cases already in the old batch is
-// copied over on the device, and newly admitted cases get their volume (the residual of a case
-// is normalised by it)
-int rebuild(cycas_server* s, cycas_server::Class& K) {
+// starts building the next batch of class K from its active cases on a worker thread (each
+// batch context has its own stream; the library's error text and launch count are per thread)
+void start_build(cycas_server* s, cycas_server::Class& K) {
+  auto B = std::make_unique<cycas_server::Class::Build>();
+  std::vector<const cycas_case*> cases;
+  for (auto& r : K.active) {
+    cases.push_back(r->cs);
+    B->members.push_back(r.get());
+    r->in_build++;
+  }
+  cycas_server::Class::Build* Bp = B.get();
+  const cycas_options opt = s->opt;
+  const int graph = s->graph;
+  B->done = std::async(std::launch::async, [Bp, cases, opt, graph]() -> int {
+    const double t0 = now_s();
+    int rc = cycas_batch_create(cases.data(), (int32_t)cases.size(), &opt, &Bp->ctx);
+    if (rc == CYCAS_OK && graph) rc = cycas_set_graph(Bp->ctx, 1);  // captured on its first iteration
+    if (rc != CYCAS_OK) Bp->error = cycas_last_error();
+    Bp->seconds = now_s() - t0;
+    return rc;
+  });
+  K.build = std::move(B);
+  K.dirty = false;
+}
+
+bool build_ready(const cycas_server::Class& K) {
+  return K.build && K.build->done.wait_for(std::chrono::seconds(0)) == std::future_status::ready;
+}
+
+// the built batch becomes K's batch (waiting for the worker if needed): the state of cases
+// already in the old batch is copied over on the device (it has advanced while the new batch was
+// built), newly admitted cases get their volume (the residual of a case is normalised by it), the
+// old batch is destroyed and the budget of the cases that left with it is released
+int finish_build(cycas_server* s, cycas_server::Class& K) {
+  std::unique_ptr<cycas_server::Class::Build> B = std::move(K.build);
+  const int brc = B->done.get();
+  for (Request* r : B->members) {
+    r->in_build--;
+    if (r->free_case) release_case(r);
+  }
+  s->t_rebuild += B->seconds;
+  s->n_rebuild++;
+  if (B->admitted) s->last_admit_rebuild_s += B->seconds;
+  if (brc != CYCAS_OK) {
+    if (B->ctx) cycas_destroy(B->ctx);
+    s->err = B->error;
+    return brc;
+  }
   cycas_ctx* old = K.ctx;
-  std::vector<Request*> old_members = K.members;
-  K.ctx = nullptr;
-  K.members.clear();
-  if (!K.active.empty()) {
-    std::vector<const cycas_case*> cases;
-    for (auto& r : K.active) {
-      cases.push_back(r->cs);
-      K.members.push_back(r.get());
-    }
-    int rc = cycas_batch_create(cases.data(), (int32_t)cases.size(), &s->opt, &K.ctx);
-    if (rc != CYCAS_OK) return fail(s, rc);
-    if (s->graph) {
-      rc = cycas_set_graph(K.ctx, 1);  // captured on the batch's first iteration
+  const std::vector<Request*> old_members = K.members;
+  K.ctx = B->ctx;
+  K.members = B->members;
+  for (size_t k = 0; k < K.members.size(); k++) {
+    auto it = std::find(old_members.begin(), old_members.end(), K.members[k]);
+    if (it != old_members.end()) {
+      int rc = cycas_batch_copy_case(K.ctx, (int32_t)k, old, (int32_t)(it - old_members.begin()));
       if (rc != CYCAS_OK) return fail(s, rc);
-    }
-    // continuing cases keep their state
-    for (size_t k = 0; k < K.members.size(); k++) {
-      auto it = std::find(old_members.begin(), old_members.end(), K.members[k]);
-      if (it != old_members.end()) {
-        rc = cycas_batch_copy_case(K.ctx, (int32_t)k, old, (int32_t)(it - old_members.begin()));
-        if (rc != CYCAS_OK) return fail(s, rc);
-      }
-    }
-    // volumes of newly admitted cases
-    std::vector<int32_t> off(K.members.size() + 1);
-    cycas_batch_offsets(K.ctx, 0, off.data());
-    for (size_t k = 0; k < K.members.size(); k++) {
-      Request* r = K.members[k];
-      if (r->volume > 0.0) continue;
-      std::vector<double> vol(off[k + 1] - off[k]);
-      rc = cycas_batch_case_field(K.ctx, (int32_t)k, "cell_vol", vol.data(), (int64_t)vol.size());
-      if (rc != CYCAS_OK) return fail(s, rc);
-      r->volume = std::accumulate(vol.begin(), vol.end(), 0.0);
     }
   }
+  std::vector<int32_t> off(K.members.size() + 1);
+  cycas_batch_offsets(K.ctx, 0, off.data());
+  for (size_t k = 0; k < K.members.size(); k++) {
+    Request* r = K.members[k];
+    if (r->volume > 0.0) continue;
+    std::vector<double> vol(off[k + 1] - off[k]);
+    int rc = cycas_batch_case_field(K.ctx, (int32_t)k, "cell_vol", vol.data(), (int64_t)vol.size());
+    if (rc != CYCAS_OK) return fail(s, rc);
+    r->volume = std::accumulate(vol.begin(), vol.end(), 0.0);
+  }
   if (old) cycas_destroy(old);
-  K.dirty = false;
-  K.cells = 0.0;
-  for (Request* r : K.members) K.cells += (double)r->dims[0];
-  K.retired_cells = 0.0;
+  // members that retired while the batch was built stay in it until the next rebuild
+  double cells = 0.0, rcells = 0.0, rfoot = 0.0;
+  for (Request* r : K.members) {
+    cells += (double)r->dims[0];
+    if (r->status != 0) {
+      rcells += (double)r->dims[0];
+      rfoot += r->footprint;
+    }
+  }
+  s->in_use -= K.retired_footprint - rfoot;
+  K.retired_footprint = rfoot;
+  K.cells = cells;
+  K.retired_cells = rcells;
+  if (rcells > 0.0 && rcells >= 0.25 * cells) K.dirty = true;
+  return CYCAS_OK;
+}
+
+// a class without active cases: its batch goes, with the budget of its (retired) members
+void drop_batch(cycas_server* s, cycas_server::Class& K) {
+  if (K.ctx) cycas_destroy(K.ctx);
+  K.ctx = nullptr;
+  K.members.clear();
   s->in_use -= K.retired_footprint;
   K.retired_footprint = 0.0;
-  return CYCAS_OK;
+  K.cells = K.retired_cells = 0.0;
+  K.dirty = false;
+}
+
+// synchronous rebuild (a class with no batch to iterate meanwhile, or budget to release now)
+int rebuild_now(cycas_server* s, cycas_server::Class& K) {
+  if (K.build) {
+    int rc = finish_build(s, K);
+    if (rc != CYCAS_OK) return rc;
+  }
+  if (K.active.empty()) {
+    drop_batch(s, K);
+    return CYCAS_OK;
+  }
+  start_build(s, K);
+  return finish_build(s, K);
 }
 
 }  // namespace
@@ -181,6 +270,12 @@ int cycas_server_set_max_cells(cycas_server* s, double max_cells) {
   return CYCAS_OK;
 }
 
+int cycas_server_set_async_rebuild(cycas_server* s, int32_t on) {
+  if (!s) return CYCAS_ERR_INVALID;
+  s->async = on ? 1 : 0;
+  return CYCAS_OK;
+}
+
 int cycas_server_set_graph(cycas_server* s, int32_t on) {
   if (!s) return CYCAS_ERR_INVALID;
   s->graph = on ? 1 : 0;
@@ -194,8 +289,16 @@ int cycas_server_set_graph(cycas_server* s, int32_t on) {
 
 void cycas_server_destroy(cycas_server* s) {
   if (!s) return;
-  for (auto& kv : s->classes)
-    if (kv.second.ctx) cycas_destroy(kv.second.ctx);
+  for (auto& kv : s->classes) {
+    auto& K = kv.second;
+    if (K.build) {
+      K.build->done.wait();
+      if (K.build->ctx) cycas_destroy(K.build->ctx);
+      for (Request* r : K.build->members) r->in_build--;
+      K.build.reset();
+    }
+    if (K.ctx) cycas_destroy(K.ctx);
+  }
   auto free_req = [](Request* r) {
     if (r->cs) cycas_case_free(r->cs);
   };
@@ -248,10 +351,7 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
     for (auto& kv : s->classes) {
       auto& K = kv.second;
       if (K.retired_footprint <= 0.0) continue;
-      const double t0 = now_s();
-      int rc = rebuild(s, K);
-      s->t_rebuild += now_s() - t0;
-      s->n_rebuild++;
+      int rc = rebuild_now(s, K);
       if (rc != CYCAS_OK) return rc;
     }
   }
@@ -277,17 +377,24 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
     s->last_admit_rebuild_s = 0.0;
     s->iterate_since_admit_s = 0.0;
   }
-  // 2-4. per class: rebuild if needed, one iteration, retire
+  // 2-4. per class: switch to a built batch, start a rebuild if needed, one iteration, retire
   for (auto& kv : s->classes) {
     auto& K = kv.second;
-    if (K.dirty) {
-      const double t0 = now_s();
-      int rc = rebuild(s, K);
-      const double dt = now_s() - t0;
-      s->t_rebuild += dt;
-      s->n_rebuild++;
-      if (admitted.count(kv.first)) s->last_admit_rebuild_s += dt;
+    if (build_ready(K)) {
+      int rc = finish_build(s, K);
       if (rc != CYCAS_OK) return rc;
+    }
+    if (K.dirty && !K.build) {
+      if (K.active.empty()) {
+        drop_batch(s, K);
+      } else {
+        start_build(s, K);
+        K.build->admitted = admitted.count(kv.first) > 0;
+        if (!K.ctx || !s->async) {  // nothing to iterate meanwhile, or built in line
+          int rc = finish_build(s, K);
+          if (rc != CYCAS_OK) return rc;
+        }
+      }
     }
     if (K.members.empty()) continue;
     const int nc = (int)K.members.size();
@@ -336,8 +443,7 @@ int cycas_server_step(cycas_server* s, int32_t* n_active, int32_t* n_queued) {
           K.retired_footprint += r->footprint;
           K.retired_cells += (double)r->dims[0];
           s->active_cells -= (double)r->dims[0];
-          cycas_case_free(r->cs);
-          r->cs = nullptr;
+          release_case(r.get());  // at once, or when no batch build reads it any more
           s->finished.push_back(std::move(r));
         } else {
           keep.push_back(std::move(r));

@@ -579,6 +579,11 @@ class Server:
         cap; cycas_server_set_max_cells)."""
         capi.check(capi.load().cycas_server_set_max_cells(self._h, float(max_cells)))
 
+    def set_async_rebuild(self, on: bool) -> None:
+        """Build new batches on a worker thread while the current ones keep iterating
+        (cycas_server_set_async_rebuild)."""
+        capi.check(capi.load().cycas_server_set_async_rebuild(self._h, 1 if on else 0))
+
     def submit(self, param_path: str) -> int:
         i = C.c_int64()
         rc = capi.load().cycas_server_submit(self._h, param_path.encode(), C.byref(i))

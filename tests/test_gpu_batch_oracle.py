@@ -55,10 +55,14 @@ def test_batched_cases_match_oracle_alone(cases):
     b.close()
 
 
-def test_served_requests_match_oracle_alone(cases):
+@pytest.mark.parametrize("async_rebuild", [False, True])
+def test_served_requests_match_oracle_alone(cases, async_rebuild):
+    """Also with batches rebuilt on a worker thread: the late arrival's batch is built while the
+    first two requests keep iterating, and their state moves over at the switch."""
     names = ["cavity4", "cavity8", "channel_tiny"]
     params = {n: cases(n) for n in names}
     srv = Server(hbm_budget_gb=100.0, residual_tol=1e-5, max_iters=12, keep_fields=True, options=_tight_gpu())
+    srv.set_async_rebuild(async_rebuild)
     ids = {n: srv.submit(params[n]) for n in names[:2]}
     for step in range(100):
         if step == 2:  # a later arrival joins the running server

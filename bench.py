@@ -1248,6 +1248,7 @@ def run_batch256(args):
         opt.mixed = 1 if mixed else 0
         srv = Server(hbm_budget_gb=args.budget_gb, residual_tol=args.tol, max_iters=args.max_iters, options=opt)
         srv.set_graph(True)
+        srv.set_async_rebuild(args.async_rebuild)
         t0 = Server.clock()
         ids = [srv.submit(p) for p in params]
         steps = 0
@@ -1303,7 +1304,8 @@ def run_batch256(args):
             "dtype": "mixed", "data": "synthetic", "cells": cells,
             "config": {"workload": "%d cavities n~U{8..40}^3 hexahedra, jitter 0.1h, Re~logU[10,1000], each to "
                                    "1e-6; continuous-batching server, CUDA graph per batch iteration" % len(params),
-                       "budget_gb": args.budget_gb, "max_iters": args.max_iters},
+                       "budget_gb": args.budget_gb, "max_iters": args.max_iters,
+                       "batch_rebuilds": "worker thread" if args.async_rebuild else "in line"},
             **out}
     a = out.get("one_at_a_time_plain_fp64") or {}
     for k in ("batched", "batched_mixed"):
@@ -1380,6 +1382,8 @@ def main():
     ap.add_argument("--mixed", action="store_true")
     ap.add_argument("--sync-rebuild", action="store_true",
                     help="serve workload: rebuild batches in line instead of on a worker thread")
+    ap.add_argument("--async-rebuild", action="store_true",
+                    help="batch256 workload: rebuild batches on a worker thread")
     ap.add_argument("--serve-seed", type=int, default=5)
     ap.add_argument("--outer-rtol", type=float, default=1e-10, help="precision workload: rtol of every system")
     # --workload profile: the generated case and its solver options

@@ -46,24 +46,29 @@ using namespace kry;
 constexpr int kThreads = 256;
 
 // ---------------------------------------------------------------- per-solve setup
-__global__ void k_amg_level0(int nnz, const double* __restrict__ val64, float* __restrict__ val) {
+// FP32 copy of the pressure matrix; a diagonal entry also gives its row's smoother weight w / a_ii
+__global__ void k_amg_level0(int nnz, const double* __restrict__ val64, float* __restrict__ val,
+                             const int* __restrict__ diag_row, float omega, float* __restrict__ wdinv) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < nnz) val[k] = (float)val64[k];
+  if (k >= nnz) return;
+  const float v = (float)val64[k];
+  val[k] = v;
+  const int i = diag_row[k];
+  if (i >= 0) wdinv[i] = omega / v;
 }
 
+// Galerkin sum of one coarse entry (fine entries in ascending order); a diagonal entry also
+// gives its row's smoother weight
 __global__ void k_amg_galerkin(int nnz_c, const int* __restrict__ cptr, const int* __restrict__ csrc,
-                               const float* __restrict__ valf, float* __restrict__ valc) {
+                               const float* __restrict__ valf, float* __restrict__ valc,
+                               const int* __restrict__ diag_row_c, float omega, float* __restrict__ wdinv_c) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nnz_c) return;
   float s = 0.0f;
   for (int q = cptr[c]; q < cptr[c + 1]; q++) s += valf[csrc[q]];
   valc[c] = s;
-}
-
-__global__ void k_amg_wdinv(int n, float omega, const int* __restrict__ diag, const float* __restrict__ val,
-                            float* __restrict__ wdinv) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) wdinv[i] = omega / val[diag[i]];
+  const int i = diag_row_c[c];
+  if (i >= 0) wdinv_c[i] = omega / s;
 }
 
 // dense inverse of A_L + s 11^T, s = mean(diag)/n, for the coarsest level of case blockIdx.x,
@@ -697,16 +702,13 @@ void launch_amg_setup_values(const AmgHostView& h, cudaStream_t s) {
   // the dense inverse of every case's coarsest level
   const int D = (int)h.dep.size();
   const AmgHostView::Depth& d0 = h.dep[0];
-  ++g_launch_count, k_amg_level0<<<(d0.nnz + kThreads - 1) / kThreads, kThreads, 0, s>>>(d0.nnz, h.val64, d0.val);
-  ++g_launch_count, k_amg_wdinv<<<(d0.nrows + kThreads - 1) / kThreads, kThreads, 0, s>>>(d0.nrows, h.omega, d0.diag,
-                                                                                         d0.val, d0.wdinv);
+  ++g_launch_count, k_amg_level0<<<(d0.nnz + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+                        d0.nnz, h.val64, d0.val, d0.diag_row, h.omega, d0.wdinv);
   for (int l = 0; l + 1 < D; l++) {
     const AmgHostView::Depth& F = h.dep[l];
     const AmgHostView::Depth& C = h.dep[l + 1];
-    ++g_launch_count, k_amg_galerkin<<<(C.nnz + kThreads - 1) / kThreads, kThreads, 0, s>>>(C.nnz, F.cptr, F.csrc,
-                                                                                           F.val, C.val);
-    ++g_launch_count, k_amg_wdinv<<<(C.nrows + kThreads - 1) / kThreads, kThreads, 0, s>>>(C.nrows, h.omega, C.diag,
-                                                                                          C.val, C.wdinv);
+    ++g_launch_count, k_amg_galerkin<<<(C.nnz + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+                          C.nnz, F.cptr, F.csrc, F.val, C.val, C.diag_row, h.omega, C.wdinv);
   }
   ++g_launch_count, k_amg_coarse_inverse<<<h.ncases, 1024, 0, s>>>(h.d_cases);
 }

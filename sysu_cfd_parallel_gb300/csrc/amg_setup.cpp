@@ -349,6 +349,15 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
     const int* d_rp = l == 0 ? rowptr_dev : up.upload_int(rp.data(), (long)rp.size());
     const int* d_cl = l == 0 ? col_dev : up.upload_int(cl.data(), (long)cl.size());
     d.diag = l == 0 ? diag_dev : up.upload_int(dg.data(), (long)dg.size());
+    {  // the row of every diagonal entry (the setup kernels write w / a_ii where they make a_ii)
+      std::vector<int> dr(std::max(1, nnzs[l]), -1);
+      for (int c = 0; c < nc; c++) {
+        if ((int)H(c).lv.size() <= l) continue;
+        const AmgHostLevel& L = H(c).lv[l];
+        for (int i = 0; i < L.n; i++) dr[L.diag[i] + nnz_off[l][c]] = row_off[l][c] + i;
+      }
+      d.diag_row = up.upload_int(dr.data(), (long)dr.size());
+    }
     d.val = up.alloc_float(std::max(1, nnzs[l]));
     d.wdinv = up.alloc_float(std::max(1, nrows[l]));
     float* d_r = up.alloc_float(std::max(1, nrows[l]));

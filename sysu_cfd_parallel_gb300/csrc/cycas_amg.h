@@ -121,6 +121,7 @@ struct AmgHostView {
   struct Depth {
     int nrows = 0, nnz = 0;
     const int* diag = nullptr;  // [nrows] global positions of the diagonals
+    const int* diag_row = nullptr;  // [nnz] the row of a diagonal entry, -1 off the diagonal
     float* val = nullptr;       // [nnz]
     float* wdinv = nullptr;     // [nrows]
     const int* cptr = nullptr;  // depth+1 nnz -> range in csrc (null for the deepest depth)

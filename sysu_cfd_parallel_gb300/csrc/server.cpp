@@ -146,20 +146,27 @@ void start_build(cycas_server* s, cycas_server::Class& K) {
   cycas_server::Class::Build* Bp = B.get();
   const cycas_options opt = s->opt;
   const int graph = s->graph;
-  B->done = std::async(std::launch::async, [Bp, cases, opt, graph]() -> int {
+  auto job = [Bp, cases, opt, graph]() -> int {
     const double t0 = now_s();
     int rc = cycas_batch_create(cases.data(), (int32_t)cases.size(), &opt, &Bp->ctx);
     if (rc == CYCAS_OK && graph) rc = cycas_set_graph(Bp->ctx, 1);  // captured on its first iteration
     if (rc != CYCAS_OK) Bp->error = cycas_last_error();
     Bp->seconds = now_s() - t0;
     return rc;
-  });
+  };
+  try {
+    B->done = std::async(s->async ? std::launch::async : std::launch::deferred, job);
+  } catch (const std::exception&) {  // no worker thread: build when the result is asked for
+    B->done = std::async(std::launch::deferred, job);
+  }
   K.build = std::move(B);
   K.dirty = false;
 }
 
 bool build_ready(const cycas_server::Class& K) {
-  return K.build && K.build->done.wait_for(std::chrono::seconds(0)) == std::future_status::ready;
+  if (!K.build) return false;
+  const std::future_status st = K.build->done.wait_for(std::chrono::seconds(0));
+  return st == std::future_status::ready || st == std::future_status::deferred;  // deferred: built on get()
 }
 
 // the built batch becomes K's batch (waiting for the worker if needed): the state of cases

@@ -171,19 +171,20 @@ struct cycas_ctx {
   const DevBatch* bptr() const { return is_batch ? &batch : nullptr; }
 
   template <class T>
-  T* alloc(long n) {
+  T* alloc(long n, bool zero = true) {
     void* p = nullptr;
     size_t bytes = sizeof(T) * (size_t)(n > 0 ? n : 1);
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) throw StatusError(CYCAS_ERR_ALLOC, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
     allocs.push_back(p);
-    CK(cudaMemsetAsync(p, 0, bytes, stream));
+    if (zero) CK(cudaMemsetAsync(p, 0, bytes, stream));
     return (T*)p;
   }
   template <class T>
   T* upload(const T* h, long n) {
-    T* d = alloc<T>(n);
-    if (n > 0 && h) CK(cudaMemcpyAsync(d, h, sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, stream));
+    const bool full = n > 0 && h;  // the copy overwrites every element
+    T* d = alloc<T>(n, !full);
+    if (full) CK(cudaMemcpyAsync(d, h, sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, stream));
     return d;
   }
   double* dfield(const char* name, long n) {

@@ -18,6 +18,11 @@ The cases are those of make_golden.py (run for ``golden_steps`` iterations or ti
 with GMRES(30) rtol 1e-8 on every system (-ksp_type gmres -ksp_rtol 1e-8), as the configuration
 runs the reference.  Preconditioners: ``ilu`` (PETSc's default, ILU(0)) and ``jacobi``.
 
+``cavity48/ref_ilu_tight.npz``: the bench's cavity (48^3 hexahedra) for its first 5 SIMPLE
+iterations with the reference's own solvers and ILU(0), every system to rtol 1e-10
+(-ksp_rtol 1e-10): residual history, Krylov log, and the L2 norm and sum of u, v, w, p (the
+fields themselves would be megabytes).
+
 Needs the reference tree (REF, default /root/reference) and g++.  Run from the repository root:
     python tests/golden/make_ref_golden.py
 """
@@ -98,8 +103,35 @@ def write_cavity20(d):
     return os.path.dirname(meshgen.write_case(d, "cavity", n=20, steps=200))
 
 
+def write_cavity48(d):
+    """The bench's cavity inputs (48^3 uniform hexahedra; meshgen writes the same bytes every time)."""
+    from sysu_cfd_parallel_gb300 import meshgen
+    return os.path.dirname(meshgen.write_case(d, "cavity", n=48, steps=5))
+
+
+CAVITY48_OPTIONS = ["-ksp_rtol", "1e-10"]
+CAVITY48_STEPS = 5
+
+
+def cavity48_fixture():
+    tmp = tempfile.mkdtemp()
+    try:
+        o = run_reference(write_cavity48(tmp), CAVITY48_STEPS, CAVITY48_OPTIONS)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    keep = {"residual": o["residual"].reshape(-1, 10), "ksp": o["ksp"].reshape(-1, 4), "info": o["info"],
+            "steps": np.array(CAVITY48_STEPS), "options": np.array(" ".join(CAVITY48_OPTIONS))}
+    for nm in ("U", "V", "W", "P"):
+        keep[nm + "_norm"] = np.array(np.linalg.norm(o[nm]))
+        keep[nm + "_sum"] = np.array(np.sum(o[nm]))
+    os.makedirs(os.path.join(HERE, "cavity48"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "cavity48", "ref_ilu_tight.npz"), **keep)
+    print("cavity48 iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
+
+
 def main():
     build()
+    cavity48_fixture()
     tmp = tempfile.mkdtemp()
     os.makedirs(os.path.join(HERE, "cavity20"), exist_ok=True)
     for name, (steps, opts) in RUNS.items():

@@ -106,6 +106,23 @@ def test_cavity20_configured_run_bit_exact(pc, tmp_path):
     o.close()
 
 
+def test_cavity48_first_iterations_bit_exact(tmp_path):
+    """The bench's cavity (48^3 hexahedra) for its first 5 SIMPLE iterations, ILU(0) and rtol
+    1e-10 on every system: residual history, every Krylov count, and the L2 norm and sum of u, v,
+    w, p equal the reference build's (tests/golden/cavity48/ref_ilu_tight.npz)."""
+    from make_ref_golden import write_cavity48
+    g = dict(np.load(os.path.join(GOLDEN, "cavity48", "ref_ilu_tight.npz")))
+    d = write_cavity48(str(tmp_path))
+    o = _oracle(os.path.join(d, "param.in"), "ilu", rtol=1e-10)
+    res, its = _run(o, int(g["steps"]), False)
+    assert np.array_equal(res.view(np.int64), g["residual"].view(np.int64)), np.abs(res - g["residual"]).max()
+    assert np.array_equal(its, g["ksp"][:, 1].astype(np.int32))
+    for nm in ("U", "V", "W", "P"):
+        x = o.get(nm)
+        assert np.linalg.norm(x) == g[nm + "_norm"] and np.sum(x) == g[nm + "_sum"], nm
+    o.close()
+
+
 def test_pow15_differs_from_libm_by_one_ulp_at_most():
     """TE^1.5 (the wall function's pow) in the two oracle modes: the once-rounded value the GPU
     computes and the C library's, on the k-epsilon channel fixture; the fields after its six

@@ -192,11 +192,17 @@ int finish_build(cycas_server* s, cycas_server::Class& K) {
   const std::vector<Request*> old_members = K.members;
   K.ctx = B->ctx;
   K.members = B->members;
+  // an error leaves the server unusable; the old batch goes all the same
+  auto give_up = [&](int rc) {
+    const int out = fail(s, rc);
+    if (old) cycas_destroy(old);
+    return out;
+  };
   for (size_t k = 0; k < K.members.size(); k++) {
     auto it = std::find(old_members.begin(), old_members.end(), K.members[k]);
     if (it != old_members.end()) {
       int rc = cycas_batch_copy_case(K.ctx, (int32_t)k, old, (int32_t)(it - old_members.begin()));
-      if (rc != CYCAS_OK) return fail(s, rc);
+      if (rc != CYCAS_OK) return give_up(rc);
     }
   }
   std::vector<int32_t> off(K.members.size() + 1);
@@ -206,7 +212,7 @@ int finish_build(cycas_server* s, cycas_server::Class& K) {
     if (r->volume > 0.0) continue;
     std::vector<double> vol(off[k + 1] - off[k]);
     int rc = cycas_batch_case_field(K.ctx, (int32_t)k, "cell_vol", vol.data(), (int64_t)vol.size());
-    if (rc != CYCAS_OK) return fail(s, rc);
+    if (rc != CYCAS_OK) return give_up(rc);
     r->volume = std::accumulate(vol.begin(), vol.end(), 0.0);
   }
   if (old) cycas_destroy(old);

@@ -1,4 +1,4 @@
-// Driver of the reference's own solver, compiled from its unmodified sources against the
+// Main program running the reference's own solver, compiled from its unmodified sources against the
 // single-rank runtime of this folder (TEST INFRASTRUCTURE ONLY).
 //
 //   cycas_ref <case-dir> <out-dir> [--iters N] [--residual R] [PETSc / reference options ...]

@@ -5,7 +5,7 @@
 // restatement can be checked against the code it restates.  Nothing here computes physics:
 //   * MPI: rank 0 of a communicator of size 1.  Collectives copy; messages to oneself are queued
 //     and matched by tag; every MPI_Allreduce of doubles is also appended to a log, which is how
-//     the driver reads the residual vector NSSolve reduces each iteration (navier.cpp:94).
+//     refpin_main.cpp reads the residual vector NSSolve reduces each iteration (navier.cpp:94).
 //   * PETSc: Vec is a double array; Mat keeps the union of every entry ever set (explicit zeros
 //     included) with sorted columns; KSPSolve hands the assembled matrix to the oracle's
 //     GMRES / CG (oracle/oracle_krylov.cpp) with the options PETSc would apply, and logs the

@@ -1,4 +1,4 @@
-// Logs the single-rank runtime keeps for the driver (TEST INFRASTRUCTURE ONLY).
+// Logs the single-rank runtime keeps for the main program (refpin_main.cpp) (TEST INFRASTRUCTURE ONLY).
 #pragma once
 #include <vector>
 

@@ -8,8 +8,13 @@
 // every coarse non-zero, the fine non-zeros that add into it (in ascending order), so the
 // device rebuilds the coarse values each iteration with deterministic gathers.
 #include <algorithm>
+#include <atomic>
+#include <exception>
+#include <memory>
 #include <numeric>
 #include <stdexcept>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "cycas_amg.h"
@@ -232,6 +237,64 @@ TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz, c
   return T;
 }
 
+// entries of a level's SELL-32 layout (sell32(L).col.size()) without building it: 32 times the
+// length of every 32nd row in decreasing row length, from a histogram of the row lengths
+long sell_entries(const AmgHostLevel& L) {
+  int mx = 0;
+  for (int i = 0; i < L.n; i++) mx = std::max(mx, L.rowptr[i + 1] - L.rowptr[i]);
+  std::vector<long> cnt(mx + 1, 0);
+  for (int i = 0; i < L.n; i++) cnt[L.rowptr[i + 1] - L.rowptr[i]]++;
+  long total = 0, p = 0;  // positions [p, p + cnt[v]) of the decreasing order have length v
+  for (int v = mx; v >= 0; v--) {
+    const long first = (p + 31) / 32 * 32;  // the first slice head at or after p
+    if (first < p + cnt[v]) total += 32L * v * ((p + cnt[v] - 1 - first) / 32 + 1);
+    p += cnt[v];
+  }
+  return total;
+}
+
+// Runs job(c) for every case c, the largest (by work[c]) first, on up to 16 of the host's
+// hardware threads; every job writes only its own case's slices, so the result does not depend
+// on the thread count.  Returns the exception each case's job raised (null where none).
+template <class Job>
+std::vector<std::exception_ptr> for_each_case(const std::vector<long>& work, const Job& job) {
+  const int n = (int)work.size();
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+  const long total = std::accumulate(work.begin(), work.end(), 0L);
+  const int hw = (int)std::thread::hardware_concurrency();
+  // small setups stay on the calling thread (starting threads would cost more than the work)
+  const int nt = total < (1L << 16) ? 1 : std::max(1, std::min(std::min(n, hw), 16));
+  std::vector<std::exception_ptr> err(n);
+  std::atomic<int> next{0};
+  auto run = [&]() {
+    for (int q = next++; q < n; q = next++) {
+      try {
+        job(order[q]);
+      } catch (...) {
+        err[order[q]] = std::current_exception();
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) {
+    try {
+      pool.emplace_back(run);
+    } catch (const std::system_error&) {  // no more threads: the ones running share the cases
+      break;
+    }
+  }
+  run();
+  for (auto& th : pool) th.join();
+  return err;
+}
+
+void rethrow_first(const std::vector<std::exception_ptr>& err) {
+  for (const auto& e : err)
+    if (e) std::rethrow_exception(e);
+}
+
 }  // namespace
 
 void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, const double* weight,
@@ -243,33 +306,42 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
   std::vector<std::shared_ptr<const AmgHostHierarchy>> Hp(nc);
   std::vector<int> case_nnz0(nc + 1, 0);  // first level-0 entry of every case (cases are contiguous)
   int D = 0;
+  // the hierarchies of the cases not in the cache, built in parallel (they are independent)
+  std::vector<long> build_work(nc, 0);
   for (int c = 0; c < nc; c++) {
+    const bool in_range = hi[c] - lo[c] >= 1 && hi[c] <= n && lo[c] >= 0;
+    if (in_range && !(cache && (*cache)[c]) && rowptr) build_work[c] = rowptr[hi[c]] - rowptr[lo[c]];
+  }
+  std::vector<std::exception_ptr> build_err = for_each_case(build_work, [&](int c) {
     const int l0 = lo[c], nr = hi[c] - lo[c];
-    if (nr < 1 || hi[c] > n) throw std::runtime_error("AMG: empty or out-of-range case");
+    if (nr < 1 || hi[c] > n || l0 < 0) throw std::runtime_error("AMG: empty or out-of-range case");
     if (cache && (*cache)[c]) {
       Hp[c] = (*cache)[c];
       if (Hp[c]->lv.empty() || Hp[c]->lv[0].n != nr) throw std::runtime_error("AMG: cached hierarchy of another case");
-    } else {
-      if (!rowptr || !col || !weight) throw std::runtime_error("AMG: pattern needed to build a hierarchy");
-      const int k0 = rowptr[l0];
-      std::vector<int> rp(nr + 1), cl(rowptr[hi[c]] - k0);
-      std::vector<double> w(cl.size());
-      for (int i = 0; i <= nr; i++) rp[i] = rowptr[l0 + i] - k0;
-      for (size_t k = 0; k < cl.size(); k++) {
-        const int j = col[k0 + k];
-        if (j < l0 || j >= hi[c]) throw std::runtime_error("AMG: the pressure system couples two cases");
-        cl[k] = j - l0;
-        w[k] = weight[k0 + k];
-      }
-      auto h = std::make_shared<AmgHostHierarchy>(
-          amg_build(nr, rp.data(), cl.data(), w.data(), 4, kAmgCoarseMax, kAmgMaxLevels));
-      if (h->lv.back().n > kAmgCoarseMax)
-        throw std::runtime_error("aggregation did not reach a small enough coarsest level");
-      Hp[c] = h;
-      if (cache) (*cache)[c] = h;
+      return;
     }
+    if (!rowptr || !col || !weight) throw std::runtime_error("AMG: pattern needed to build a hierarchy");
+    const int k0 = rowptr[l0];
+    std::vector<int> rp(nr + 1), cl(rowptr[hi[c]] - k0);
+    std::vector<double> w(cl.size());
+    for (int i = 0; i <= nr; i++) rp[i] = rowptr[l0 + i] - k0;
+    for (size_t k = 0; k < cl.size(); k++) {
+      const int j = col[k0 + k];
+      if (j < l0 || j >= hi[c]) throw std::runtime_error("AMG: the pressure system couples two cases");
+      cl[k] = j - l0;
+      w[k] = weight[k0 + k];
+    }
+    auto h = std::make_shared<AmgHostHierarchy>(
+        amg_build(nr, rp.data(), cl.data(), w.data(), 4, kAmgCoarseMax, kAmgMaxLevels));
+    if (h->lv.back().n > kAmgCoarseMax) throw std::runtime_error("aggregation did not reach a small enough coarsest level");
+    Hp[c] = h;
+  });
+  // case by case, as if built in order: a case's build error comes before its own contiguity check
+  for (int c = 0; c < nc; c++) {
+    if (build_err[c]) std::rethrow_exception(build_err[c]);
+    if (cache) (*cache)[c] = Hp[c];
     case_nnz0[c + 1] = case_nnz0[c] + Hp[c]->lv[0].nnz;
-    if (rowptr && rowptr[l0] != case_nnz0[c]) throw std::runtime_error("AMG: cases are not contiguous in the pattern");
+    if (rowptr && rowptr[lo[c]] != case_nnz0[c]) throw std::runtime_error("AMG: cases are not contiguous in the pattern");
     D = std::max(D, (int)Hp[c]->lv.size());
   }
   auto H = [&](int c) -> const AmgHostHierarchy& { return *Hp[c]; };
@@ -309,75 +381,72 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
   nrows[0] = n;
   nnzs[0] = case_nnz0[nc];
 
-  // host arrays per depth
+  // host arrays per depth; every case fills its own slices (in parallel), then they are uploaded
+  // in a fixed order
   for (int l = 0; l < D; l++) {
-    std::vector<int> rp, cl, dg, ag, pp, pr, cptr, csrc;
-    if (l > 0) {
-      rp.reserve(nrp[l]);
-      cl.reserve(nnzs[l]);
-      dg.reserve(nrows[l]);
-    }
-    ag.assign(l == 0 ? n : nrows[l], -1);
-    for (int c = 0; c < nc; c++) {
-      if ((int)H(c).lv.size() <= l) continue;
+    const bool next = l + 1 < D;
+    std::vector<int> rp(l > 0 ? nrp[l] : 0), cl(l > 0 ? nnzs[l] : 0), dg(l > 0 ? nrows[l] : 0);
+    std::vector<int> ag(l == 0 ? n : nrows[l], -1), pp(npt[l]), pr(nptr[l]);
+    // Galerkin map into depth l+1, in the depth l+1 order of cases: coarse entry e of case c is
+    // entry nnz_off[l+1][c] + e of depth l+1 and sums the fine entries csrc[cptr[.]..cptr[.+1])
+    std::vector<int> cptr(next ? nnzs[l + 1] + 1 : 0);
+    if (next) cptr[0] = 0;
+    // The arrays of one entry per entry of the depth are written only by the cases (the cases'
+    // entries tile the depth, level 0 included: they are checked contiguous), so they start
+    // uninitialised: csrc, the row of every diagonal entry (-1 elsewhere; the setup kernels write
+    // w / a_ii where they make a_ii) and agg[col[k]] (cases without a coarser level: unused zeros).
+    const long ne = std::max(1, nnzs[l]);
+    std::unique_ptr<int[]> csrc(new int[next ? std::max(1, ncp[l]) : 1]);
+    std::unique_ptr<int[]> dr(new int[ne]), ac(new int[ne]);
+    dr[0] = -1;  // the depth has entries; this only covers an empty one
+    ac[0] = 0;
+    std::vector<long> fill_work(nc, 0);
+    for (int c = 0; c < nc; c++)
+      if ((int)H(c).lv.size() > l) fill_work[c] = H(c).lv[l].nnz;
+    rethrow_first(for_each_case(fill_work, [&](int c) {
+      if ((int)H(c).lv.size() <= l) return;
       const AmgHostLevel& L = H(c).lv[l];
+      const int ro = row_off[l][c], no = nnz_off[l][c];
       if (l > 0) {
-        rp.insert(rp.end(), L.rowptr.begin(), L.rowptr.end());
-        cl.insert(cl.end(), L.col.begin(), L.col.end());
-        for (int i = 0; i < L.n; i++) dg.push_back(L.diag[i] + nnz_off[l][c]);
+        std::copy(L.rowptr.begin(), L.rowptr.end(), rp.begin() + rp_off[l][c]);
+        std::copy(L.col.begin(), L.col.end(), cl.begin() + no);
+        for (int i = 0; i < L.n; i++) dg[ro + i] = L.diag[i] + no;
       }
-      if (l + 1 < (int)H(c).lv.size()) {
-        for (int i = 0; i < L.n; i++) ag[row_off[l][c] + i] = L.agg[i];
-        pp.insert(pp.end(), L.ptptr.begin(), L.ptptr.end());
-        for (int i = 0; i < L.n; i++) pr.push_back(L.ptrow[i] + (l == 0 ? lo[c] : 0));
+      std::fill(dr.get() + no, dr.get() + no + L.nnz, -1);
+      for (int i = 0; i < L.n; i++) dr[L.diag[i] + no] = ro + i;
+      if ((int)H(c).lv.size() <= l + 1) {
+        std::fill(ac.get() + no, ac.get() + no + L.nnz, 0);
+        return;
       }
-    }
-    // Galerkin map into depth l+1, in the depth l+1 order of cases
-    if (l + 1 < D) {
-      cptr.push_back(0);
-      for (int c = 0; c < nc; c++) {
-        if ((int)H(c).lv.size() <= l + 1) continue;
-        const AmgHostLevel& L = H(c).lv[l];
-        const int base = cptr.back();
-        for (size_t q = 1; q < L.cptr.size(); q++) cptr.push_back(base + L.cptr[q]);
-        for (int k : L.csrc) csrc.push_back(k + nnz_off[l][c]);
-      }
-    }
+      for (int i = 0; i < L.n; i++) ag[ro + i] = L.agg[i];
+      std::copy(L.ptptr.begin(), L.ptptr.end(), pp.begin() + pt_off[l][c]);
+      const int shift = l == 0 ? lo[c] : 0;
+      for (int i = 0; i < L.n; i++) pr[ptr_off[l][c] + i] = L.ptrow[i] + shift;
+      const int e0 = nnz_off[l + 1][c], base = cp_off[l][c];
+      for (size_t q = 1; q < L.cptr.size(); q++) cptr[e0 + q] = base + L.cptr[q];
+      for (size_t k = 0; k < L.csrc.size(); k++) csrc[base + k] = L.csrc[k] + no;
+      for (int k = 0; k < L.nnz; k++) ac[no + k] = L.agg[L.col[k]];
+    }));
     AmgHostView::Depth& d = v.dep[l];
     d.nrows = nrows[l];
     d.nnz = nnzs[l];
     const int* d_rp = l == 0 ? rowptr_dev : up.upload_int(rp.data(), (long)rp.size());
     const int* d_cl = l == 0 ? col_dev : up.upload_int(cl.data(), (long)cl.size());
     d.diag = l == 0 ? diag_dev : up.upload_int(dg.data(), (long)dg.size());
-    {  // the row of every diagonal entry (the setup kernels write w / a_ii where they make a_ii)
-      std::vector<int> dr(std::max(1, nnzs[l]), -1);
-      for (int c = 0; c < nc; c++) {
-        if ((int)H(c).lv.size() <= l) continue;
-        const AmgHostLevel& L = H(c).lv[l];
-        for (int i = 0; i < L.n; i++) dr[L.diag[i] + nnz_off[l][c]] = row_off[l][c] + i;
-      }
-      d.diag_row = up.upload_int(dr.data(), (long)dr.size());
-    }
+    d.diag_row = up.upload_int(dr.get(), ne);
     d.val = up.alloc_float(std::max(1, nnzs[l]));
     d.wdinv = up.alloc_float(std::max(1, nrows[l]));
     float* d_r = up.alloc_float(std::max(1, nrows[l]));
     float* d_t = l == 0 ? nullptr : up.alloc_float(std::max(1, nrows[l]));
     float* d_wr = up.alloc_float(std::max(1, nrows[l]));
     float* d_sr = up.alloc_float(std::max(1, nrows[l]));
-    // agg[col[k]] of every entry of the depth (cases without a coarser level: unused zeros)
-    std::vector<int> ac(std::max(1, nnzs[l]), 0);
-    for (int c = 0; c < nc; c++) {
-      if ((int)H(c).lv.size() <= l + 1) continue;
-      const AmgHostLevel& L = H(c).lv[l];
-      for (int k = 0; k < L.nnz; k++) ac[nnz_off[l][c] + k] = L.agg[L.col[k]];
-    }
-    const int* d_ac = up.upload_int(ac.data(), (long)ac.size());
+    const int* d_ac = up.upload_int(ac.get(), ne);
     const int* d_ag = up.upload_int(ag.data(), (long)ag.size());
     const int* d_pp = pp.empty() ? nullptr : up.upload_int(pp.data(), (long)pp.size());
     const int* d_pr = pr.empty() ? nullptr : up.upload_int(pr.data(), (long)pr.size());
     if (l + 1 < D) {
       d.cptr = up.upload_int(cptr.data(), (long)cptr.size());
-      d.csrc = up.upload_int(csrc.data(), (long)csrc.size());
+      d.csrc = up.upload_int(csrc.get(), (long)ncp[l]);
       d.nnz_next = (int)cptr.size() - 1;
     }
     for (int c = 0; c < nc; c++) {
@@ -432,13 +501,11 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
   int tail_max = 0;
   for (int c = 0; c < nc; c++) {
     std::vector<int> ln, lz, ls;
-    std::vector<Sell> sells;
     for (const AmgHostLevel& L : H(c).lv) {
       ln.push_back(L.n);
       lz.push_back(L.nnz);
       // the SELL copy only matters for levels small enough to be in the tail
-      sells.push_back(L.n < 65536 ? sell32(L) : Sell{});
-      ls.push_back(L.n < 65536 ? (int)sells.back().col.size() : L.nnz);
+      ls.push_back(L.n < 65536 ? (int)sell_entries(L) : L.nnz);
     }
     AmgCaseDesc& cd = v.cases[c];
     cd.lo = lo[c];
@@ -454,7 +521,7 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
       e.sell_row = nullptr;
       e.sell_len = 0;
       if (l < cd.tl.tail || l + 1 >= cd.nlev) continue;
-      const Sell& S = sells[l];
+      const Sell S = sell32(H(c).lv[l]);
       e.sell_ptr = up.upload_int(S.ptr.data(), (long)S.ptr.size());
       e.sell_col = (const unsigned short*)up.upload_bytes(S.col.data(), 2L * (long)S.col.size());
       e.sell_src = up.upload_int(S.src.data(), (long)S.src.size());

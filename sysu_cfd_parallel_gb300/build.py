@@ -6,6 +6,7 @@ Translation units:
                  reference's source orders each product and sum
   krylov.cu      nvcc -- persistent GMRES, reductions
   capi.cu        nvcc -- C ABI and iteration schedule
+  mesh_tables.cpp g++ -- CSR pattern, slots and face orders of a mesh (host threads)
   result_io.cpp  g++ -ffp-contract=off -- result files in the reference's formats
 Objects are compiled in parallel and linked with nvcc into
 ``sysu_cfd_parallel_gb300/_build/libcycasgpu.so``.
@@ -37,6 +38,7 @@ UNITS = [
     ("capi.cu", "nvcc", []),
     ("noalloc.cu", "nvcc", []),
     ("server.cpp", "cxx", []),
+    ("mesh_tables.cpp", "cxx", []),
     ("result_io.cpp", "cxx", ["-ffp-contract=off"]),
 ]
 # bench-only: the FP64/FP32 FMA-rate probe bench.py uses for the FP64 roofline of the channel

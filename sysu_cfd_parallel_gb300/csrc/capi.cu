@@ -20,6 +20,7 @@
 #include "cycas_amg.h"
 #include "cycas_device.h"
 #include "cycas_host.h"
+#include "mesh_tables.h"
 
 struct cycas_case {
   cycas::HostCase hc;
@@ -269,41 +270,9 @@ void build_device_mesh(cycas_ctx& c, const cycas_mesh_view& v) {
     int t = v.bnd_type[i];
     require(t >= 1 && t <= 4, "boundary type must be wall/inlet/outlet/symmetry");
   }
-  std::vector<int> gface(6 * (size_t)n, -1), face_sm(6 * (size_t)n, -1), slot(6 * (size_t)n, -1), diag(n);
-  std::vector<int> rowptr(n + 1, 0), col;
-  col.reserve((size_t)n * 7);
-  std::vector<int> cols;
-  for (int i = 0; i < n; i++) {
-    int k = v.cell_nface[i];
-    require(k >= 1 && k <= 6, "cell_nface out of range");
-    int tmp[6];
-    cols.clear();
-    cols.push_back(i);
-    for (int j = 0; j < k; j++) {
-      int fid = v.cell_face[6 * (size_t)i + j];
-      require(fid >= 0 && fid < nf, "cell_face out of range");
-      require(v.face_cell1[fid] == i || v.face_cell2[fid] == i, "cell_face does not touch its cell");
-      tmp[j] = fid;
-      face_sm[(size_t)j * n + i] = fid;
-      int nbh = v.face_cell2[fid] < 0 ? -1 : (v.face_cell1[fid] == i ? v.face_cell2[fid] : v.face_cell1[fid]);
-      if (nbh >= 0) cols.push_back(nbh);
-    }
-    std::sort(tmp, tmp + k);
-    for (int j = 0; j < k; j++) gface[(size_t)j * n + i] = tmp[j];
-    std::sort(cols.begin(), cols.end());
-    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-    rowptr[i + 1] = rowptr[i] + (int)cols.size();
-    int base = (int)col.size();
-    for (int cc : cols) col.push_back(cc);
-    for (int j = 0; j < k; j++) {
-      int fid = tmp[0];
-      fid = v.cell_face[6 * (size_t)i + j];
-      int nbh = v.face_cell2[fid] < 0 ? -1 : (v.face_cell1[fid] == i ? v.face_cell2[fid] : v.face_cell1[fid]);
-      if (nbh >= 0) slot[(size_t)j * n + i] = base + (int)(std::lower_bound(cols.begin(), cols.end(), nbh) - cols.begin());
-    }
-    diag[i] = base + (int)(std::lower_bound(cols.begin(), cols.end(), i) - cols.begin());
-  }
-  m.nnz = (int)col.size();
+  // CSR pattern, slots, diagonals and per-cell face orders (checks the cells' face lists)
+  const MeshTables T = mesh_tables(n, nf, v.cell_nface, v.cell_face, v.face_cell1, v.face_cell2);
+  m.nnz = (int)T.col.size();
   // boundary lists in boundary order
   std::vector<int> inl, outl, sym;
   std::vector<std::vector<int>> wall_of_cell;
@@ -340,14 +309,14 @@ void build_device_mesh(cycas_ctx& c, const cycas_mesh_view& v) {
   m.f_c2 = c.upload(v.face_cell2, nf);
   m.f_bnd = c.upload(v.face_bnd, nf);
   m.c_nface = c.upload(v.cell_nface, n);
-  m.c_face = c.upload(face_sm.data(), 6L * n);
-  m.c_gface = c.upload(gface.data(), 6L * n);
-  m.c_slot = c.upload(slot.data(), 6L * n);
-  m.c_diag = c.upload(diag.data(), n);
+  m.c_face = c.upload(T.face_sm.data(), 6L * n);
+  m.c_gface = c.upload(T.gface.data(), 6L * n);
+  m.c_slot = c.upload(T.slot.data(), 6L * n);
+  m.c_diag = c.upload(T.diag.data(), n);
   m.b_face = c.upload(v.bnd_face, nb);
   m.b_type = c.upload(v.bnd_type, nb);
-  m.rowptr = c.upload(rowptr.data(), n + 1);
-  m.col = c.upload(col.data(), m.nnz);
+  m.rowptr = c.upload(T.rowptr.data(), n + 1);
+  m.col = c.upload(T.col.data(), m.nnz);
   m.n_inlet = (int)inl.size();
   m.n_outlet = (int)outl.size();
   m.n_sym = (int)sym.size();

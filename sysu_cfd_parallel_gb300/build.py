@@ -39,6 +39,7 @@ UNITS = [
     ("noalloc.cu", "nvcc", []),
     ("server.cpp", "cxx", []),
     ("mesh_tables.cpp", "cxx", []),
+    ("union_mesh.cpp", "cxx", []),
     ("result_io.cpp", "cxx", ["-ffp-contract=off"]),
 ]
 # bench-only: the FP64/FP32 FMA-rate probe bench.py uses for the FP64 roofline of the channel

@@ -8,16 +8,14 @@
 // every coarse non-zero, the fine non-zeros that add into it (in ascending order), so the
 // device rebuilds the coarse values each iteration with deterministic gathers.
 #include <algorithm>
-#include <atomic>
 #include <exception>
 #include <memory>
 #include <numeric>
 #include <stdexcept>
-#include <system_error>
-#include <thread>
 #include <vector>
 
 #include "cycas_amg.h"
+#include "host_threads.h"
 
 namespace cycas {
 
@@ -251,48 +249,6 @@ long sell_entries(const AmgHostLevel& L) {
     p += cnt[v];
   }
   return total;
-}
-
-// Runs job(c) for every case c, the largest (by work[c]) first, on up to 16 of the host's
-// hardware threads; every job writes only its own case's slices, so the result does not depend
-// on the thread count.  Returns the exception each case's job raised (null where none).
-template <class Job>
-std::vector<std::exception_ptr> for_each_case(const std::vector<long>& work, const Job& job) {
-  const int n = (int)work.size();
-  std::vector<int> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
-  const long total = std::accumulate(work.begin(), work.end(), 0L);
-  const int hw = (int)std::thread::hardware_concurrency();
-  // small setups stay on the calling thread (starting threads would cost more than the work)
-  const int nt = total < (1L << 16) ? 1 : std::max(1, std::min(std::min(n, hw), 16));
-  std::vector<std::exception_ptr> err(n);
-  std::atomic<int> next{0};
-  auto run = [&]() {
-    for (int q = next++; q < n; q = next++) {
-      try {
-        job(order[q]);
-      } catch (...) {
-        err[order[q]] = std::current_exception();
-      }
-    }
-  };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nt; t++) {
-    try {
-      pool.emplace_back(run);
-    } catch (const std::system_error&) {  // no more threads: the ones running share the cases
-      break;
-    }
-  }
-  run();
-  for (auto& th : pool) th.join();
-  return err;
-}
-
-void rethrow_first(const std::vector<std::exception_ptr>& err) {
-  for (const auto& e : err)
-    if (e) std::rethrow_exception(e);
 }
 
 }  // namespace

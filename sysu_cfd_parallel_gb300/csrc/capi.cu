@@ -967,99 +967,7 @@ void set_field(cycas_ctx& c, const char* name, const double* src, long n) {
 }
 
 // ---------------------------------------------------------------- batches
-// Concatenates independent cases into one mesh.  Cells, boundaries and vertices are appended
-// case by case; faces are renumbered so that the boundary faces of all cases come first (in
-// case order) followed by all interior faces (in case order).  Each case keeps the reference's
-// own numbering properties: boundary b is face b, and the faces of every cell keep their
-// relative order.
-struct UnionMesh {
-  HostCase h;                // topology + InitFlowField arrays of the union
-  std::vector<int> cell0, bnd0, iface0;  // iface0: first interior face of each case (union index)
-};
-
-UnionMesh build_union(const std::vector<const HostCase*>& hs) {
-  UnionMesh u;
-  HostCase& U = u.h;
-  const int nc = (int)hs.size();
-  int NC = 0, NB = 0, NF = 0, NV = 0;
-  for (const HostCase* h : hs) {
-    NC += h->ncel;
-    NB += h->nbnd;
-    NF += h->nfac;
-    NV += h->nvrt;
-  }
-  U.ncel = NC;
-  U.nbnd = NB;
-  U.nfac = NF;
-  U.nvrt = NV;
-  U.face_cell1.resize(NF);
-  U.face_cell2.resize(NF);
-  U.face_bnd.resize(NF);
-  U.face_vertices.resize(4L * NF);
-  u.cell0.assign(nc + 1, 0);
-  u.bnd0.assign(nc + 1, 0);
-  u.iface0.assign(nc + 1, 0);
-  int c0 = 0, b0 = 0, i0 = NB, v0 = 0;
-  for (int k = 0; k < nc; k++) {
-    const HostCase& h = *hs[k];
-    u.cell0[k] = c0;
-    u.bnd0[k] = b0;
-    u.iface0[k] = i0;
-    for (int f = 0; f < h.nfac; f++)
-      if ((h.face_bnd[f] >= 0) != (f < h.nbnd) || (f < h.nbnd && h.face_bnd[f] != f))
-        throw StatusError(CYCAS_ERR_MESH, "a batched case does not number its boundary faces first");
-    auto fmap = [&](int f) { return f < h.nbnd ? b0 + f : i0 + (f - h.nbnd); };
-    for (int f = 0; f < h.nfac; f++) {
-      const int g = fmap(f);
-      U.face_cell1[g] = h.face_cell1[f] + c0;
-      U.face_cell2[g] = h.face_cell2[f] >= 0 ? h.face_cell2[f] + c0 : h.face_cell2[f];
-      U.face_bnd[g] = h.face_bnd[f] >= 0 ? h.face_bnd[f] + b0 : h.face_bnd[f];
-      for (int q = 0; q < 4; q++) U.face_vertices[4L * g + q] = h.face_vertices[4L * f + q] + v0;
-    }
-    for (int i = 0; i < h.ncel; i++) {
-      U.cell_nface.push_back(h.cell_nface[i]);
-      U.cell_rid.push_back(h.cell_rid[i]);
-      for (int j = 0; j < 6; j++) {
-        const int f = h.cell_face[6L * i + j], cc = h.cell_cell[6L * i + j];
-        U.cell_face.push_back(f >= 0 ? fmap(f) : f);
-        U.cell_cell.push_back(cc >= 0 ? cc + c0 : cc);
-      }
-      for (int q = 0; q < 8; q++) U.cell_vertices.push_back(h.cell_vertices[8L * i + q] + v0);
-    }
-    for (int b = 0; b < h.nbnd; b++) {
-      U.bnd_face.push_back(fmap(h.bnd_face[b]));
-      U.bnd_type.push_back(h.bnd_type[b]);
-      U.bnd_rid.push_back(h.bnd_rid[b]);
-    }
-    U.vert.insert(U.vert.end(), h.vert.begin(), h.vert.end());
-    auto cat = [](std::vector<double>& dst, const std::vector<double>& src) { dst.insert(dst.end(), src.begin(), src.end()); };
-    cat(U.U, h.U);
-    cat(U.V, h.V);
-    cat(U.W, h.W);
-    cat(U.P, h.P);
-    cat(U.R, h.R);
-    cat(U.T, h.T);
-    cat(U.VisLam, h.VisLam);
-    cat(U.VisTur, h.VisTur);
-    cat(U.TE, h.TE);
-    cat(U.ED, h.ED);
-    cat(U.BU, h.BU);
-    cat(U.BV, h.BV);
-    cat(U.BW, h.BW);
-    cat(U.BRo, h.BRo);
-    cat(U.BTem, h.BTem);
-    cat(U.BTE, h.BTE);
-    cat(U.BED, h.BED);
-    c0 += h.ncel;
-    b0 += h.nbnd;
-    i0 += h.nfac - h.nbnd;
-    v0 += h.nvrt;
-  }
-  u.cell0[nc] = c0;
-  u.bnd0[nc] = b0;
-  u.iface0[nc] = i0;
-  return u;
-}
+// (the union of a batch's cases: build_union, union_mesh.cpp)
 
 // Teams for the batched Krylov launches: a case with at least N/G rows (N rows in all, G CTAs)
 // gets a team of about rows*G/N CTAs of its own; the smaller cases are spread over single-CTA

@@ -52,6 +52,20 @@ void build_faces(HostCase& hc);
 void init_fields(HostCase& hc);
 void load_case(HostCase& hc, const std::string& paramPath, bool msh_binary = false);
 
+// ---------------------------------------------------------------- batches (union_mesh.cpp)
+// Independent cases concatenated into one mesh.  Cells, boundaries and vertices are appended
+// case by case; faces are renumbered so that the boundary faces of all cases come first (in
+// case order) followed by all interior faces (in case order).  Each case keeps the reference's
+// own numbering properties: boundary b is face b, and the faces of every cell keep their
+// relative order.
+struct UnionMesh {
+  HostCase h;                            // topology + InitFlowField arrays of the union
+  std::vector<int> cell0, bnd0, iface0;  // iface0: first interior face of each case (union index)
+};
+// Every case fills its own slices of the union on the host's threads.  Throws MeshError for the
+// first case (in case order) that does not number its boundary faces first.
+UnionMesh build_union(const std::vector<const HostCase*>& hs);
+
 // ---------------------------------------------------------------- result files (result_io.cpp)
 // The cell fields one case writes, each [ncel] on the host (TE and ED only read with k-epsilon).
 struct CellFieldsView {

@@ -40,6 +40,7 @@ UNITS = [
     ("server.cpp", "cxx", []),
     ("mesh_tables.cpp", "cxx", []),
     ("union_mesh.cpp", "cxx", []),
+    ("batch_schedule.cpp", "cxx", []),
     ("result_io.cpp", "cxx", ["-ffp-contract=off"]),
 ]
 # bench-only: the FP64/FP32 FMA-rate probe bench.py uses for the FP64 roofline of the channel

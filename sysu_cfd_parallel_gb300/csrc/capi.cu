@@ -20,6 +20,7 @@
 #include "cycas_amg.h"
 #include "cycas_device.h"
 #include "cycas_host.h"
+#include "batch_schedule.h"
 #include "mesh_tables.h"
 
 struct cycas_case {
@@ -969,91 +970,22 @@ void set_field(cycas_ctx& c, const char* name, const double* src, long n) {
 // ---------------------------------------------------------------- batches
 // (the union of a batch's cases: build_union, union_mesh.cpp)
 
-// Teams for the batched Krylov launches: a case with at least N/G rows (N rows in all, G CTAs)
-// gets a team of about rows*G/N CTAs of its own; the smaller cases are spread over single-CTA
-// teams, largest first onto the least loaded team.
-// G: CTAs of the Krylov launches (at most the co-resident maximum); factor scales the row
-// share that earns a case its own team.
+// Teams for the batched Krylov launches (team_schedule, batch_schedule.cpp), uploaded as the
+// device schedule.  G: CTAs of the Krylov launches (at most the co-resident maximum); factor
+// scales the row share that earns a case its own team.
 void build_schedule(cycas_ctx& c, int G, double factor) {
   const int nc = c.ncases;
   G = std::max(1, std::min(G, c.kw.nblocks));
-  long N = 0;
-  for (int k = 0; k < nc; k++) N += c.case_hi[k] - c.case_lo[k];
-  const double target = factor * (double)N / G;
-  std::vector<int> k_of(nc, 0);
-  int used = 0;
-  bool small = false;
-  for (int k = 0; k < nc; k++) {
-    const int rows = c.case_hi[k] - c.case_lo[k];
-    if (rows >= target) {
-      k_of[k] = std::max(1, (int)(rows / target));
-      used += k_of[k];
-    } else {
-      small = true;
-    }
-  }
-  const int avail = G - (small ? 1 : 0);
-  while (used > avail) {
-    int big = -1;
-    for (int k = 0; k < nc; k++)
-      if (k_of[k] > 1 && (big < 0 || k_of[k] > k_of[big])) big = k;
-    if (big < 0) {  // every big case has one CTA: the smallest of them joins the small cases
-      int sm = -1;
-      for (int k = 0; k < nc; k++)
-        if (k_of[k] == 1 && (sm < 0 || c.case_hi[k] - c.case_lo[k] < c.case_hi[sm] - c.case_lo[sm])) sm = k;
-      k_of[sm] = 0;
-      small = true;
-    } else {
-      k_of[big]--;
-    }
-    used--;
-  }
-  std::vector<int> cta_team, cta_rank, team_size, team_cta0, team_case0, case_list;
-  auto add_team = [&](int size, const std::vector<int>& cases) {
-    const int t = (int)team_size.size();
-    team_cta0.push_back((int)cta_team.size());
-    team_size.push_back(size);
-    team_case0.push_back((int)case_list.size());
-    case_list.insert(case_list.end(), cases.begin(), cases.end());
-    for (int r = 0; r < size; r++) {
-      cta_team.push_back(t);
-      cta_rank.push_back(r);
-    }
-  };
-  for (int k = 0; k < nc; k++)
-    if (k_of[k] > 0) add_team(k_of[k], {k});
-  const int rest = G - (int)cta_team.size();
-  if (small) {
-    require(rest >= 1, "batch schedule left no CTA for the small cases");
-    std::vector<int> order;
-    for (int k = 0; k < nc; k++)
-      if (k_of[k] == 0) order.push_back(k);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-      return c.case_hi[a] - c.case_lo[a] > c.case_hi[b] - c.case_lo[b];
-    });
-    const int nteam = std::min(rest, (int)order.size());
-    std::vector<long> load(nteam, 0);
-    std::vector<std::vector<int>> lists(nteam);
-    for (int k : order) {
-      int t = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-      lists[t].push_back(k);
-      load[t] += c.case_hi[k] - c.case_lo[k];
-    }
-    for (int t = 0; t < nteam; t++) {
-      std::sort(lists[t].begin(), lists[t].end());
-      add_team(1, lists[t]);
-    }
-  }
-  team_case0.push_back((int)case_list.size());
-  c.nteams = (int)team_size.size();
-  c.sched_grid = (int)cta_team.size();
+  const TeamSchedule S = team_schedule(c.case_lo, c.case_hi, G, factor);
+  c.nteams = (int)S.team_size.size();
+  c.sched_grid = (int)S.cta_team.size();
   BatchSchedule hs;
-  hs.cta_team = c.upload(cta_team.data(), (long)cta_team.size());
-  hs.cta_rank = c.upload(cta_rank.data(), (long)cta_rank.size());
-  hs.team_size = c.upload(team_size.data(), (long)team_size.size());
-  hs.team_cta0 = c.upload(team_cta0.data(), (long)team_cta0.size());
-  hs.team_case0 = c.upload(team_case0.data(), (long)team_case0.size());
-  hs.case_list = c.upload(case_list.data(), (long)case_list.size());
+  hs.cta_team = c.upload(S.cta_team.data(), (long)S.cta_team.size());
+  hs.cta_rank = c.upload(S.cta_rank.data(), (long)S.cta_rank.size());
+  hs.team_size = c.upload(S.team_size.data(), (long)S.team_size.size());
+  hs.team_cta0 = c.upload(S.team_cta0.data(), (long)S.team_cta0.size());
+  hs.team_case0 = c.upload(S.team_case0.data(), (long)S.team_case0.size());
+  hs.case_list = c.upload(S.case_list.data(), (long)S.case_list.size());
   hs.case_lo = c.upload(c.case_lo.data(), nc);
   hs.case_hi = c.upload(c.case_hi.data(), nc);
   c.d_sched = c.upload(&hs, 1);

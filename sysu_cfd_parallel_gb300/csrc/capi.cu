@@ -2007,9 +2007,16 @@ int cycas_batch_autotune(cycas_ctx* c, int32_t iters, int32_t* best_grid, double
     const int G0 = c->kw.nblocks;
     const int grids[3] = {G0, std::max(1, (3 * G0) / 4), std::max(1, G0 / 2)};
     const double factors[3] = {0.5, 1.0, 2.0};
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    struct Events {  // destroyed on every way out, errors included
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      ~Events() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+      }
+    } ev;
+    CK(cudaEventCreate(&ev.e0));
+    CK(cudaEventCreate(&ev.e1));
+    cudaEvent_t e0 = ev.e0, e1 = ev.e1;
     const bool graph = c->use_graph;
     int bg = G0;
     double bf = 1.0, bms = 1e300;
@@ -2033,14 +2040,12 @@ int cycas_batch_autotune(cycas_ctx* c, int32_t iters, int32_t* best_grid, double
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         if (rc == CYCAS_NOT_CONVERGED) rc = CYCAS_OK;
-        if (ms < bms) {
+        if (rc == CYCAS_OK && ms < bms) {  // a schedule whose iterations failed stopped early: not a candidate
           bms = ms;
           bg = grids[gi];
           bf = factors[fi];
         }
       }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     build_schedule(*c, bg, bf);
     if (c->gexec) {
       CK(cudaStreamSynchronize(c->stream));

@@ -1254,6 +1254,9 @@ int cycas_create(const cycas_mesh_view* mesh, const cycas_params* params, const 
   return guard([&]() -> int {
     require(mesh && params && out, "null argument");
     *out = nullptr;
+    // the kernels read p' at this cell: checked before anything reaches the device
+    require(mesh->ncel <= 0 || (params->cell_pressure_ref >= 0 && params->cell_pressure_ref < mesh->ncel),
+            "PressureRef cell out of range");
     cycas_ctx* c = new cycas_ctx();
     try {
       init_ctx(*c, params, opt);

@@ -273,6 +273,20 @@ def test_library_exports_every_declared_function():
     assert sorted(capi.EXPORTS) == names
 
 
+@pytest.mark.parametrize("ref", [-1, 8, 1000])
+def test_create_rejects_a_reference_cell_outside_the_mesh(ref):
+    """The kernels read p' at cellPressureRef: a value outside the mesh is an argument error,
+    reported before anything reaches a device (so this runs without one)."""
+    L = capi.load()
+    mesh = capi.MeshView()
+    mesh.ncel, mesh.nfac, mesh.nbnd, mesh.nvrt = 8, 36, 24, 27
+    p = capi.Params()
+    p.cell_pressure_ref = ref
+    ctx = C.c_void_p()
+    assert L.cycas_create(C.byref(mesh), C.byref(p), None, C.byref(ctx)) == capi.CYCAS_ERR_INVALID
+    assert capi.last_error() == "PressureRef cell out of range" and not ctx.value
+
+
 def test_defaults_follow_reference():
     o = capi.Options()
     capi.load().cycas_options_default(C.byref(o))

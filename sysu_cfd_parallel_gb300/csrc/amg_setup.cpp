@@ -192,7 +192,7 @@ Sell sell32(const AmgHostLevel& L) {
 // tail = the shortest suffix of levels ending at the coarsest whose arrays fit the budget;
 // columns are stored in 16 bits, so a tail level has fewer than 65536 rows.  sell[l]: entries of
 // level l's SELL-32 layout
-TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& nnz, const std::vector<int>& sell) {
+TailLayout tail_layout(const std::vector<int>& n, const std::vector<int>& sell) {
   TailLayout T{};
   const int L = (int)n.size();
   auto level_bytes = [&](int l) -> long {
@@ -468,7 +468,7 @@ void amg_setup_cases(AmgHostView& v, int n, const int* rowptr, const int* col, c
     cd.hi = hi[c];
     cd.nlev = (int)H(c).lv.size();
     cd.coarse_inv = v.coarse_inv + inv_off[c];
-    cd.tl = tail_layout(ln, lz, ls);
+    cd.tl = tail_layout(ln, ls);
     for (int l = 0; l < cd.nlev; l++) {
       AmgDevLevel& e = v.levels[c][l];
       e.sell_ptr = nullptr;

@@ -23,6 +23,11 @@ iterations with the reference's own solvers and ILU(0), every system to rtol 1e-
 (-ksp_rtol 1e-10): residual history, Krylov log, and the L2 norm and sum of u, v, w, p (the
 fields themselves would be megabytes).
 
+``channel_coarse/ref_ilu.npz``: the configured k-epsilon channel's physics on a coarse mesh
+(50x5x5 hexahedra split into 6 jittered Kuhn tetrahedra each, 7,500 cells, jitter 0.15h, seed
+2026) for its first 10 SIMPLE iterations at the reference's own tolerances and ILU(0): residual
+history, Krylov log, and the L2 norm and sum of u, v, w, p, k, epsilon.
+
 Needs the reference tree (REF, default /root/reference) and g++.  Run from the repository root:
     python tests/golden/make_ref_golden.py
 """
@@ -129,9 +134,36 @@ def cavity48_fixture():
     print("cavity48 iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
 
 
+def write_channel_coarse(d):
+    """The coarse k-epsilon channel (meshgen writes the same bytes every time)."""
+    from sysu_cfd_parallel_gb300 import meshgen
+    return os.path.dirname(meshgen.write_case(d, "channel", nx=50, ny=5, nz=5, jitter=0.15, seed=2026,
+                                              steps=CHANNEL_COARSE_STEPS))
+
+
+CHANNEL_COARSE_STEPS = 10
+
+
+def channel_coarse_fixture():
+    tmp = tempfile.mkdtemp()
+    try:
+        o = run_reference(write_channel_coarse(tmp), CHANNEL_COARSE_STEPS, [])
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    keep = {"residual": o["residual"].reshape(-1, 10), "ksp": o["ksp"].reshape(-1, 4), "info": o["info"],
+            "steps": np.array(CHANNEL_COARSE_STEPS)}
+    for nm in ("U", "V", "W", "P", "TE", "ED"):
+        keep[nm + "_norm"] = np.array(np.linalg.norm(o[nm]))
+        keep[nm + "_sum"] = np.array(np.sum(o[nm]))
+    os.makedirs(os.path.join(HERE, "channel_coarse"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "channel_coarse", "ref_ilu.npz"), **keep)
+    print("channel_coarse iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
+
+
 def main():
     build()
     cavity48_fixture()
+    channel_coarse_fixture()
     tmp = tempfile.mkdtemp()
     os.makedirs(os.path.join(HERE, "cavity20"), exist_ok=True)
     for name, (steps, opts) in RUNS.items():

@@ -101,8 +101,10 @@ int cycas_case_load(const char* param_path, cycas_case** out);
  * type, int32 ntag, ntag int32 tags, one-based int32 vertex ids} per element. */
 #define CYCAS_LOAD_MSH_BINARY 1
 int cycas_case_load_ex(const char* param_path, int32_t flags, cycas_case** out);
+/* releases a loaded case (no counterpart: the reference keeps its mesh until the process exits) */
 void cycas_case_free(cycas_case* c);
-/* dims: [0] Ncel [1] Nfac [2] Nbnd [3] Nvrt [4] TurModel [5] MaxStep [6] cellPressureRef [7] nnz */
+/* dims: [0] Ncel [1] Nfac [2] Nbnd [3] Nvrt (the solver's mesh sizes, NS/navier.h:104) [4] TurModel
+ * [5] MaxStep [6] cellPressureRef (the options pool, NS/navier.cpp:475-516) [7] nnz */
 int cycas_case_dims(const cycas_case* c, int64_t dims[8]);
 /* residual stop value and relaxation factors of the case (dbOptions, NS/navier.cpp:777-791) */
 int cycas_case_params(const cycas_case* c, double* residual_steady, double urf[8], double gravity[3]);
@@ -207,21 +209,28 @@ typedef struct {
   int32_t reserved;
 } cycas_options;
 
-/* fills defaults: the reference's Krylov methods (GMRES(30); CG for pressure), Jacobi,
- * reference tolerances, device 0 */
+/* fills defaults: the reference's Krylov methods (GMRES(30); CG for pressure; the KSP set-up of
+ * DataPartition::solve*, NS/MPIStructure.cpp:234-531), Jacobi, the reference's per-call
+ * tolerances (NS/navier_velocity.cpp:28, navier_pressure.cpp:28, navier_scalar.cpp:98), device 0 */
 void cycas_options_default(cycas_options* o);
 
 /* ---- device context ------------------------------------------------------------------ */
 typedef struct cycas_ctx cycas_ctx;
 
-/* Copies the mesh (and computes geometry if not given) into device memory. */
+/* Replaces the NavierStokesSolver constructor (NS/navier.cpp:749) and DataPartition's matrix and
+ * vector set-up (NS/MPIStructure.cpp:9-55, 204-233): copies the mesh (and computes geometry if
+ * not given) into device memory.  cycas_create_from_case does the same for a loaded case and
+ * sets InitFlowField's fields (NS/navier.cpp:588-697); cycas_destroy replaces
+ * ~NavierStokesSolver (NS/navier.cpp:817) and DataPartition::deinit (NS/MPIStructure.cpp:56). */
 int cycas_create(const cycas_mesh_view* mesh, const cycas_params* params, const cycas_options* opt,
                  cycas_ctx** out);
 /* Same from a loaded case; fields start at the case's InitFlowField state. */
 int cycas_create_from_case(const cycas_case* c, const cycas_options* opt, cycas_ctx** out);
 void cycas_destroy(cycas_ctx* ctx);
 
-/* Named device arrays: cell fields U V W P R T TE ED deltaP VisLam VisTur Apr; face field RUFace;
+/* Direct access to the solver's arrays (FlowField, NS/BasicType.h:74-148; RUFace, NS/navier.h:128;
+ * the Face/Cell geometry, NS/BasicType.h:151-243).
+ * Named device arrays: cell fields U V W P R T TE ED deltaP VisLam VisTur Apr; face field RUFace;
  * boundary arrays BRo BU BV BW BPre BTE BED; gradients dUdX dVdX dWdX dPdX dPhidX ([3*Ncel]);
  * geometry face_x face_n face_area face_lambda face_rlencos face_xpac face_xnac cell_vol cell_x
  * bnd_distance; matrix values A_val (+ b0 b1 b2 right-hand sides) of the last assembled system.
@@ -259,9 +268,8 @@ typedef struct {
  * vec_max(residual).  Returns CYCAS_NOT_CONVERGED if any solve reported reason < 0. */
 int cycas_simple_iteration(cycas_ctx* ctx, double residual[10], double* resmax, cycas_iter_stats* stats);
 
-/* Runs n iterations back to back on the device and reads the residual history once at the
- * end (no host synchronisation between iterations). res_hist: [n*10], resmax: [n], its: [n*8]. */
-/* one SIMPLE-C iteration with the caller's host fields as its state: the nin input fields are
+/* One SIMPLE-C iteration (the loop body of NSSolve, NS/navier.cpp:60-111) with the caller's host
+ * fields as its state: the nin input fields are
  * uploaded before the stage that first reads them, the nout output fields downloaded once they
  * are final, and both kinds of copies overlap the iteration where its stages allow (inputs of
  * the k-epsilon stage upload during momentum and pressure; velocity, pressure and face-flux
@@ -272,6 +280,10 @@ int cycas_simple_iteration_io(cycas_ctx* c, int32_t nin, const char* const* in_n
                               const int64_t* in_n, int32_t nout, const char* const* out_names,
                               double* const* out_dst, const int64_t* out_n, double residual[10], double* resmax,
                               cycas_iter_stats* stats);
+/* n passes of the loop body of NSSolve (NS/navier.cpp:60-111), as n calls of
+ * cycas_simple_iteration, back to back on the device, the residual history read once at the end
+ * (no host synchronisation between iterations): res_hist[10k..], resmax[k], Krylov its[8k..] and
+ * reasons[8k..] of pass k */
 int cycas_simple_iterations(cycas_ctx* ctx, int32_t n, double* res_hist, double* resmax, int32_t* its,
                             int32_t* reasons);
 
@@ -293,7 +305,12 @@ int cycas_solve_steady(cycas_ctx* ctx, int32_t max_step, double residual_steady,
 #define CYCAS_RESTART_RESTORE 1
 int cycas_restart_point(cycas_ctx* ctx, int32_t op);
 
-/* Individual stages for parity tests: bc_velocity bc_pressure bc_deltap grad_uvwp grad_deltap
+/* The solver's members one at a time (SetBCVelocity/SetBCPressure/SetBCDeltaP,
+ * NS/navier_bc.cpp:8-181; Gradient, navier_gradient.cpp:12-74; BuildVelocityMatrix,
+ * navier_velocity.cpp:63-393; CalRUFace2, navier_velocity.cpp:425-477; BuildPressureMatrix,
+ * navier_pressure.cpp:99-232; the corrections, navier_pressure.cpp:45-70 and 235-278;
+ * UpdateTurKEpsilon, navier_scalar.cpp:11-197; SaveTransientOldData, navier.h:191).
+ * Individual stages for parity tests: bc_velocity bc_pressure bc_deltap grad_uvwp grad_deltap
  * build_velocity ruface2 build_pressure correct_cells correct_ruface calculate_velocity
  * calculate_pressure keps build_te (the k rows of keps) build_ed (the epsilon rows, on the
  * current k) energy build_energy save_transient clear_residual. */
@@ -310,7 +327,8 @@ typedef struct {
 } cycas_solve_stats;
 
 /* ---- measurement hooks ------------------------------------------------------------- */
-/* The CUDA stream (cudaStream_t) all work of the context is issued on. */
+/* The CUDA stream (cudaStream_t) all work of the context is issued on (no counterpart: a
+ * measurement hook). */
 int cycas_get_stream(cycas_ctx* ctx, void** stream);
 typedef struct {
   int64_t kernel_launches;   /* kernels this context launched since the last reset */
@@ -378,7 +396,8 @@ int cycas_solve_pressure(cycas_ctx* ctx, double tol, int32_t maxit, double* xp, 
 /* solveScarlar_GMRES (MPIStructure.cpp:378-446): As with bs. */
 int cycas_solve_scalar(cycas_ctx* ctx, double tol, int32_t maxit, double* xs, cycas_iter_stats* stats);
 
-/* Standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
+/* DataPartition::solve* (NS/MPIStructure.cpp:234-531) on a caller's matrix:
+ * standalone Krylov solve of A x = b for a CSR matrix in HOST memory (int32 rowptr[n+1],
  * col[nnz], double val[nnz]); b and x are host arrays, x holds the initial guess unless
  * guess_zero.  Same GMRES/PC as the SIMPLE path. */
 int cycas_csr_solve(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
@@ -413,7 +432,8 @@ int cycas_batch_autotune(cycas_ctx* ctx, int32_t iters, int32_t* best_grid, doub
 int cycas_batch_residuals(cycas_ctx* ctx, double* residual);
 
 /* Moves the state of case sc of batch src (fields, boundary values, face fluxes) into case dc
- * of batch dst; the two cases must be the same mesh.  Used when a batch is re-formed. */
+ * of batch dst; the two cases must be the same mesh.  Used when a batch is re-formed.  (Batches
+ * have no counterpart in the reference, nor do the two calls below.) */
 int cycas_batch_copy_case(cycas_ctx* dst, int32_t dc, cycas_ctx* src, int32_t sc);
 /* the slice of a per-cell or per-boundary field belonging to case k of a batch */
 int cycas_batch_case_field(cycas_ctx* ctx, int32_t k, const char* name, double* dst, int64_t n);
@@ -437,7 +457,8 @@ typedef struct {
   double t_arrival, t_admit, t_done;
   double resmax;       /* normalised residual at retirement */
 } cycas_request_result;
-/* estimated device bytes of a case in a batch (what admission counts against the budget) */
+/* estimated device bytes of a case in a batch (what admission counts against the budget); this and
+ * the cycas_server_* calls have no counterpart in the reference */
 double cycas_footprint_estimate(const cycas_case* c);
 int cycas_server_create(const cycas_options* opt, double hbm_budget_bytes, double residual_tol, int32_t max_iters,
                         int32_t keep_fields, cycas_server** out);

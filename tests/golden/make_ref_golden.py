@@ -28,6 +28,11 @@ fields themselves would be megabytes).
 2026) for its first 10 SIMPLE iterations at the reference's own tolerances and ILU(0): residual
 history, Krylov log, and the L2 norm and sum of u, v, w, p, k, epsilon.
 
+``channel_coarse_tr/ref_ilu.npz``: the same mesh run transient (Euler, dt 0.1, at most 6 outer
+iterations per step) with the energy equation and 290 K walls, for 3 time steps at the
+reference's tolerances and ILU(0): residual history of every outer iteration, Krylov log, and
+the L2 norm and sum of u, v, w, p, k, epsilon, T, rho.
+
 Needs the reference tree (REF, default /root/reference) and g++.  Run from the repository root:
     python tests/golden/make_ref_golden.py
 """
@@ -142,6 +147,14 @@ def write_channel_coarse(d):
 
 
 CHANNEL_COARSE_STEPS = 10
+CHANNEL_COARSE_TR_STEPS = 3
+
+
+def write_channel_coarse_tr(d):
+    """The coarse channel, transient with the energy equation (meshgen writes the same bytes)."""
+    from sysu_cfd_parallel_gb300 import meshgen
+    return os.path.dirname(meshgen.write_case(d, "channel", nx=50, ny=5, nz=5, jitter=0.15, seed=2026,
+                                              time=(0.1, 1.0, 6, "Euler"), energy=True, wall_t=290))
 
 
 def channel_coarse_fixture():
@@ -160,10 +173,27 @@ def channel_coarse_fixture():
     print("channel_coarse iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
 
 
+def channel_coarse_tr_fixture():
+    tmp = tempfile.mkdtemp()
+    try:
+        o = run_reference(write_channel_coarse_tr(tmp), CHANNEL_COARSE_TR_STEPS, [])
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    keep = {"residual": o["residual"].reshape(-1, 10), "ksp": o["ksp"].reshape(-1, 4), "info": o["info"],
+            "steps": np.array(CHANNEL_COARSE_TR_STEPS)}
+    for nm in ("U", "V", "W", "P", "TE", "ED", "T", "R"):
+        keep[nm + "_norm"] = np.array(np.linalg.norm(o[nm]))
+        keep[nm + "_sum"] = np.array(np.sum(o[nm]))
+    os.makedirs(os.path.join(HERE, "channel_coarse_tr"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "channel_coarse_tr", "ref_ilu.npz"), **keep)
+    print("channel_coarse_tr outer iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
+
+
 def main():
     build()
     cavity48_fixture()
     channel_coarse_fixture()
+    channel_coarse_tr_fixture()
     tmp = tempfile.mkdtemp()
     os.makedirs(os.path.join(HERE, "cavity20"), exist_ok=True)
     for name, (steps, opts) in RUNS.items():

@@ -141,6 +141,25 @@ def test_channel_coarse_k_epsilon_bit_exact(tmp_path):
     o.close()
 
 
+def test_channel_coarse_transient_energy_bit_exact(tmp_path):
+    """The same 7,500-tet channel run transient (Euler, dt 0.1) with the energy equation for 3
+    time steps: the residual of every outer iteration, every Krylov count, and the L2 norm and
+    sum of u, v, w, p, k, epsilon, T and rho equal the reference build's
+    (tests/golden/channel_coarse_tr/ref_ilu.npz)."""
+    from make_ref_golden import write_channel_coarse_tr
+    g = dict(np.load(os.path.join(GOLDEN, "channel_coarse_tr", "ref_ilu.npz")))
+    d = write_channel_coarse_tr(str(tmp_path))
+    o = _oracle(os.path.join(d, "param.in"), "ilu")
+    res, its = _run(o, int(g["steps"]), True)
+    assert res.shape == g["residual"].shape
+    assert np.array_equal(res.view(np.int64), g["residual"].view(np.int64)), np.abs(res - g["residual"]).max()
+    assert np.array_equal(its, g["ksp"][:, 1].astype(np.int32))
+    for nm in ("U", "V", "W", "P", "TE", "ED", "T", "R"):
+        x = o.get(nm)
+        assert np.linalg.norm(x) == g[nm + "_norm"] and np.sum(x) == g[nm + "_sum"], nm
+    o.close()
+
+
 def test_pow15_differs_from_libm_by_one_ulp_at_most():
     """TE^1.5 (the wall function's pow) in the two oracle modes: the once-rounded value the GPU
     computes and the C library's, on the k-epsilon channel fixture; the fields after its six

@@ -33,6 +33,11 @@ iterations per step) with the energy equation and 290 K walls, for 3 time steps 
 reference's tolerances and ILU(0): residual history of every outer iteration, Krylov log, and
 the L2 norm and sum of u, v, w, p, k, epsilon, T, rho.
 
+``cavity16g_dual/ref_ilu.npz``: a perfect-gas cavity (16^3 hexahedra, jitter 0.1h, walls 300 K,
+lid 330 K) with the reference's second-order "Dual" scheme (dt 0.05, at most 8 outer iterations
+per step) for 3 time steps at the reference's tolerances and ILU(0): residual history, Krylov
+log, and the L2 norm and sum of u, v, w, p, T, rho.
+
 Needs the reference tree (REF, default /root/reference) and g++.  Run from the repository root:
     python tests/golden/make_ref_golden.py
 """
@@ -148,6 +153,14 @@ def write_channel_coarse(d):
 
 CHANNEL_COARSE_STEPS = 10
 CHANNEL_COARSE_TR_STEPS = 3
+CAVITY16G_STEPS = 3
+
+
+def write_cavity16g_dual(d):
+    """The perfect-gas cavity with the Dual scheme (meshgen writes the same bytes every time)."""
+    from sysu_cfd_parallel_gb300 import meshgen
+    return os.path.dirname(meshgen.write_case(d, "cavity", n=16, jitter=0.1, seed=9, density=1, wall_t=300,
+                                              lid_t=330, time=(0.05, 1.0, 8, "Dual")))
 
 
 def write_channel_coarse_tr(d):
@@ -189,11 +202,28 @@ def channel_coarse_tr_fixture():
     print("channel_coarse_tr outer iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
 
 
+def cavity16g_fixture():
+    tmp = tempfile.mkdtemp()
+    try:
+        o = run_reference(write_cavity16g_dual(tmp), CAVITY16G_STEPS, [])
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    keep = {"residual": o["residual"].reshape(-1, 10), "ksp": o["ksp"].reshape(-1, 4), "info": o["info"],
+            "steps": np.array(CAVITY16G_STEPS)}
+    for nm in ("U", "V", "W", "P", "T", "R"):
+        keep[nm + "_norm"] = np.array(np.linalg.norm(o[nm]))
+        keep[nm + "_sum"] = np.array(np.sum(o[nm]))
+    os.makedirs(os.path.join(HERE, "cavity16g_dual"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "cavity16g_dual", "ref_ilu.npz"), **keep)
+    print("cavity16g_dual outer iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
+
+
 def main():
     build()
     cavity48_fixture()
     channel_coarse_fixture()
     channel_coarse_tr_fixture()
+    cavity16g_fixture()
     tmp = tempfile.mkdtemp()
     os.makedirs(os.path.join(HERE, "cavity20"), exist_ok=True)
     for name, (steps, opts) in RUNS.items():

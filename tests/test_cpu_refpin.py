@@ -160,6 +160,24 @@ def test_channel_coarse_transient_energy_bit_exact(tmp_path):
     o.close()
 
 
+def test_cavity16_perfect_gas_dual_bit_exact(tmp_path):
+    """A perfect-gas cavity (16^3 hexahedra) with the reference's "Dual" scheme for 3 time steps:
+    the residual of every outer iteration, every Krylov count, and the L2 norm and sum of u, v, w,
+    p, T and rho equal the reference build's (tests/golden/cavity16g_dual/ref_ilu.npz)."""
+    from make_ref_golden import write_cavity16g_dual
+    g = dict(np.load(os.path.join(GOLDEN, "cavity16g_dual", "ref_ilu.npz")))
+    d = write_cavity16g_dual(str(tmp_path))
+    o = _oracle(os.path.join(d, "param.in"), "ilu")
+    res, its = _run(o, int(g["steps"]), True)
+    assert res.shape == g["residual"].shape
+    assert np.array_equal(res.view(np.int64), g["residual"].view(np.int64)), np.abs(res - g["residual"]).max()
+    assert np.array_equal(its, g["ksp"][:, 1].astype(np.int32))
+    for nm in ("U", "V", "W", "P", "T", "R"):
+        x = o.get(nm)
+        assert np.linalg.norm(x) == g[nm + "_norm"] and np.sum(x) == g[nm + "_sum"], nm
+    o.close()
+
+
 def test_pow15_differs_from_libm_by_one_ulp_at_most():
     """TE^1.5 (the wall function's pow) in the two oracle modes: the once-rounded value the GPU
     computes and the C library's, on the k-epsilon channel fixture; the fields after its six

@@ -78,3 +78,17 @@ def test_host_replicas_bounded():
     nproc, cores = bench.host_replicas()
     assert 1 <= nproc <= cores
     assert bench.host_replicas(per_replica_gb=1e9)[0] == 1
+
+
+def test_l2_flush_is_larger_than_l2_and_reports_when_off():
+    """The flush writes twice the GB300's 129 MB L2; where its buffer cannot be made (here: no
+    GPU) it is off, calling it does nothing, and the line's l2 note says so instead of claiming a
+    flush."""
+    assert bench.L2_FLUSH_BYTES >= 2 * 129 * 10**6
+    f = bench.L2Flush("cuda:0", None)
+    assert f.state.startswith("off (")
+    f(None)
+    note = bench.l2_note(f)
+    assert note.startswith("no flush") and "flushed" not in note
+    f.state = "on"
+    assert bench.l2_note(f).startswith("L2 flushed before every timed solve")

@@ -23,6 +23,10 @@ iterations with the reference's own solvers and ILU(0), every system to rtol 1e-
 (-ksp_rtol 1e-10): residual history, Krylov log, and the L2 norm and sum of u, v, w, p (the
 fields themselves would be megabytes).
 
+``cavity48/ref_ilu_converged.npz``: the bench's cavity (48^3) run by the reference build to its
+own stop test (NSSolve's ResMax < 1e-6, the param's residual) at its own tolerances and ILU(0):
+ResMax of every SIMPLE iteration (about 15 minutes on one core; not run by main()).
+
 ``channel_coarse/ref_ilu.npz``: the configured k-epsilon channel's physics on a coarse mesh
 (50x5x5 hexahedra split into 6 jittered Kuhn tetrahedra each, 7,500 cells, jitter 0.15h, seed
 2026) for its first 10 SIMPLE iterations at the reference's own tolerances and ILU(0): residual
@@ -142,6 +146,23 @@ def cavity48_fixture():
     os.makedirs(os.path.join(HERE, "cavity48"), exist_ok=True)
     np.savez_compressed(os.path.join(HERE, "cavity48", "ref_ilu_tight.npz"), **keep)
     print("cavity48 iterations", o["residual"].size // 10, "solves", o["ksp"].size // 4)
+
+
+def cavity48_converged_fixture():
+    """The bench cavity to the reference's own stop test; keeps ResMax of every iteration."""
+    from sysu_cfd_parallel_gb300 import meshgen
+    tmp = tempfile.mkdtemp()
+    try:
+        d = os.path.dirname(meshgen.write_case(tmp, "cavity", n=48, steps=3000, residual=1e-6))
+        o = run_reference(d, 3000, [])
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    res = o["residual"].reshape(-1, 10)
+    resmax = np.maximum(res.max(axis=1), 0.0)  # vec_max of localRes, floored at 0 (navier.cpp:94-96)
+    os.makedirs(os.path.join(HERE, "cavity48"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "cavity48", "ref_ilu_converged.npz"), resmax=resmax,
+                        residual_steady=np.array(1e-6))
+    print("cavity48 to the stop test: iterations", len(resmax), "last ResMax", resmax[-1])
 
 
 def write_channel_coarse(d):

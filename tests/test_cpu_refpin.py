@@ -123,6 +123,22 @@ def test_cavity48_first_iterations_bit_exact(tmp_path):
     o.close()
 
 
+def test_cavity48_reference_run_to_the_stop_test(tmp_path):
+    """The reference build ran the bench's cavity to its own stop test (ResMax < 1e-6) at its own
+    tolerances with ILU(0) (tests/golden/cavity48/ref_ilu_converged.npz): it stops at the first
+    iteration below 1e-6, iteration 863 -- the iteration at which the GPU path with its own
+    preconditioners stops too -- and its first iterations are the oracle's, bit for bit."""
+    from sysu_cfd_parallel_gb300 import meshgen
+    g = dict(np.load(os.path.join(GOLDEN, "cavity48", "ref_ilu_converged.npz")))
+    rm = g["resmax"]
+    assert len(rm) == 863 and rm[-1] < 1e-6 and np.all(rm[:-1] >= 1e-6)
+    d = os.path.dirname(meshgen.write_case(str(tmp_path), "cavity", n=48, steps=3000, residual=1e-6))
+    o = _oracle(os.path.join(d, "param.in"), "ilu")
+    r = o.iterate(5)
+    assert np.array_equal(np.asarray(r["resmax"]).view(np.int64), rm[:5].view(np.int64))
+    o.close()
+
+
 def test_channel_coarse_k_epsilon_bit_exact(tmp_path):
     """The configured k-epsilon channel's physics on a 7,500-tet jittered mesh for 10 SIMPLE
     iterations at the reference's tolerances with ILU(0): residual history, every Krylov count,

@@ -27,6 +27,11 @@ fields themselves would be megabytes).
 own stop test (NSSolve's ResMax < 1e-6, the param's residual) at its own tolerances and ILU(0):
 ResMax of every SIMPLE iteration (about 15 minutes on one core; not run by main()).
 
+``batch_cavities/ref_stop.npz``: the cavities of the batched workload (seed 4: n^3 hexahedra with
+n uniform in 8..40, jitter 0.1h, mu = 1/Re with Re log-uniform in [10, 1000]) that have at most
+16^3 cells, each run by the reference build to its own stop test (ResMax < 1e-6) with ILU(0):
+the SIMPLE iteration at which each stops (about 5 minutes; not run by main()).
+
 ``channel_coarse/ref_ilu.npz``: the configured k-epsilon channel's physics on a coarse mesh
 (50x5x5 hexahedra split into 6 jittered Kuhn tetrahedra each, 7,500 cells, jitter 0.15h, seed
 2026) for its first 10 SIMPLE iterations at the reference's own tolerances and ILU(0): residual
@@ -163,6 +168,43 @@ def cavity48_converged_fixture():
     np.savez_compressed(os.path.join(HERE, "cavity48", "ref_ilu_converged.npz"), resmax=resmax,
                         residual_steady=np.array(1e-6))
     print("cavity48 to the stop test: iterations", len(resmax), "last ResMax", resmax[-1])
+
+
+BATCH_SEED = 4  # the batched workload's master seed
+
+
+def batch_cavity_specs():
+    """(n, mesh seed, mu) of the batched workload's 256 cavities, in case order."""
+    rng = np.random.default_rng(BATCH_SEED)
+    ns = rng.integers(8, 41, size=256)
+    res = 10.0 ** rng.uniform(1.0, 3.0, size=256)
+    return [(int(ns[k]), 1000 + k, float(1.0 / res[k])) for k in range(256)]
+
+
+def write_batch_cavity(d, n, seed, mu):
+    from sysu_cfd_parallel_gb300 import meshgen
+    return os.path.dirname(meshgen.write_case(d, "cavity", n=n, jitter=0.1, seed=seed, steps=2000, mu=mu,
+                                              residual=1e-6))
+
+
+def batch_stop_fixture(max_n=16):
+    specs = batch_cavity_specs()
+    rows = [k for k in sorted(range(256), key=lambda k: (specs[k][0], k)) if specs[k][0] <= max_n]
+    stop = []
+    for k in rows:
+        tmp = tempfile.mkdtemp()
+        try:
+            o = run_reference(write_batch_cavity(tmp, *specs[k]), 2000, [])
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        stop.append(o["residual"].size // 10)  # NSSolve stopped at ResMax < 1e-6
+    k = np.array(rows)
+    os.makedirs(os.path.join(HERE, "batch_cavities"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "batch_cavities", "ref_stop.npz"), case=k,
+                        n=np.array([specs[i][0] for i in rows]), seed=np.array([specs[i][1] for i in rows]),
+                        mu=np.array([specs[i][2] for i in rows]), ref_stop=np.array(stop), jitter=np.array(0.1),
+                        residual=np.array(1e-6))
+    print("batch cavities up to n =", max_n, ":", len(rows), "cases")
 
 
 def write_channel_coarse(d):

@@ -139,6 +139,27 @@ def test_cavity48_reference_run_to_the_stop_test(tmp_path):
     o.close()
 
 
+def test_batch_cavities_stop_where_the_reference_stops(tmp_path):
+    """The batched workload's cavities up to 16^3 cells, each run by the reference build to its
+    own stop test (tests/golden/batch_cavities/ref_stop.npz): the oracle stops the three smallest
+    at the same SIMPLE iterations."""
+    from make_ref_golden import batch_cavity_specs, write_batch_cavity
+    g = dict(np.load(os.path.join(GOLDEN, "batch_cavities", "ref_stop.npz")))
+    specs = batch_cavity_specs()
+    assert all(specs[k][:2] == (int(n), int(s)) for k, n, s in zip(g["case"], g["n"], g["seed"]))
+    for i in range(3):
+        k = int(g["case"][i])
+        d = write_batch_cavity(str(tmp_path / str(k)), *specs[k])
+        o = _oracle(os.path.join(d, "param.in"), "ilu")
+        stop = None
+        for it in range(1, 2 * int(g["ref_stop"][i])):
+            if o.iterate(1)["resmax"][0] < 1e-6:
+                stop = it
+                break
+        assert stop == int(g["ref_stop"][i]), (k, stop, int(g["ref_stop"][i]))
+        o.close()
+
+
 def test_channel_coarse_k_epsilon_bit_exact(tmp_path):
     """The configured k-epsilon channel's physics on a 7,500-tet jittered mesh for 10 SIMPLE
     iterations at the reference's tolerances with ILU(0): residual history, every Krylov count,

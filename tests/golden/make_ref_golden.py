@@ -29,8 +29,8 @@ ResMax of every SIMPLE iteration (about 15 minutes on one core; not run by main(
 
 ``batch_cavities/ref_stop.npz``: the cavities of the batched workload (seed 4: n^3 hexahedra with
 n uniform in 8..40, jitter 0.1h, mu = 1/Re with Re log-uniform in [10, 1000]) that have at most
-16^3 cells, each run by the reference build to its own stop test (ResMax < 1e-6) with ILU(0):
-the SIMPLE iteration at which each stops (about 5 minutes; not run by main()).
+40^3 cells (all 256), each run by the reference build to its own stop test (ResMax < 1e-6) with
+ILU(0): the SIMPLE iteration at which each stops (about 20 minutes on 8 cores; not run by main()).
 
 ``channel_coarse/ref_ilu.npz``: the configured k-epsilon channel's physics on a coarse mesh
 (50x5x5 hexahedra split into 6 jittered Kuhn tetrahedra each, 7,500 cells, jitter 0.15h, seed
@@ -187,17 +187,22 @@ def write_batch_cavity(d, n, seed, mu):
                                               residual=1e-6))
 
 
-def batch_stop_fixture(max_n=16):
+def batch_stop_fixture(max_n=40, workers=8):
+    """Every case runs as its own reference process; `workers` of them at a time."""
+    from concurrent.futures import ThreadPoolExecutor
     specs = batch_cavity_specs()
     rows = [k for k in sorted(range(256), key=lambda k: (specs[k][0], k)) if specs[k][0] <= max_n]
-    stop = []
-    for k in rows:
+
+    def one(k):
         tmp = tempfile.mkdtemp()
         try:
             o = run_reference(write_batch_cavity(tmp, *specs[k]), 2000, [])
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
-        stop.append(o["residual"].size // 10)  # NSSolve stopped at ResMax < 1e-6
+        return o["residual"].size // 10  # NSSolve stopped at ResMax < 1e-6
+
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        stop = list(ex.map(one, rows))
     k = np.array(rows)
     os.makedirs(os.path.join(HERE, "batch_cavities"), exist_ok=True)
     np.savez_compressed(os.path.join(HERE, "batch_cavities", "ref_stop.npz"), case=k,

@@ -140,12 +140,13 @@ def test_cavity48_reference_run_to_the_stop_test(tmp_path):
 
 
 def test_batch_cavities_stop_where_the_reference_stops(tmp_path):
-    """The batched workload's cavities up to 16^3 cells, each run by the reference build to its
-    own stop test (tests/golden/batch_cavities/ref_stop.npz): the oracle stops the three smallest
-    at the same SIMPLE iterations."""
+    """The batched workload's 256 cavities, each run by the reference build to its own stop test
+    (tests/golden/batch_cavities/ref_stop.npz): the oracle stops the three smallest at the same
+    SIMPLE iterations."""
     from make_ref_golden import batch_cavity_specs, write_batch_cavity
     g = dict(np.load(os.path.join(GOLDEN, "batch_cavities", "ref_stop.npz")))
     specs = batch_cavity_specs()
+    assert len(g["case"]) == 256 and g["ref_stop"].sum() == 79640
     assert all(specs[k][:2] == (int(n), int(s)) for k, n, s in zip(g["case"], g["n"], g["seed"]))
     for i in range(3):
         k = int(g["case"][i])

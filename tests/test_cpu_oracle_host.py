@@ -287,6 +287,28 @@ def test_create_rejects_a_reference_cell_outside_the_mesh(ref):
     assert capi.last_error() == "PressureRef cell out of range" and not ctx.value
 
 
+def test_header_is_a_plain_c_abi(tmp_path):
+    """include/cycasgpu.h compiles as pedantic C99 and C++11, and a C program links the library and
+    calls a host entry point through it (no GPU needed for the defaults)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None or shutil.which("g++") is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    src.write_text('#include "cycasgpu.h"\n'
+                   "int main(void) { cycas_options o; cycas_options_default(&o);\n"
+                   "  return o.ksp[0].restart == 30 && o.ksp[1].restart == 30 ? 0 : 1; }\n")
+    inc = os.path.join(ROOT, "include")
+    flags = ["-Wall", "-Wextra", "-pedantic", "-Werror", "-I", inc, "-c", str(src)]
+    subprocess.run(["gcc", "-std=c99", *flags, "-o", str(tmp_path / "c.o")], check=True)
+    subprocess.run(["g++", "-std=c++11", "-x", "c++", *flags, "-o", str(tmp_path / "cxx.o")], check=True)
+    lib = capi.library_path() if os.path.exists(capi.library_path()) else capi.load()._name
+    exe = str(tmp_path / "abi")
+    subprocess.run(["gcc", "-std=c99", "-I", inc, str(src), lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", exe],
+                   check=True)
+    assert subprocess.run([exe]).returncode == 0
+
+
 def test_defaults_follow_reference():
     o = capi.Options()
     capi.load().cycas_options_default(C.byref(o))
